@@ -1,0 +1,334 @@
+#!/usr/bin/env python3
+"""Benchmark of the block-tensor permute + sector-GEMM path on GB300.
+
+Workload (one step): the iTEBD network of the spin-1/2 Heisenberg chain with
+U(1) symmetry, chi = 512 over charges -8..8, d = 2: La-A-Lb-B-Lc-gate
+contracted to theta[a,s1'|s2',c] through Network::launch (every pairwise
+contract permutes its operands and runs all its sector GEMMs in one grouped
+launch), inputs resident in HBM.  Metric: contract() TFLOP/s counted as the
+FP64-equivalent sum of 2*M*N*K over the sector GEMMs the reference issues for
+this network and ORDER (the same count in every precision mode).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--mode split|fp64|bf16|tf32]
+  python bench.py --impl reference ...   # the reference path on the host cores
+
+Under torchrun (N > 1) every rank runs an independent replica (no
+collective); rank 0 prints the single JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from trim_gb300 import workloads as wl  # noqa: E402
+
+METRIC = "contract() TFLOP/s (FP64-equivalent sector-GEMM flops), iTEBD chi=512 U(1) step"
+WORKLOAD = "itebd_u1_chi512_d2"
+L2_FLUSH_BYTES = 512 << 20  # > 129 MB L2: written between timed steps
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
+
+
+def itebd_inputs():
+    spec = wl.itebd()
+    rng = np.random.default_rng(spec["seed"])
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    return spec, els
+
+
+# ----------------------------------------------------------------- clocks
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, p[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- CPU reference
+def run_reference_steps(steps: int, warmup: int):
+    """The reference path on the host cores: the numpy restatement of
+    Network::launch with per-sector BLAS dgemm (the compiled reference does
+    not run on this machine's architecture)."""
+    from oracle import symtensor as st
+
+    spec, els = itebd_inputs()
+    ob = lambda bonds: [st.Bond.from_runs(t, [(st.Qnum(u, p, f), d) for (u, p, f, d) in runs]) for t, runs in bonds]
+    tens = {s.name: st.UniTensor(ob(s.bonds), s.labels, els[s.name]) for s in spec["tensors"]}
+    shapes = []
+    net = st.Network(text=spec["net"])
+    for s in spec["tensors"]:
+        net.put_tensor(s.name, tens[s.name])
+    net.launch(gemm=lambda a, b: (shapes.append(a.shape + (b.shape[1],)), a @ b)[1])
+    flops = sum(2.0 * m * k * n for m, k, n in shapes)
+
+    def step():
+        n = st.Network(text=spec["net"])
+        for s in spec["tensors"]:
+            n.put_tensor(s.name, tens[s.name])
+        return n.launch()
+
+    for _ in range(warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        step()
+    dt = (time.perf_counter() - t0) / steps
+    return flops, dt
+
+
+def reference_main(args, rank, world):
+    if rank != 0:
+        return
+    flops, dt = run_reference_steps(args.steps, args.warmup)
+    v = flops / dt / 1e12
+    cores = os.cpu_count()
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "TFLOP/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "chi": 512, "sectors": 17, "flops_per_step": flops, "mode": "fp64"},
+        "cpu_baseline": {"value": v, "unit": "TFLOP/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} full iTEBD network steps, numpy BLAS on {cores} host threads"},
+        "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+# ----------------------------------------------------------------- GPU arm
+def gpu_main(args, rank, local, world):
+    import torch
+
+    torch.cuda.set_device(local)
+    from trim_gb300 import uni10 as tu
+
+    stream = torch.cuda.Stream()
+    tu.set_stream(stream.cuda_stream)
+    spec, els = itebd_inputs()
+    names = [s.name for s in spec["tensors"]]
+    dev = {s.name: tu.UniTensor(s.bonds, s.labels, els[s.name]) for s in spec["tensors"]}
+    net = tu.Network(spec["net"])
+    mode = args.mode
+
+    def step():
+        for n in names:
+            net.put_tensor(n, dev[n])
+        return net.launch(mode)
+
+    # correctness against FP64 on the device (reported, checked in tests)
+    th64 = None
+    for _ in range(max(1, args.warmup)):
+        th = step()
+    ref_net = tu.Network(spec["net"])
+    for n in names:
+        ref_net.put_tensor(n, dev[n])
+    th64 = ref_net.launch("fp64").get_elem()
+    thm = th.get_elem()
+    err = float(np.linalg.norm(thm - th64) / np.linalg.norm(th64))
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = tu.launch_count()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))  # L2 flush between timed steps, outside the events
+            starts[k].record(stream)
+            step()
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    launches = (tu.launch_count() - l0) // args.steps
+    if world > 1:
+        torch.distributed.barrier()
+    dt_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
+    if world > 1:
+        t = torch.tensor([dt_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        dt_ms = float(t.item())
+
+    # per-kernel timing pass (events on the library stream around each launch)
+    tu.prof_enable(True)
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        step()
+    prof = tu.prof_read()
+    tu.prof_enable(False)
+    flops = sum(v["flops"] for k_, v in prof.items() if k_.startswith("gemm")) / args.steps
+    value = world * flops / (dt_ms * 1e-3) / 1e12
+
+    # end to end through the C ABI: pinned host inputs -> device, theta -> host
+    pinned = {n: torch.from_numpy(els[n]).pin_memory() for n in names}
+    out_host = torch.empty(th64.size, dtype=torch.float64).pin_memory()
+    h2d = sum(8 * els[n].size for n in names)
+    d2h = 8 * th64.size
+    torch.cuda.synchronize()
+    t0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    t1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e2e_ms = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        torch.cuda.synchronize()
+        w0 = time.perf_counter()
+        for n in names:
+            dev[n].set_elem_host_ptr(pinned[n].data_ptr(), els[n].size)
+            net.put_tensor(n, dev[n])
+        th = net.launch(mode)
+        tu.capi.call("tn_tensor_get_elem", th.h, out_host.data_ptr(), th64.size)
+        e2e_ms.append((time.perf_counter() - w0) * 1e3)
+    e2e_step = statistics.median(e2e_ms)
+    e2e_val = world * flops / (e2e_step * 1e-3) / 1e12
+
+    # roofline of the dominant kernel
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    peaks = {}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks = json.load(f)
+    except OSError:
+        pass
+    dname, d = dom
+    avg_ms = d["ms"] / d["launches"]
+    if dname == "permute":
+        ach = d["bytes"] / d["launches"] / (avg_ms * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"kernel": dname, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    elif dname.startswith("gemm_fp64"):
+        ach = d["flops"] / d["launches"] / (avg_ms * 1e-3) / 1e12
+        peak = 1.25
+        roof = {"kernel": dname, "bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "peak_source": "nominal FP64 rate (no measured FP64 figure)"}
+    else:
+        ach = d["flops"] / d["launches"] / (avg_ms * 1e-3) / 1e12
+        peak = peaks.get("bf16_tflops", 1900.0)
+        roof = {"kernel": dname, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+                "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
+    roof["avg_launch_ms"] = avg_ms
+    roof["traffic"] = None
+    kernels = {k_: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps} for k_, v in prof.items()}
+    pbytes = prof.get("permute", {}).get("bytes", 0.0)
+    pms = prof.get("permute", {}).get("ms", 0.0)
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        budget = args.cpu_seconds
+        n = 1
+        f_, dt1 = run_reference_steps(1, 1)
+        n = max(3, int(budget / max(dt1, 1e-4)))
+        f_, dtc = run_reference_steps(n, 0)
+        cpu = {"value": f_ / dtc / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"{n} full iTEBD network steps (the whole workload), numpy BLAS on {os.cpu_count()} host threads"}
+
+    if rank == 0:
+        print(json.dumps({
+            "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if mode == "fp64" else "f64 (bf16 slices on tcgen05)",
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "chi": 512, "sectors": 17, "mode": mode, "flops_per_step": flops,
+                       "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"},
+            "error_vs_fp64": err,
+            "permute": {"gb_s": (pbytes / (pms * 1e-3) / 1e9) if pms else None, "bytes_per_step": pbytes / args.steps},
+            "kernels": kernels,
+            "roofline": roof,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": "TFLOP/s", "ms_per_step": e2e_step, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "clocks": clk.summary(),
+            "gpu_launches": int(launches),
+        }))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="fp64", choices=["fp64", "split", "bf16", "tf32"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank, local, world = dist_env()
+    if args.impl == "reference":
+        reference_main(args, rank, world)
+        return
+    if world > 1:
+        import torch
+
+        torch.distributed.init_process_group("nccl")
+    gpu_main(args, rank, local, world)
+    if world > 1:
+        import torch
+
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

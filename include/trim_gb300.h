@@ -1,0 +1,168 @@
+/*
+ * trim_gb300 -- C ABI of the GB300 (sm_103a) symmetric block-tensor
+ * permute + sector-GEMM path.
+ *
+ * Every entry point is extern "C", takes plain pointers and sizes, never
+ * throws, and returns an int status (TN_OK == 0).  tn_last_error() gives the
+ * message of the last failure on the calling thread, worded like the
+ * reference's exceptions.
+ *
+ * Two levels:
+ *  - kernel level: sector maps, permute and grouped sector GEMMs on device
+ *    buffers the caller owns;
+ *  - tensor level: handles mirroring the reference's UniTensor / Network
+ *    operations (what the reference's SWIG binding, pyUni10, wraps), with the
+ *    element buffer resident in HBM and host copies only at set/get.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   uni10/src/uni10/tensor-network/UniTensor.h, Network.h, lib/UniTensorReal.cpp,
+ *   lib/UniTensorTools.cpp, lib/Network.cpp, numeric/lapack/lib/uni10_lapack_cpu.cpp.
+ *
+ * Bond signatures are passed as parallel arrays: bond b has type btype[b]
+ * (+1 = BD_IN, -1 = BD_OUT) and nq[b] charge runs; the runs of all bonds are
+ * packed in order, run r having Qnum (qnum[3r], qnum[3r+1], qnum[3r+2]) =
+ * (U1, parity, fermionic parity) and degeneracy deg[r] -- the run-length
+ * form (Qnums, Qdegs) of uni10::Bond (data-structure/Bond.h:175-179).
+ */
+#ifndef TRIM_GB300_H
+#define TRIM_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  TN_OK = 0,
+  TN_ERR_ARG = 1,         /* bad argument (std::runtime_error in the reference) */
+  TN_ERR_OOM = 2,         /* device allocation failed */
+  TN_ERR_TIMEOUT = 3,     /* a bounded device wait gave up */
+  TN_ERR_CUDA = 4,        /* CUDA runtime / library error */
+  TN_ERR_SHAPE = 5,       /* dimension mismatch between contracted bonds/blocks */
+  TN_ERR_LABEL = 6,       /* labels do not correspond */
+  TN_ERR_UNSUPPORTED = 7, /* valid in the reference, not supported here */
+  TN_ERR_NOBLOCK = 8,     /* no symmetry block with the given bonds */
+  TN_ERR_FILE = 9         /* file could not be opened/parsed */
+};
+
+/* ---- precision of the sector GEMMs ------------------------------------- */
+enum {
+  TN_MODE_FP64 = 0,      /* plain FP64 GEMM per sector: the drop-in form */
+  TN_MODE_SPLIT = 1,     /* split-precision: BF16 slices on tcgen05, FP64-level error */
+  TN_MODE_FAST_BF16 = 2, /* one BF16 slice, FP32 accumulation */
+  TN_MODE_FAST_TF32 = 3  /* TF32 operands, FP32 accumulation */
+};
+
+typedef struct tn_ctx_s* tn_ctx_t;
+typedef struct tn_smap_s* tn_smap_t;
+typedef struct tn_tensor_s* tn_tensor_t;
+typedef struct tn_network_s* tn_network_t;
+
+/* One sector GEMM of a contraction: C[M x N] = A[M x K] . B[K x N], all
+ * row-major and dense (ld = K, N, N), at element offsets into the A, B, C
+ * base buffers.  Replaces matrixMul (numeric/lapack/lib/uni10_lapack_cpu.cpp:41-44)
+ * called per matching Qnum in contract (tensor-network/lib/UniTensorTools.cpp:191-203). */
+typedef struct {
+  int64_t M, N, K;
+  int64_t a_off, b_off, c_off;
+} tn_sector_gemm;
+
+/* ---- errors / version -------------------------------------------------- */
+const char* tn_last_error(void);
+int tn_version(void);
+
+/* ---- context: device, stream, memory pool ------------------------------
+ * Replaces the reference's global device mode (guni10_create,
+ * tools/lib/uni10_tools_gpu.cu:7-66) with an explicit context. */
+int tn_ctx_create(int device, tn_ctx_t* ctx);
+int tn_ctx_destroy(tn_ctx_t ctx);
+int tn_ctx_set_stream(tn_ctx_t ctx, void* cuda_stream);
+int tn_ctx_sync(tn_ctx_t ctx);
+/* number of kernels this context has launched (for launch accounting) */
+int tn_ctx_launch_count(tn_ctx_t ctx, int64_t* count);
+/* Per-kernel timing: when enabled, every kernel launch of the context is
+ * bracketed by CUDA events on the context's stream.  tn_prof_read syncs and
+ * returns, per kernel name (32-byte slots in names), the summed elapsed ms,
+ * launch count and algorithmic bytes/flops; enabling again clears them. */
+int tn_prof_enable(tn_ctx_t ctx, int on);
+int tn_prof_read(tn_ctx_t ctx, int cap, char* names, double* ms, int64_t* launches, double* bytes, double* flops,
+                 int* n);
+
+/* ---- sector map (UniTensor::grouping, tensor-network/lib/UniTensorReal.cpp:1169-1321)
+ * Built once per bond signature and cached, host and device copies. */
+int tn_sectormap_build(tn_ctx_t ctx, int nbonds, const int* btype, const int* nq, const int* qnum,
+                       const int* deg, tn_smap_t* out);
+int tn_sectormap_query(tn_smap_t m, int64_t* elem_num, int* nblocks, int* rbond_num);
+/* block list in Qnum order: qnum[3*i..], rows[i], cols[i], offset[i] (elements) */
+int tn_sectormap_blocks(tn_smap_t m, int* qnum, int64_t* rows, int64_t* cols, int64_t* offset);
+int tn_sectormap_destroy(tn_smap_t m);
+
+/* ---- permute data movement (UniTensor::permute, UniTensorReal.cpp:532-768)
+ * dst must be the sector map of the permuted bonds: out bond b is in bond
+ * rsp[b], changed to IN for b < dst's row-bond count and to OUT otherwise.
+ * src_elem/dst_elem are device buffers of elem_num doubles.  Bit-exact. */
+int tn_permute(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_elem,
+               double* dst_elem);
+
+/* Host-side check of a permute plan: runs the kernel's tile decode and walk
+ * on the CPU over host buffers, checking every offset against the element
+ * count and that each destination element is written once.  No GPU needed;
+ * it is how a plan is checked before its first device run. */
+int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host, double* dst_host,
+                          int64_t* written);
+
+/* ---- grouped sector GEMMs (contract's per-sector matrixMul) ------------
+ * All n sector GEMMs in one launch; list is a host array.  A, B, C device. */
+int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A,
+                        const double* B, double* C);
+
+/* ---- tensor level (UniTensor, tensor-network/UniTensor.h) -------------- */
+/* UniTensor(const std::vector<Bond>&, const std::string& name) (UniTensor.h:326) */
+int tn_tensor_create(tn_ctx_t ctx, int nbonds, const int* btype, const int* nq, const int* qnum,
+                     const int* deg, tn_tensor_t* out);
+int tn_tensor_destroy(tn_tensor_t t);
+/* copy constructor (deep copy, UniTensor.cpp:236-305) */
+int tn_tensor_copy(tn_tensor_t t, tn_tensor_t* out);
+/* setElem(const Real*, bool ongpu=false) / host read-back of getElem() */
+int tn_tensor_set_elem(tn_tensor_t t, const double* host, int64_t n);
+int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n);
+/* device-resident element buffer (getElem() on a device build) */
+int tn_tensor_device_elem(tn_tensor_t t, double** dev, int64_t* n);
+int tn_tensor_set_elem_device(tn_tensor_t t, const double* dev, int64_t n);
+int tn_tensor_set_label(tn_tensor_t t, int n, const int* labels);
+int tn_tensor_get_labels(tn_tensor_t t, int* labels, int* n);
+/* bond signature of the tensor (same packing as tn_tensor_create); sizes in/out */
+int tn_tensor_bonds(tn_tensor_t t, int* nbonds, int* btype, int* nq, int* qnum, int* deg, int cap_runs);
+int tn_tensor_sectormap(tn_tensor_t t, tn_smap_t* m);
+/* permute(const std::vector<int>& newLabels, int inBondNum) (UniTensor.h:583) */
+int tn_tensor_permute(tn_tensor_t t, int n, const int* new_labels, int in_bond_num);
+/* transpose() (UniTensor.h:576) */
+int tn_tensor_transpose(tn_tensor_t t);
+/* combineBond(const std::vector<int>&) (UniTensor.h:619) */
+int tn_tensor_combine_bond(tn_tensor_t t, int n, const int* labels);
+/* contract(Ta, Tb, fast) (UniTensor.h:605; UniTensorTools.cpp:124-244);
+ * mutates a and b like the reference (restored unless fast). */
+int tn_contract(tn_tensor_t a, tn_tensor_t b, int fast, int mode, tn_tensor_t* out);
+/* otimes(Ta, Tb) (UniTensorTools.cpp:246-273) */
+int tn_otimes(tn_tensor_t a, tn_tensor_t b, int mode, tn_tensor_t* out);
+/* multiply every element by a (operator*=(Real), UniTensor.h:262) */
+int tn_tensor_scale(tn_tensor_t t, double a);
+
+/* ---- network (Network.h:67-233, lib/Network.cpp) ------------------------ */
+/* Network(const std::string& fname) -- text is the content of a .net file */
+int tn_network_create(tn_ctx_t ctx, const char* net_text, tn_network_t* out);
+int tn_network_destroy(tn_network_t net);
+/* putTensor(const std::string& name, const UniTensor&, bool force=true) */
+int tn_network_put_tensor(tn_network_t net, const char* name, tn_tensor_t t);
+/* launch(const std::string& name="") */
+int tn_network_launch(tn_network_t net, int mode, tn_tensor_t* out);
+/* the contraction tree as a bracket string, e.g. "((A B) C)" */
+int tn_network_tree(tn_network_t net, char* buf, int cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TRIM_GB300_H */

@@ -1,0 +1,120 @@
+// uni10::UniTensor -- drop-in for the reference's tensor-network/UniTensor.h
+// (UniTensor.h:58-970) on the permute / contract path.  The element buffer is
+// one device allocation (HBM) laid out exactly as the reference lays it out:
+// blocks back to back in ascending Qnum order, each row-major
+// (tensor-network/lib/UniTensorReal.cpp:1365-1374), so getElem(), at() and
+// save() match the reference element for element.
+#ifndef TRIM_UNI10_UNITENSOR_H
+#define TRIM_UNI10_UNITENSOR_H
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "Bond.h"
+#include "Matrix.h"
+#include "Qnum.h"
+
+namespace tn {
+struct SectorMap;
+struct DevBuf;
+}  // namespace tn
+
+namespace uni10 {
+
+// Precision of contract()'s sector GEMMs (process-wide default, per thread).
+// TN_MODE_* values of trim_gb300.h: 0 FP64 (the drop-in), 1 split precision
+// on the tensor cores, 2 BF16 fast, 3 TF32 fast.
+void setContractMode(int mode);
+int contractMode();
+
+class UniTensor {
+ public:
+  UniTensor();
+  explicit UniTensor(double val);
+  UniTensor(const std::vector<Bond>& _bonds, const std::string& _name = "");
+  UniTensor(const std::vector<Bond>& _bonds, std::vector<int>& labels, const std::string& _name = "");
+  UniTensor(const std::vector<Bond>& _bonds, int* labels, const std::string& _name = "");
+  UniTensor(const UniTensor& UniT);
+  explicit UniTensor(const std::string& fname);  // UniTensor::save layout (UniTensor.cpp:486-583)
+  UniTensor& operator=(const UniTensor& UniT);
+  ~UniTensor();
+
+  // elements
+  void setElem(const double* elem, bool _ongpu = false);
+  void setElem(const std::vector<double>& elem, bool _ongpu = false);
+  double* getElem();               // device pointer
+  std::vector<double> hostElem() const;
+  double at(size_t idx) const;
+  double operator[](size_t idx) const { return at(idx); }
+  void set_zero();
+  void setRawElem(const std::vector<double>& rawElem);  // dense -> blocks (UniTensorReal.cpp:96-174)
+  std::vector<double> getRawElem() const;               // blocks -> dense (UniTensorReal.cpp:241-280)
+
+  // labels / bonds / blocks
+  void setLabel(const int newLabel, const size_t idx);
+  void setLabel(const std::vector<int>& newLabels);
+  void setLabel(int* newLabels);
+  std::vector<int> label() const { return labels; }
+  int label(size_t idx) const { return labels.at(idx); }
+  void setName(const std::string& _name) { name = _name; }
+  std::string getName() const { return name; }
+  size_t bondNum() const { return bonds.size(); }
+  size_t inBondNum() const { return RBondNum; }
+  std::vector<Bond> bond() const { return bonds; }
+  Bond bond(size_t idx) const { return bonds.at(idx); }
+  size_t elemNum() const { return m_elemNum; }
+  size_t blockNum() const;
+  std::vector<Qnum> blockQnum() const;
+  Qnum blockQnum(size_t idx) const;
+  Matrix getBlock(bool diag = false) const;
+  Matrix getBlock(const Qnum& qnum, bool diag = false) const;
+  void putBlock(const Block& mat);
+  void putBlock(const Qnum& qnum, const Block& mat);
+
+  // the hot path
+  UniTensor& permute(const std::vector<int>& newLabels, int inBondNum);
+  UniTensor& permute(int* newLabels, int inBondNum);
+  UniTensor& permute(int inBondNum);
+  UniTensor& transpose();
+  UniTensor& combineBond(const std::vector<int>& combined_labels);
+  friend UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast);
+  friend UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
+
+  UniTensor& operator*=(double a);
+  friend UniTensor operator*(const UniTensor& Ta, double a);
+  friend UniTensor operator*(double a, const UniTensor& Ta);
+  friend UniTensor operator*(const UniTensor& Ta, const UniTensor& Tb);
+  UniTensor& operator*=(const UniTensor& Tb);
+
+  void save(const std::string& fname) const;  // UniTensor.cpp:922-986
+  // the cached sector map of this tensor's bonds (internal)
+  const tn::SectorMap* sectorMap() const { return smap.get(); }
+
+  friend class Network;
+  friend class Node;
+
+ private:
+  struct NoFill {};
+  UniTensor(const std::vector<Bond>& _bonds, const std::string& _name, NoFill);
+  void initUniT(bool zero = true);
+  std::string name;
+  std::vector<Bond> bonds;
+  std::vector<int> labels;
+  int RBondNum = 0;
+  size_t m_elemNum = 0;
+  int status = 0;
+  std::shared_ptr<const tn::SectorMap> smap;
+  std::shared_ptr<tn::DevBuf> elem;
+  static const int HAVEBOND = 1;
+  static const int HAVEELEM = 2;
+};
+
+UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast = false);
+UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
+UniTensor operator*(const UniTensor& Ta, double a);
+UniTensor operator*(double a, const UniTensor& Ta);
+UniTensor operator*(const UniTensor& Ta, const UniTensor& Tb);
+
+}  // namespace uni10
+#endif

@@ -1,0 +1,93 @@
+"""C-ABI checks that need no GPU: the library loads and exports every symbol
+the header declares, sector maps equal the oracle's grouping, and every
+permute plan -- the kernel's own tile decode and walk, run on the CPU --
+moves the elements exactly as the reference does."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import symtensor as st
+from tests import golden_data as G
+from trim_gb300 import capi, workloads as wl
+from trim_gb300 import uni10 as tu
+
+
+def to_bonds(spec_bonds):
+    return [st.Bond.from_runs(t, [(st.Qnum(u, p, f), d) for (u, p, f, d) in runs]) for t, runs in spec_bonds]
+
+
+def test_exports_every_header_symbol():
+    L = capi.lib()
+    names = capi.header_symbols()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    assert capi.lib().tn_version() >= 100
+
+
+def _sectormap_matches(bonds):
+    ours = tu.SectorMap(bonds)
+    ora = st.grouping(to_bonds(bonds))
+    assert ours.elem_num == ora.elem_num
+    got = ours.blocks()
+    want = [((q.u1, q.prt, q.prtf), r, c, off) for (q, r, c, off) in ora.blocks]
+    assert got == want
+
+
+PERM = [c for c in G.cases().values() if c["kind"] == "permute"]
+
+
+@pytest.mark.parametrize("case", PERM, ids=[c["id"] for c in PERM])
+def test_sectormap_and_permute_plan_match_reference(case):
+    bonds = G.bonds_of(case["T"])
+    _sectormap_matches(bonds)
+    src = tu.SectorMap(bonds)
+    # destination bonds as permute builds them (UniTensorReal.cpp:568-580)
+    labels, new = case["T"]["labels"], case["new_labels"]
+    rsp = [labels.index(l) for l in new]
+    out = [wl.change(bonds[rsp[b]], 1 if b < case["rownum"] else -1) for b in range(len(bonds))]
+    dst = tu.SectorMap(out)
+    x = G.arr(case["id"], "T")
+    got, written = tu.plan_check_permute(src, dst, rsp, x)
+    assert written == x.size
+    assert np.array_equal(got, G.arr(case["id"], "P"))
+
+
+def test_permute_plans_of_workloads_bit_exact():
+    rng = np.random.default_rng(7)
+    # workload 1's permute, the iTEBD tensors' contract permutes, MERA chi=6
+    cases = []
+    w1 = wl.u1_rank4()
+    cases.append((w1["tensors"][0].bonds, [0, 1, 2, 3], [0, 1, 3, 2], 2))
+    it = wl.itebd()
+    A = it["tensors"][1]
+    cases.append((A.bonds, [10, 1, 11], [1, 11, 10], 1))
+    cases.append((A.bonds, [10, 1, 11], [11, 10, 1], 2))
+    m = wl.mera(chi=6)
+    O = m["tensors"][3]
+    cases.append((O.bonds, [0, 1, 2, 3, 4, 5], [4, 5, 0, 1, 2, 3], 2))
+    cases.append((O.bonds, [0, 1, 2, 3, 4, 5], [5, 3, 1, 0, 2, 4], 3))
+    for bonds, labels, new, rn in cases:
+        x = rng.uniform(-1, 1, wl.elem_count(bonds))
+        t = st.UniTensor(to_bonds(bonds), labels, x)
+        t.permute(new, rn)
+        rsp = [labels.index(l) for l in new]
+        out = [wl.change(bonds[rsp[b]], 1 if b < rn else -1) for b in range(len(bonds))]
+        got, written = tu.plan_check_permute(tu.SectorMap(bonds), tu.SectorMap(out), rsp, x)
+        assert written == x.size
+        assert np.array_equal(got, t.elem)
+
+
+def test_errors_are_statuses():
+    with pytest.raises(capi.TnError) as e:
+        tu.SectorMap([(1, [(1, 0, 0, 2)]), (-1, [(0, 0, 0, 2)])])  # no common charge
+    assert e.value.code == 8
+    with pytest.raises(capi.TnError) as e:
+        tu.SectorMap([(-1, [(0, 0, 0, 2)]), (1, [(0, 0, 0, 2)])])  # IN after OUT
+    assert e.value.code == 1
+    assert "BD_OUT bonds must be placed after all BD_IN bonds" in str(e.value)
+    with pytest.raises(capi.TnError):
+        tu.SectorMap([(1, [(1000, 0, 0, 2)])])  # U1 out of range
+    with pytest.raises(capi.TnError):
+        tu.SectorMap([(2, [(0, 0, 0, 2)])])  # bad type

@@ -1,0 +1,196 @@
+"""GPU parity: the CUDA path through the C ABI against the reference's golden
+outputs and the CPU oracle.  Bit-exact for permute/transpose (pure data
+movement); FP64 contraction within 1e-13 relative Frobenius error."""
+import hashlib
+
+import numpy as np
+import pytest
+
+from oracle import symtensor as st
+from tests import golden_data as G
+from trim_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+FP64_TOL = 1e-13
+
+
+@pytest.fixture(scope="module")
+def tu():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from trim_gb300 import uni10 as tu
+
+    return tu
+
+
+def sha(a):
+    return hashlib.sha256(np.ascontiguousarray(a, dtype="<f8").tobytes()).hexdigest()
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def to_obonds(spec_bonds):
+    return [st.Bond.from_runs(t, [(st.Qnum(u, p, f), d) for (u, p, f, d) in runs]) for t, runs in spec_bonds]
+
+
+PERM = [c for c in G.cases().values() if c["kind"] == "permute"]
+CON = [c for c in G.cases().values() if c["kind"] == "contract"]
+
+
+@pytest.mark.parametrize("case", PERM, ids=[c["id"] for c in PERM])
+def test_permute_transpose_bit_exact(tu, case):
+    t = tu.UniTensor(G.bonds_of(case["T"]), case["T"]["labels"], G.arr(case["id"], "T"))
+    t.permute(case["new_labels"], case["rownum"])
+    assert [[b[0], [list(r) for r in b[1]]] for b in t.bonds()] == case["out"]["bonds"]
+    assert t.labels() == case["out"]["labels"]
+    assert sha(t.get_elem()) == case["out"]["sha256"]
+    t.transpose()
+    assert np.array_equal(t.get_elem(), G.arr(case["id"], "PT"))
+
+
+@pytest.mark.parametrize("case", CON, ids=[c["id"] for c in CON])
+def test_contract_fp64(tu, case):
+    a = tu.UniTensor(G.bonds_of(case["A"]), case["A"]["labels"], G.arr(case["id"], "A"))
+    b = tu.UniTensor(G.bonds_of(case["B"]), case["B"]["labels"], G.arr(case["id"], "B"))
+    c = tu.contract(a, b, fast=False, mode="fp64")
+    assert [[x[0], [list(r) for r in x[1]]] for x in c.bonds()] == case["out"]["bonds"]
+    assert c.labels() == case["out"]["labels"]
+    assert rel(c.get_elem(), G.arr(case["id"], "C")) <= FP64_TOL
+    # fast=false restores the operands bit for bit
+    assert np.array_equal(a.get_elem(), G.arr(case["id"], "A"))
+    assert a.labels() == case["A"]["labels"]
+
+
+def test_workload1_permute_and_contract(tu):
+    c = G.cases()["u1_rank4"]
+    spec = wl.u1_rank4()
+    A, B = spec["tensors"]
+    ta = tu.UniTensor(A.bonds, A.labels, G.arr("u1_rank4", "A"))
+    tb = tu.UniTensor(B.bonds, B.labels, G.arr("u1_rank4", "B"))
+    ta.permute([0, 1, 3, 2], 2)
+    assert sha(ta.get_elem()) == c["PA"]["sha256"]
+    tc = tu.contract(ta, tb, mode="fp64")
+    assert rel(tc.get_elem(), G.arr("u1_rank4", "C")) <= FP64_TOL
+
+
+def _itebd_inputs():
+    spec = wl.itebd()
+    rng = np.random.default_rng(spec["seed"])
+    return spec, {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+
+
+def test_itebd_network_fp64(tu):
+    c = G.cases()["itebd"]
+    spec, els = _itebd_inputs()
+    assert {k: sha(v) for k, v in els.items()} == c["inputs_sha"]
+    net = tu.Network(spec["net"])
+    ts = {}
+    for s in spec["tensors"]:
+        ts[s.name] = tu.UniTensor(s.bonds, s.labels, els[s.name])
+        net.put_tensor(s.name, ts[s.name])
+    th = net.launch(mode="fp64")
+    assert [[x[0], [list(r) for r in x[1]]] for x in th.bonds()] == c["TH"]["bonds"]
+    assert th.labels() == c["TH"]["labels"]
+    assert rel(th.get_elem(), G.arr("itebd", "TH")) <= FP64_TOL
+    assert net.tree() == "(((((La A) Lb) B) Lc) U)"
+
+
+def test_greedy_network_tree_and_values(tu):
+    c = G.cases()["greedy_net"]
+    net = tu.Network(c["net"])
+    keep = []
+    for n, meta in c["tensors"].items():
+        t = tu.UniTensor(G.bonds_of(meta), meta["labels"], G.arr("greedy_net", n))
+        keep.append(t)
+        net.put_tensor(n, t)
+    onet = st.Network(text=c["net"])
+    for n, meta in c["tensors"].items():
+        onet.put_tensor(n, st.UniTensor(to_obonds(G.bonds_of(meta)), meta["labels"], G.arr("greedy_net", n)))
+    r = net.launch(mode="fp64")
+    assert rel(r.get_elem(), G.arr("greedy_net", "R")) <= FP64_TOL
+
+
+def test_batched_small_fp64(tu):
+    c = G.cases()["batched_small"]
+    spec = wl.batched(**c["params"])
+    for i, (t1, t2) in enumerate(spec["pairs"]):
+        a = tu.UniTensor(t1.bonds, t1.labels, G.arr("batched_small", t1.name))
+        b = tu.UniTensor(t2.bonds, t2.labels, G.arr("batched_small", t2.name))
+        r = tu.contract(a, b, mode="fp64")
+        assert rel(r.get_elem(), G.arr("batched_small", f"C{i}")) <= FP64_TOL
+
+
+def test_mera_small_fp64(tu):
+    c = G.cases()["mera_small"]
+    spec = wl.mera(**c["params"])
+    rng = np.random.default_rng(0)
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    for dname, netx in spec["nets"].items():
+        net = tu.Network(netx)
+        keep = []
+        for s in spec["tensors"]:
+            t = tu.UniTensor(s.bonds, s.labels, els[s.name])
+            keep.append(t)
+            net.put_tensor(s.name, t)
+        r = net.launch(mode="fp64")
+        assert rel(r.get_elem(), G.arr("mera_small", dname)) <= FP64_TOL
+
+
+def test_ipeps_small_double_layer_and_quadrant(tu):
+    c = G.cases()["ipeps_small"]
+    spec = wl.ipeps_ctm(**c["params"])
+    site, C_, T1, T2 = spec["tensors"]
+    a = tu.UniTensor(site.bonds, site.labels, G.arr("ipeps_small", "a"))
+    ac = a.copy()
+    ac.set_label([0, 11, 12, 13, 14])
+    aa = tu.contract(a, ac, mode="fp64")
+    for x in (1, 2, 3, 4):
+        aa.combine_bond([x, x + 10])
+    aa.permute(aa.labels(), 2)
+    assert [[x[0], [list(r) for r in x[1]]] for x in aa.bonds()] == c["AA"]["bonds"]
+    assert rel(aa.get_elem(), G.arr("ipeps_small", "AA")) <= FP64_TOL
+    aa.set_label([10, 20, 30, 40])
+    net = tu.Network(spec["net"])
+    keep = [aa]
+    for s in (C_, T1, T2):
+        t = tu.UniTensor(s.bonds, s.labels, G.arr("ipeps_small", s.name))
+        keep.append(t)
+        net.put_tensor(s.name, t)
+    net.put_tensor("A2", aa)
+    q = net.launch(mode="fp64")
+    assert rel(q.get_elem(), G.arr("ipeps_small", "Q")) <= FP64_TOL
+
+
+def test_large_dense_permute_bit_exact(tu):
+    """A chi=20 rank-6 dense tensor (64M elements): the transpose-mode tiles."""
+    chi = 20
+    bonds = [wl.dense_bond(1, chi)] * 3 + [wl.dense_bond(-1, chi)] * 3
+    rng = np.random.default_rng(3)
+    x = rng.standard_normal(chi ** 6)
+    t = tu.UniTensor(bonds, list(range(6)), x)
+    t.permute([4, 5, 0, 1, 2, 3], 2)
+    want = x.reshape([chi] * 6).transpose(4, 5, 0, 1, 2, 3).ravel()
+    assert np.array_equal(t.get_elem(), want)
+    t.permute([2, 0, 5, 4, 1, 3], 3)  # labels now (4,5,0,1,2,3) -> arbitrary order
+    want2 = want.reshape([chi] * 6)
+    cur = [4, 5, 0, 1, 2, 3]
+    want2 = want2.transpose([cur.index(l) for l in [2, 0, 5, 4, 1, 3]]).ravel()
+    assert np.array_equal(t.get_elem(), want2)
+
+
+def test_errors_on_device_path(tu):
+    from trim_gb300 import capi
+
+    a = tu.UniTensor([wl.dense_bond(1, 3), wl.dense_bond(-1, 4)], [1, 2], np.ones(12))
+    b = tu.UniTensor([wl.dense_bond(1, 5), wl.dense_bond(-1, 4)], [2, 3], np.ones(20))
+    with pytest.raises(capi.TnError) as e:
+        tu.contract(a, b)
+    assert "Cannot contract two bonds having different dimensions" in str(e.value)
+    with pytest.raises(capi.TnError) as e:
+        a.permute([1, 9], 1)
+    assert "do not 1-1 correspond" in str(e.value)

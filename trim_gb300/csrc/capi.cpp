@@ -1,0 +1,460 @@
+// extern "C" boundary of trim_gb300 (include/trim_gb300.h).  Every entry
+// point catches all exceptions and returns a status; the message is kept for
+// tn_last_error().
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <tuple>
+#include <memory>
+#include <sstream>
+
+#include "../../include/trim_gb300.h"
+#include "../../include/uni10.hpp"
+#include "engine/engine.h"
+
+namespace uni10 {
+std::vector<tn::BondSig> to_sigs(const std::vector<Bond>& bonds);
+}
+namespace tn {
+Ctx* create_ctx(int device);
+}
+
+struct tn_smap_s {
+  tn::SectorMapP m;
+};
+struct tn_tensor_s {
+  uni10::UniTensor t;
+};
+struct tn_network_s {
+  std::unique_ptr<uni10::Network> net;
+};
+
+namespace {
+
+template <class F>
+int guard(F&& f) {
+  try {
+    f();
+    return TN_OK;
+  } catch (const tn::Error& e) {
+    tn::set_last_error(e.what());
+    return e.code;
+  } catch (const std::bad_alloc& e) {
+    tn::set_last_error("host allocation failed");
+    return TN_ERR_OOM;
+  } catch (const std::exception& e) {
+    std::string m = e.what();
+    tn::set_last_error(m);
+    if (m.find("label") != std::string::npos) return TN_ERR_LABEL;
+    if (m.find("dimension") != std::string::npos) return TN_ERR_SHAPE;
+    if (m.find("no symmetry block") != std::string::npos) return TN_ERR_NOBLOCK;
+    if (m.find("file") != std::string::npos) return TN_ERR_FILE;
+    return TN_ERR_ARG;
+  } catch (...) {
+    tn::set_last_error("unknown error");
+    return TN_ERR_ARG;
+  }
+}
+
+void need(const void* p, const char* what) {
+  if (!p) tn::fail(TN_ERR_ARG, std::string("null argument: ") + what);
+}
+
+std::vector<uni10::Bond> make_bonds(int nbonds, const int* btype, const int* nq, const int* qnum, const int* deg) {
+  std::vector<tn::BondSig> sig = tn::unpack_bonds(nbonds, btype, nq, qnum, deg);
+  std::vector<uni10::Bond> bonds;
+  for (const auto& s : sig) {
+    std::vector<uni10::Qnum> ql;
+    for (size_t i = 0; i < s.q.size(); i++)
+      for (int d = 0; d < s.deg[i]; d++)
+        ql.push_back(uni10::Qnum((uni10::parityFType)s.q[i].prtf, s.q[i].u1, (uni10::parityType)s.q[i].prt));
+    bonds.push_back(uni10::Bond((uni10::bondType)s.type, ql));
+  }
+  return bonds;
+}
+
+// run a tensor-level operation with this call's precision mode
+struct ModeScope {
+  int old;
+  explicit ModeScope(int m) : old(uni10::contractMode()) { uni10::setContractMode(m); }
+  ~ModeScope() { uni10::setContractMode(old); }
+};
+
+}  // namespace
+
+extern "C" {
+
+const char* tn_last_error(void) { return tn::last_error(); }
+int tn_version(void) { return 100; }
+
+int tn_ctx_create(int device, tn_ctx_t* ctx) {
+  return guard([&] {
+    need(ctx, "ctx");
+    *ctx = reinterpret_cast<tn_ctx_t>(tn::create_ctx(device));
+  });
+}
+
+int tn_ctx_destroy(tn_ctx_t ctx) {
+  return guard([&] {
+    if (!ctx) return;
+    tn::Ctx* c = tn::as_ctx(ctx);
+    cudaStreamSynchronize(c->stream);
+    c->perm_cache.clear();
+    c->workspace.reset();
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    delete c;
+  });
+}
+
+int tn_ctx_set_stream(tn_ctx_t ctx, void* stream) {
+  return guard([&] {
+    tn::Ctx* c = tn::as_ctx(ctx);
+    TN_CUDA(cudaStreamSynchronize(c->stream));
+    if (c->own_stream) cudaStreamDestroy(c->stream);
+    c->stream = (cudaStream_t)stream;
+    c->own_stream = false;
+  });
+}
+
+int tn_ctx_sync(tn_ctx_t ctx) { return guard([&] { TN_CUDA(cudaStreamSynchronize(tn::as_ctx(ctx)->stream)); }); }
+
+int tn_ctx_launch_count(tn_ctx_t ctx, int64_t* count) {
+  return guard([&] {
+    need(count, "count");
+    *count = tn::as_ctx(ctx)->launches;
+  });
+}
+
+int tn_prof_enable(tn_ctx_t ctx, int on) {
+  return guard([&] {
+    tn::Ctx* c = tn::as_ctx(ctx);
+    TN_CUDA(cudaStreamSynchronize(c->stream));
+    for (auto& r : c->prof_recs) {
+      cudaEventDestroy(r.start);
+      cudaEventDestroy(r.stop);
+    }
+    c->prof_recs.clear();
+    c->prof = on != 0;
+  });
+}
+
+int tn_prof_read(tn_ctx_t ctx, int cap, char* names, double* ms, int64_t* launches, double* bytes, double* flops,
+                 int* n) {
+  return guard([&] {
+    tn::Ctx* c = tn::as_ctx(ctx);
+    TN_CUDA(cudaStreamSynchronize(c->stream));
+    std::vector<std::string> keys;
+    std::map<std::string, std::tuple<double, int64_t, double, double>> agg;
+    for (auto& r : c->prof_recs) {
+      float t = 0;
+      TN_CUDA(cudaEventElapsedTime(&t, r.start, r.stop));
+      auto& a = agg[r.name];
+      if (std::get<1>(a) == 0 && std::find(keys.begin(), keys.end(), r.name) == keys.end()) keys.push_back(r.name);
+      std::get<0>(a) += t;
+      std::get<1>(a) += 1;
+      std::get<2>(a) += r.bytes;
+      std::get<3>(a) += r.flops;
+    }
+    int k = 0;
+    for (const auto& name : keys) {
+      if (k >= cap) break;
+      auto& a = agg[name];
+      if (names) {
+        std::strncpy(names + 32 * k, name.c_str(), 31);
+        names[32 * k + 31] = 0;
+      }
+      if (ms) ms[k] = std::get<0>(a);
+      if (launches) launches[k] = std::get<1>(a);
+      if (bytes) bytes[k] = std::get<2>(a);
+      if (flops) flops[k] = std::get<3>(a);
+      k++;
+    }
+    if (n) *n = k;
+  });
+}
+
+// ---------------------------------------------------------------- sector maps
+int tn_sectormap_build(tn_ctx_t, int nbonds, const int* btype, const int* nq, const int* qnum, const int* deg,
+                       tn_smap_t* out) {
+  return guard([&] {
+    need(out, "out");
+    auto sig = tn::unpack_bonds(nbonds, btype, nq, qnum, deg);
+    auto m = tn::get_sectormap(sig);
+    if (m->blocks.empty()) tn::fail(TN_ERR_NOBLOCK, "There is no symmetry block with the given bonds");
+    *out = new tn_smap_s{m};
+  });
+}
+
+int tn_sectormap_query(tn_smap_t m, int64_t* elem_num, int* nblocks, int* rbond_num) {
+  return guard([&] {
+    need(m, "smap");
+    if (elem_num) *elem_num = m->m->elem_num;
+    if (nblocks) *nblocks = (int)m->m->blocks.size();
+    if (rbond_num) *rbond_num = m->m->rbond_num;
+  });
+}
+
+int tn_sectormap_blocks(tn_smap_t m, int* qnum, int64_t* rows, int64_t* cols, int64_t* offset) {
+  return guard([&] {
+    need(m, "smap");
+    const auto& bl = m->m->blocks;
+    for (size_t i = 0; i < bl.size(); i++) {
+      if (qnum) {
+        qnum[3 * i] = bl[i].q.u1;
+        qnum[3 * i + 1] = bl[i].q.prt;
+        qnum[3 * i + 2] = bl[i].q.prtf;
+      }
+      if (rows) rows[i] = bl[i].rows;
+      if (cols) cols[i] = bl[i].cols;
+      if (offset) offset[i] = bl[i].off;
+    }
+  });
+}
+
+int tn_sectormap_destroy(tn_smap_t m) {
+  return guard([&] { delete m; });
+}
+
+// ---------------------------------------------------------------- kernels
+int tn_permute(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_elem, double* dst_elem) {
+  return guard([&] {
+    need(src, "src");
+    need(dst, "dst");
+    need(rsp, "rsp");
+    tn::Ctx* c = tn::as_ctx(ctx);
+    std::vector<int> r(rsp, rsp + src->m->bonds.size());
+    auto plan = tn::get_perm_plan(*c, *src->m, *dst->m, r);
+    if (plan->elem_num > 0) {
+      need(src_elem, "src_elem");
+      need(dst_elem, "dst_elem");
+    }
+    tn::run_permute(*c, *plan, src_elem, dst_elem);
+  });
+}
+
+int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host, double* dst_host,
+                          int64_t* written) {
+  return guard([&] {
+    need(src, "src");
+    need(dst, "dst");
+    need(rsp, "rsp");
+    std::vector<int> r(rsp, rsp + src->m->bonds.size());
+    auto plan = tn::host_plan(tn::build_perm_subs(*src->m, *dst->m, r), src->m->elem_num);
+    int64_t w = tn::check_permute_plan_host(*plan, src_host, dst_host);
+    if (written) *written = w;
+  });
+}
+
+int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A, const double* B,
+                        double* C) {
+  return guard([&] {
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative sector count");
+    if (n == 0) return;
+    need(list, "list");
+    std::vector<tn_sector_gemm> l(list, list + n);
+    tn::run_sector_gemms(*tn::as_ctx(ctx), mode, l, A, B, C);
+  });
+}
+
+// ---------------------------------------------------------------- tensors
+int tn_tensor_create(tn_ctx_t, int nbonds, const int* btype, const int* nq, const int* qnum, const int* deg,
+                     tn_tensor_t* out) {
+  return guard([&] {
+    need(out, "out");
+    auto bonds = make_bonds(nbonds, btype, nq, qnum, deg);
+    *out = new tn_tensor_s{uni10::UniTensor(bonds)};
+  });
+}
+
+int tn_tensor_destroy(tn_tensor_t t) {
+  return guard([&] { delete t; });
+}
+
+int tn_tensor_copy(tn_tensor_t t, tn_tensor_t* out) {
+  return guard([&] {
+    need(t, "tensor");
+    need(out, "out");
+    *out = new tn_tensor_s{t->t};
+  });
+}
+
+int tn_tensor_set_elem(tn_tensor_t t, const double* host, int64_t n) {
+  return guard([&] {
+    need(t, "tensor");
+    if ((size_t)n != t->t.elemNum()) tn::fail(TN_ERR_ARG, "element count does not match the tensor");
+    need(host, "host");
+    t->t.setElem(host, false);
+  });
+}
+
+int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n) {
+  return guard([&] {
+    need(t, "tensor");
+    if ((size_t)n != t->t.elemNum()) tn::fail(TN_ERR_ARG, "element count does not match the tensor");
+    need(host, "host");
+    tn::Ctx* c = tn::default_ctx();
+    TN_CUDA(cudaMemcpyAsync(host, t->t.getElem(), n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    TN_CUDA(cudaStreamSynchronize(c->stream));
+  });
+}
+
+int tn_tensor_device_elem(tn_tensor_t t, double** dev, int64_t* n) {
+  return guard([&] {
+    need(t, "tensor");
+    if (dev) *dev = t->t.getElem();
+    if (n) *n = (int64_t)t->t.elemNum();
+  });
+}
+
+int tn_tensor_set_elem_device(tn_tensor_t t, const double* dev, int64_t n) {
+  return guard([&] {
+    need(t, "tensor");
+    if ((size_t)n != t->t.elemNum()) tn::fail(TN_ERR_ARG, "element count does not match the tensor");
+    t->t.setElem(dev, true);
+  });
+}
+
+int tn_tensor_set_label(tn_tensor_t t, int n, const int* labels) {
+  return guard([&] {
+    need(t, "tensor");
+    need(labels, "labels");
+    t->t.setLabel(std::vector<int>(labels, labels + n));
+  });
+}
+
+int tn_tensor_get_labels(tn_tensor_t t, int* labels, int* n) {
+  return guard([&] {
+    need(t, "tensor");
+    auto l = t->t.label();
+    if (n) *n = (int)l.size();
+    if (labels) std::memcpy(labels, l.data(), l.size() * sizeof(int));
+  });
+}
+
+int tn_tensor_bonds(tn_tensor_t t, int* nbonds, int* btype, int* nq, int* qnum, int* deg, int cap_runs) {
+  return guard([&] {
+    need(t, "tensor");
+    auto bonds = t->t.bond();
+    if (nbonds) *nbonds = (int)bonds.size();
+    int r = 0;
+    for (size_t b = 0; b < bonds.size(); b++) {
+      if (btype) btype[b] = bonds[b].type();
+      if (nq) nq[b] = (int)bonds[b].qnums().size();
+      for (size_t i = 0; i < bonds[b].qnums().size(); i++, r++) {
+        if (r >= cap_runs) continue;
+        const auto& q = bonds[b].qnums()[i];
+        if (qnum) {
+          qnum[3 * r] = q.U1();
+          qnum[3 * r + 1] = q.prt();
+          qnum[3 * r + 2] = q.prtF();
+        }
+        if (deg) deg[r] = bonds[b].qdegs()[i];
+      }
+    }
+    if (r > cap_runs) tn::fail(TN_ERR_ARG, "run capacity too small");
+  });
+}
+
+int tn_tensor_sectormap(tn_tensor_t t, tn_smap_t* m) {
+  return guard([&] {
+    need(t, "tensor");
+    need(m, "out");
+    *m = new tn_smap_s{tn::get_sectormap(uni10::to_sigs(t->t.bond()))};
+  });
+}
+
+int tn_tensor_permute(tn_tensor_t t, int n, const int* new_labels, int in_bond_num) {
+  return guard([&] {
+    need(t, "tensor");
+    need(new_labels, "labels");
+    t->t.permute(std::vector<int>(new_labels, new_labels + n), in_bond_num);
+  });
+}
+
+int tn_tensor_transpose(tn_tensor_t t) {
+  return guard([&] {
+    need(t, "tensor");
+    t->t.transpose();
+  });
+}
+
+int tn_tensor_combine_bond(tn_tensor_t t, int n, const int* labels) {
+  return guard([&] {
+    need(t, "tensor");
+    need(labels, "labels");
+    t->t.combineBond(std::vector<int>(labels, labels + n));
+  });
+}
+
+int tn_tensor_scale(tn_tensor_t t, double a) {
+  return guard([&] {
+    need(t, "tensor");
+    t->t *= a;
+  });
+}
+
+int tn_contract(tn_tensor_t a, tn_tensor_t b, int fast, int mode, tn_tensor_t* out) {
+  return guard([&] {
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    ModeScope ms(mode);
+    *out = new tn_tensor_s{uni10::contract(a->t, b->t, fast != 0)};
+  });
+}
+
+int tn_otimes(tn_tensor_t a, tn_tensor_t b, int mode, tn_tensor_t* out) {
+  return guard([&] {
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    ModeScope ms(mode);
+    *out = new tn_tensor_s{uni10::otimes(a->t, b->t)};
+  });
+}
+
+// ---------------------------------------------------------------- networks
+int tn_network_create(tn_ctx_t, const char* net_text, tn_network_t* out) {
+  return guard([&] {
+    need(net_text, "net_text");
+    need(out, "out");
+    auto n = std::make_unique<uni10::Network>(uni10::Network::fromText(net_text));
+    *out = new tn_network_s{std::move(n)};
+  });
+}
+
+int tn_network_destroy(tn_network_t net) {
+  return guard([&] { delete net; });
+}
+
+int tn_network_put_tensor(tn_network_t net, const char* name, tn_tensor_t t) {
+  return guard([&] {
+    need(net, "net");
+    need(name, "name");
+    need(t, "tensor");
+    net->net->putTensor(std::string(name), t->t);
+  });
+}
+
+int tn_network_launch(tn_network_t net, int mode, tn_tensor_t* out) {
+  return guard([&] {
+    need(net, "net");
+    need(out, "out");
+    ModeScope ms(mode);
+    *out = new tn_tensor_s{net->net->launch()};
+  });
+}
+
+int tn_network_tree(tn_network_t net, char* buf, int cap) {
+  return guard([&] {
+    need(net, "net");
+    std::string s = net->net->tree();
+    if (buf && cap > 0) {
+      std::strncpy(buf, s.c_str(), cap - 1);
+      buf[cap - 1] = 0;
+    }
+    if ((int)s.size() >= cap) tn::fail(TN_ERR_ARG, "buffer too small for the tree string");
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,210 @@
+// Internal engine of trim_gb300: device context, stream-ordered memory,
+// sector maps (UniTensor::grouping), permute and sector-GEMM plans, and the
+// launch interfaces of the CUDA kernels.  Not part of the public ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../../include/trim_gb300.h"
+
+namespace tn {
+
+// ---------------------------------------------------------------- errors
+// An Error carries one of the TN_ERR_* codes; the C ABI turns it into a
+// status and a message, the C++ API rethrows it as std::runtime_error.
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+[[noreturn]] void fail(int code, const std::string& msg);
+void cuda_check(cudaError_t e, const char* what);
+#define TN_CUDA(x) ::tn::cuda_check((x), #x)
+void set_last_error(const std::string& msg);
+const char* last_error();
+
+// ---------------------------------------------------------------- charges
+// Qnum (U1, parity, fermionic parity); order by key = U1*4 + prt*2 + prtF
+// (datatype/lib/Qnum.cpp:62-64, 100); fusion adds U1 and XORs parities
+// (Qnum.cpp:76-79).
+struct Q {
+  int u1 = 0, prt = 0, prtf = 0;
+  long key() const { return (long)u1 * 4 + prt * 2 + prtf; }
+  Q operator*(const Q& o) const { return Q{u1 + o.u1, prt ^ o.prt, prtf ^ o.prtf}; }
+  Q neg() const { return Q{-u1, prt, prtf}; }
+  bool operator==(const Q& o) const { return u1 == o.u1 && prt == o.prt && prtf == o.prtf; }
+  bool operator!=(const Q& o) const { return !(*this == o); }
+};
+struct QLess {
+  bool operator()(const Q& a, const Q& b) const { return a.key() < b.key(); }
+};
+
+// Run-length bond: type (+1 IN, -1 OUT), charges and degeneracies.
+struct BondSig {
+  int type = 1;
+  std::vector<Q> q;
+  std::vector<int> deg;
+  int64_t dim() const;
+  BondSig changed(int t) const;  // Bond::change (data-structure/lib/Bond.cpp:150-157)
+  bool operator==(const BondSig& o) const { return type == o.type && q == o.q && deg == o.deg; }
+};
+std::string sig_key(const std::vector<BondSig>& bonds);
+std::vector<BondSig> unpack_bonds(int nbonds, const int* btype, const int* nq, const int* qnum, const int* deg);
+
+// ---------------------------------------------------------------- sector map
+// The result of UniTensor::grouping (UniTensorReal.cpp:1169-1321) and
+// initBlocks (:1365-1374): blocks back to back in Qnum order, each row-major.
+struct SectorMap {
+  std::vector<BondSig> bonds;
+  int rbond_num = 0;
+  int64_t rqdim = 1, cqdim = 1;
+  struct Blk {
+    Q q;
+    int64_t rows, cols, off;
+  };
+  std::vector<Blk> blocks;
+  std::map<Q, int, QLess> block_of;  // charge -> block index
+  // per row Qnum-index tuple (odometer order): block, row offset in block,
+  // row extent; -1 where the tuple has no block
+  std::vector<int> rq2blk;
+  std::vector<int64_t> rq2off, rq2dim;
+  std::vector<int64_t> cq2off, cq2dim;  // per column tuple; -1 where absent
+  std::vector<int64_t> qidx_enc;        // valid sub-blocks r*cqdim+c, ascending
+  int64_t elem_num = 0;
+  std::string key;
+  int find_block(const Q& q) const {
+    auto it = block_of.find(q);
+    return it == block_of.end() ? -1 : it->second;
+  }
+};
+using SectorMapP = std::shared_ptr<const SectorMap>;
+SectorMapP build_sectormap(const std::vector<BondSig>& bonds);  // uncached
+SectorMapP get_sectormap(const std::vector<BondSig>& bonds);    // cached by signature
+
+// ---------------------------------------------------------------- device memory
+struct Ctx;
+// A stream-ordered device allocation owned by a context; it is released on
+// the context's current stream, after the work already queued there.
+struct DevBuf {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  Ctx* ctx = nullptr;
+  DevBuf() = default;
+  DevBuf(size_t n, Ctx& c);
+  ~DevBuf();
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+};
+using DevBufP = std::shared_ptr<DevBuf>;
+
+// ---------------------------------------------------------------- plans
+constexpr int kMaxDims = 12;
+// One sub-block copy of a permute, canonicalised: extent-1 bonds dropped and
+// bonds contiguous in both layouts merged.  dims/strides are listed in the
+// destination order, outermost first; the last dim is the destination's
+// innermost (stride 1 unless the sub-block is a single element).
+struct PermSub {
+  int64_t src_base, dst_base;
+  int64_t sstride[kMaxDims], dstride[kMaxDims];
+  int32_t dims[kMaxDims];
+  int32_t ndim;
+  int32_t ydim;   // index of the source-contiguous dim used as tile y (-1: none)
+  int32_t tx, ty; // tile extents along x (= dims[ndim-1]) and y
+  int32_t ntx, nty;
+  int64_t nouter;     // product of the dims other than x and y
+  int64_t tile_begin; // first tile index of this sub-block
+  double sign;        // +1 (bosonic); a fermionic sign would go here
+  int32_t mode;       // 0: lanes along x; 1: shared-memory transpose (x, y)
+};
+struct PermPlan {
+  DevBufP subs;  // PermSub[nsub]
+  DevBufP tile_start;  // int64_t[nsub+1]
+  std::vector<PermSub> host_subs;         // host copy (plan checks on the CPU)
+  std::vector<int64_t> host_tile_start;
+  int nsub = 0;
+  int64_t ntiles = 0;
+  int64_t elem_num = 0;
+};
+using PermPlanP = std::shared_ptr<PermPlan>;
+
+// FP64 grouped GEMM work item: one output tile (split along K) of a sector.
+struct GemmTile {
+  int64_t a_off, b_off, c_off;  // sector base offsets (elements)
+  int32_t M, N, K;
+  int32_t m0, n0;               // tile origin in C
+  int32_t k0, k1;               // K range of this item
+  int32_t split;                // index of this K split (0..nsplit-1)
+  int32_t nsplit;
+  int64_t ws_off;               // partial-tile slot in the workspace (elements), -1 if nsplit==1
+};
+
+// ---------------------------------------------------------------- context
+// Per-kernel timing with CUDA events on the context's stream (enabled on
+// demand; used by bench.py for the roofline of the dominant kernel).
+struct ProfRec {
+  const char* name;
+  cudaEvent_t start, stop;
+  double bytes, flops;  // algorithmic work of this launch
+};
+struct Ctx;
+struct ProfScope {
+  Ctx* c;
+  ProfRec rec;
+  bool on;
+  ProfScope(Ctx& ctx, const char* name, double bytes = 0, double flops = 0);
+  ~ProfScope();
+};
+
+struct Ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int num_sms = 0;
+  int64_t launches = 0;
+  std::mutex mu;
+  std::unordered_map<std::string, PermPlanP> perm_cache;
+  std::unordered_map<std::string, SectorMapP> smap_refs;  // keep cached maps alive per ctx
+  DevBufP workspace;  // scratch for split-K partial tiles and operand slices
+  DevBufP ensure_workspace(size_t bytes);
+  bool prof = false;
+  std::vector<ProfRec> prof_recs;
+  void launched(int n = 1) { launches += n; }
+};
+Ctx* default_ctx();  // lazily created context on the current device
+Ctx* as_ctx(tn_ctx_t c);
+
+// ---------------------------------------------------------------- operations
+PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
+PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst);
+std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
+PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num);  // tiles assigned, no device copy
+// Runs a plan's tile walk on the host (the kernel's index arithmetic, decoded
+// with the same helper): every source and destination offset is checked
+// against [0, elem_num) and the copy is done into dst.  Returns the number
+// of elements written, or throws on an out-of-range offset.
+int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double* dst);
+void run_permute(Ctx& ctx, const PermPlan& plan, const double* src, double* dst);
+
+// sector GEMMs: C_i = A_i . B_i for every item, all in one grouped launch
+void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A,
+                      const double* B, double* C);
+
+// kernel launchers (defined in the .cu files)
+void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles,
+                           const double* src, double* dst, int grid, cudaStream_t s);
+void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const double* B, double* C,
+                      double* ws, int grid, cudaStream_t s);
+void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
+                          cudaStream_t s);
+void launch_fill(double* p, int64_t n, double v, cudaStream_t s);
+void launch_scale(double* p, int64_t n, double a, cudaStream_t s);
+
+}  // namespace tn

@@ -1,0 +1,252 @@
+// Permute plans: the sub-block walk of UniTensor::permute
+// (tensor-network/lib/UniTensorReal.cpp:685-757) turned into a device work
+// list of canonical strided copies, built once per (source signature,
+// destination signature, bond map) and cached on the context.
+#include <algorithm>
+#include <cstring>
+
+#include "engine.h"
+
+namespace tn {
+
+namespace {
+
+struct Dim {
+  int64_t ext, s, d;
+};
+
+// Tile extents along the destination-contiguous dim x and a second dim y.
+// mode 0: lanes run along x for both the load and the store (x is also the
+//         best source dim); y = the next destination dim, several rows/tile.
+// mode 1: 2-D transpose through shared memory: loads run along y (the
+//         source-contiguous dim), stores along x.
+void choose_tile(PermSub& ps) {
+  const int n = ps.ndim;
+  ps.ydim = -1;
+  ps.mode = 0;
+  if (n == 0) {
+    ps.tx = ps.ty = 1;
+    ps.ntx = ps.nty = 1;
+    ps.nouter = 1;
+    return;
+  }
+  const int x = n - 1;
+  int y = -1;
+  if (ps.sstride[x] != 1) {
+    for (int i = 0; i < x; i++)
+      if (y < 0 || ps.sstride[i] < ps.sstride[y]) y = i;
+    if (y >= 0 && ps.sstride[y] > ps.sstride[x]) y = -1;
+  }
+  if (y >= 0) {
+    ps.mode = 1;
+    ps.ydim = y;
+    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 32);
+    ps.ty = (int32_t)std::min<int64_t>(ps.dims[y], std::min<int64_t>(512, std::max<int64_t>(32, 1024 / ps.tx)));
+  } else {
+    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 1024);
+    if (n >= 2) {
+      ps.ydim = n - 2;
+      ps.ty = (int32_t)std::min<int64_t>(ps.dims[n - 2], std::max<int64_t>(1, 2048 / ps.tx));
+    } else {
+      ps.ty = 1;
+    }
+  }
+  ps.ntx = (int32_t)((ps.dims[x] + ps.tx - 1) / ps.tx);
+  ps.nty = ps.ydim >= 0 ? (int32_t)((ps.dims[ps.ydim] + ps.ty - 1) / ps.ty) : 1;
+  int64_t outer = 1;
+  for (int i = 0; i < n; i++)
+    if (i != x && i != ps.ydim) outer *= ps.dims[i];
+  ps.nouter = outer;
+}
+
+}  // namespace
+
+static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermSub>& subs, int64_t elem_num);
+
+PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp) {
+  std::string key = src.key + "#" + dst.key + "#";
+  for (int r : rsp) key += std::to_string(r) + ",";
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.perm_cache.find(key);
+    if (it != ctx.perm_cache.end()) return it->second;
+  }
+  std::vector<PermSub> subs = build_perm_subs(src, dst, rsp);
+  return finish_plan(ctx, key, subs, src.elem_num);
+}
+
+std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp) {
+  const int n = (int)src.bonds.size();
+  if ((int)dst.bonds.size() != n || (int)rsp.size() != n) fail(TN_ERR_ARG, "permute: bond counts differ");
+  // the destination must be the permuted source (bond b <- source bond rsp[b])
+  std::vector<int> seen(n, 0);
+  for (int b = 0; b < n; b++) {
+    if (rsp[b] < 0 || rsp[b] >= n || seen[rsp[b]]++) fail(TN_ERR_ARG, "permute: rsp is not a permutation");
+    BondSig want = src.bonds[rsp[b]].changed(dst.bonds[b].type);
+    if (!(want == dst.bonds[b])) fail(TN_ERR_ARG, "permute: destination bonds are not the permuted source bonds");
+  }
+  if (src.elem_num != dst.elem_num) fail(TN_ERR_ARG, "permute: element counts differ");
+
+  std::vector<int64_t> qot_acc(n, 1);
+  for (int b = n - 1; b > 0; b--) qot_acc[b - 1] = qot_acc[b] * (int64_t)dst.bonds[b].q.size();
+  const int rbn_in = src.rbond_num, rbn_out = dst.rbond_num;
+
+  std::vector<PermSub> subs;
+  subs.reserve(src.qidx_enc.size());
+  std::vector<int> qin(n), deg(n);
+  std::vector<int64_t> ss(n), ds(n);
+  for (int64_t qidx : src.qidx_enc) {
+    int64_t tmp = qidx;
+    for (int b = n - 1; b >= 0; b--) {  // UniTensorReal.cpp:705-712
+      int64_t qd = (int64_t)src.bonds[b].q.size();
+      qin[b] = (int)(tmp % qd);
+      deg[b] = src.bonds[b].deg[qin[b]];
+      tmp /= qd;
+    }
+    int64_t qot = 0;
+    for (int b = 0; b < n; b++) qot += (int64_t)qin[rsp[b]] * qot_acc[b];
+    int64_t rin = qidx / src.cqdim, cin = qidx % src.cqdim;
+    int64_t rot = qot / dst.cqdim, cot = qot % dst.cqdim;
+    int bi = src.rq2blk[rin], bo = dst.rq2blk[rot];
+    if (bi < 0 || bo < 0 || dst.cq2off[cot] < 0) fail(TN_ERR_ARG, "permute: sub-block without a destination");
+    const auto& Bi = src.blocks[bi];
+    const auto& Bo = dst.blocks[bo];
+    // source strides: rows over IN bonds (x block width), columns over OUT bonds
+    int64_t acc = 1;
+    for (int b = rbn_in - 1; b >= 0; b--) { ss[b] = acc * Bi.cols; acc *= deg[b]; }
+    acc = 1;
+    for (int b = n - 1; b >= rbn_in; b--) { ss[b] = acc; acc *= deg[b]; }
+    // destination strides of source bond rsp[j]
+    acc = 1;
+    for (int j = rbn_out - 1; j >= 0; j--) { ds[rsp[j]] = acc * Bo.cols; acc *= deg[rsp[j]]; }
+    acc = 1;
+    for (int j = n - 1; j >= rbn_out; j--) { ds[rsp[j]] = acc; acc *= deg[rsp[j]]; }
+
+    PermSub ps;
+    std::memset(&ps, 0, sizeof(ps));
+    ps.src_base = Bi.off + src.rq2off[rin] * Bi.cols + src.cq2off[cin];
+    ps.dst_base = Bo.off + dst.rq2off[rot] * Bo.cols + dst.cq2off[cot];
+    ps.sign = 1.0;
+    // canonical dims in destination order: drop extent 1, merge contiguous
+    std::vector<Dim> dims;
+    for (int j = 0; j < n; j++) {
+      int b = rsp[j];
+      if (deg[b] == 1) continue;
+      Dim d{deg[b], ss[b], ds[b]};
+      if (!dims.empty()) {
+        Dim& o = dims.back();
+        if (o.s == d.s * d.ext && o.d == d.d * d.ext) {
+          o.ext *= d.ext;
+          o.s = d.s;
+          o.d = d.d;
+          continue;
+        }
+      }
+      dims.push_back(d);
+    }
+    if ((int)dims.size() > kMaxDims) fail(TN_ERR_UNSUPPORTED, "permute: more than 12 non-trivial bonds in a sub-block");
+    ps.ndim = (int32_t)dims.size();
+    for (int i = 0; i < ps.ndim; i++) {
+      if (dims[i].ext > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "permute: bond extent too large");
+      ps.dims[i] = (int32_t)dims[i].ext;
+      ps.sstride[i] = dims[i].s;
+      ps.dstride[i] = dims[i].d;
+    }
+    choose_tile(ps);
+    subs.push_back(ps);
+  }
+  return subs;
+}
+
+// Block-wise transpose of UniTensor::transpose (UniTensorReal.cpp:448-506):
+// block q of the source (R x C, row-major) becomes block q of the destination
+// (C x R).  One 2-D copy per block.
+PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst) {
+  std::string key = "T#" + src.key + "#" + dst.key;
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.perm_cache.find(key);
+    if (it != ctx.perm_cache.end()) return it->second;
+  }
+  std::vector<PermSub> subs;
+  for (const auto& bi : src.blocks) {
+    int o = dst.find_block(bi.q);
+    if (o < 0) fail(TN_ERR_ARG, "transpose: block without a destination");
+    const auto& bo = dst.blocks[o];
+    if (bo.rows != bi.cols || bo.cols != bi.rows) fail(TN_ERR_SHAPE, "transpose: block shapes differ");
+    PermSub ps;
+    std::memset(&ps, 0, sizeof(ps));
+    ps.src_base = bi.off;
+    ps.dst_base = bo.off;
+    ps.sign = 1.0;
+    std::vector<Dim> dims;
+    // destination order: (source column index, source row index)
+    if (bi.cols > 1) dims.push_back(Dim{bi.cols, 1, bi.rows});
+    if (bi.rows > 1) dims.push_back(Dim{bi.rows, bi.cols, 1});
+    if (dims.size() == 2 && dims[0].s == dims[1].s * dims[1].ext && dims[0].d == dims[1].d * dims[1].ext) {
+      dims[0].ext *= dims[1].ext;
+      dims[0].s = dims[1].s;
+      dims[0].d = dims[1].d;
+      dims.pop_back();
+    }
+    ps.ndim = (int32_t)dims.size();
+    for (int i = 0; i < ps.ndim; i++) {
+      if (dims[i].ext > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "transpose: block extent too large");
+      ps.dims[i] = (int32_t)dims[i].ext;
+      ps.sstride[i] = dims[i].s;
+      ps.dstride[i] = dims[i].d;
+    }
+    choose_tile(ps);
+    subs.push_back(ps);
+  }
+  return finish_plan(ctx, key, subs, src.elem_num);
+}
+
+PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num) {
+  auto plan = std::make_shared<PermPlan>();
+  std::vector<int64_t>& tile_start = plan->host_tile_start;
+  tile_start.reserve(subs.size() + 1);
+  int64_t tiles = 0;
+  for (auto& ps : subs) {
+    ps.tile_begin = tiles;
+    tile_start.push_back(tiles);
+    tiles += ps.nouter * ps.ntx * ps.nty;
+  }
+  tile_start.push_back(tiles);
+  plan->nsub = (int)subs.size();
+  plan->ntiles = tiles;
+  plan->elem_num = elem_num;
+  plan->host_subs = std::move(subs);
+  return plan;
+}
+
+static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermSub>& subs_in, int64_t elem_num) {
+  PermPlanP plan = host_plan(std::move(subs_in), elem_num);
+  const std::vector<PermSub>& subs = plan->host_subs;
+  const std::vector<int64_t>& tile_start = plan->host_tile_start;
+  if (!subs.empty()) {
+    plan->subs = std::make_shared<DevBuf>(subs.size() * sizeof(PermSub), ctx);
+    plan->tile_start = std::make_shared<DevBuf>(tile_start.size() * sizeof(int64_t), ctx);
+    TN_CUDA(cudaMemcpyAsync(plan->subs->ptr, subs.data(), subs.size() * sizeof(PermSub), cudaMemcpyHostToDevice,
+                            ctx.stream));
+    TN_CUDA(cudaMemcpyAsync(plan->tile_start->ptr, tile_start.data(), tile_start.size() * sizeof(int64_t),
+                            cudaMemcpyHostToDevice, ctx.stream));
+    // the host vectors die here: make the copies complete before returning
+    TN_CUDA(cudaStreamSynchronize(ctx.stream));
+  }
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  if (ctx.perm_cache.size() > 4096) ctx.perm_cache.clear();
+  ctx.perm_cache[key] = plan;
+  return plan;
+}
+
+void run_permute(Ctx& ctx, const PermPlan& plan, const double* src, double* dst) {
+  if (plan.ntiles == 0) return;
+  int64_t grid = std::min<int64_t>(plan.ntiles, (int64_t)ctx.num_sms * 8);
+  ProfScope ps(ctx, "permute", 16.0 * plan.elem_num, 0);
+  launch_permute_kernel((const PermSub*)plan.subs->ptr, (const int64_t*)plan.tile_start->ptr, plan.nsub, plan.ntiles,
+                        src, dst, (int)grid, ctx.stream);
+  ctx.launched();
+}
+
+}  // namespace tn

@@ -1,0 +1,219 @@
+// uni10::Block / uni10::Matrix on device memory: the views contract() and the
+// SVD truncation of an iTEBD step use (data-structure/lib/Block.cpp,
+// BlockReal.cpp:226-250; tensor-network/lib/MatrixReal.cpp:289-360).
+#include <cusolverDn.h>
+
+#include <cmath>
+#include <sstream>
+#include <stdexcept>
+
+#include "../../../include/uni10/Matrix.h"
+#include "../../../include/uni10/UniTensor.h"
+#include "../engine/engine.h"
+
+namespace uni10 {
+
+static tn::Ctx& C() { return *tn::default_ctx(); }
+
+std::vector<double> Block::hostElem() const {
+  std::vector<double> h(elemNum());
+  if (!h.empty()) {
+    TN_CUDA(cudaMemcpyAsync(h.data(), m_elem, h.size() * sizeof(double), cudaMemcpyDeviceToHost, C().stream));
+    TN_CUDA(cudaStreamSynchronize(C().stream));
+  }
+  return h;
+}
+
+double Block::at(size_t r, size_t c) const {
+  if (!(r < Rnum && c < Cnum)) throw std::runtime_error("The input indices are out of range.");
+  size_t idx;
+  if (diag) {
+    if (r != c) return 0.0;
+    idx = r;
+  } else {
+    idx = r * Cnum + c;
+  }
+  double v;
+  TN_CUDA(cudaMemcpyAsync(&v, m_elem + idx, sizeof(double), cudaMemcpyDeviceToHost, C().stream));
+  TN_CUDA(cudaStreamSynchronize(C().stream));
+  return v;
+}
+
+double Block::norm() const {
+  double s = 0;
+  for (double x : hostElem()) s += x * x;
+  return std::sqrt(s);
+}
+
+// ---------------------------------------------------------------- Matrix
+void Matrix::alloc() {
+  size_t n = elemNum();
+  tn::Ctx& c = C();
+  auto buf = std::make_shared<tn::DevBuf>(n * sizeof(double), c);
+  m_elem = (double*)buf->ptr;
+  m_buf = buf;
+  if (n) TN_CUDA(cudaMemsetAsync(m_elem, 0, n * sizeof(double), c.stream));
+}
+
+Matrix::Matrix() : Block() {}
+
+Matrix::Matrix(size_t r, size_t c, bool d, bool) : Block(r, c, d) { alloc(); }
+
+Matrix::Matrix(size_t r, size_t c, const double* e, bool d, bool src_ongpu) : Block(r, c, d) {
+  alloc();
+  setElem(e, src_ongpu);
+}
+
+Matrix::Matrix(const Matrix& m) : Block(m.Rnum, m.Cnum, m.diag) {
+  alloc();
+  if (elemNum())
+    TN_CUDA(cudaMemcpyAsync(m_elem, m.m_elem, elemNum() * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
+}
+
+Matrix::Matrix(const Block& b) : Block(b.row(), b.col(), b.isDiag()) {
+  alloc();
+  if (elemNum())
+    TN_CUDA(cudaMemcpyAsync(m_elem, b.getElem(), elemNum() * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
+}
+
+Matrix& Matrix::operator=(const Matrix& m) {
+  if (this == &m) return *this;
+  Rnum = m.Rnum;
+  Cnum = m.Cnum;
+  diag = m.diag;
+  alloc();
+  if (elemNum())
+    TN_CUDA(cudaMemcpyAsync(m_elem, m.m_elem, elemNum() * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
+  return *this;
+}
+
+Matrix::~Matrix() {}
+
+void Matrix::setElem(const double* e, bool src_ongpu) {
+  if (!elemNum()) return;
+  TN_CUDA(cudaMemcpyAsync(m_elem, e, elemNum() * sizeof(double),
+                          src_ongpu ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, C().stream));
+  if (!src_ongpu) TN_CUDA(cudaStreamSynchronize(C().stream));
+}
+
+// keep the leading r x c part (MatrixReal.cpp:289-360)
+Matrix& Matrix::resize(size_t r, size_t c) {
+  Matrix out(r, c, diag);
+  if (diag) {
+    size_t n = std::min(std::min(r, c), elemNum());
+    if (n) TN_CUDA(cudaMemcpyAsync(out.m_elem, m_elem, n * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
+  } else {
+    size_t rr = std::min(r, Rnum), cc = std::min(c, Cnum);
+    if (rr && cc)
+      TN_CUDA(cudaMemcpy2DAsync(out.m_elem, c * sizeof(double), m_elem, Cnum * sizeof(double), cc * sizeof(double), rr,
+                                cudaMemcpyDeviceToDevice, C().stream));
+  }
+  *this = out;
+  return *this;
+}
+
+Matrix& Matrix::operator*=(double a) {
+  tn::launch_scale(m_elem, (int64_t)elemNum(), a, C().stream);
+  C().launched();
+  return *this;
+}
+
+// dense product through the grouped sector GEMM (one sector)
+Matrix operator*(const Block& a, const Block& b) {
+  if (a.col() != b.row()) throw std::runtime_error("The dimensions of the two matrices do not match for matrix multiplication.");
+  if (a.isDiag() || b.isDiag()) {
+    Matrix da(a.row(), a.col()), db(b.row(), b.col());
+    auto expand = [](const Block& s, Matrix& d) {
+      if (!s.isDiag()) {
+        TN_CUDA(cudaMemcpyAsync(d.getElem(), s.getElem(), s.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
+                                C().stream));
+        return;
+      }
+      TN_CUDA(cudaMemcpy2DAsync(d.getElem(), (s.col() + 1) * sizeof(double), s.getElem(), sizeof(double),
+                                sizeof(double), s.elemNum(), cudaMemcpyDeviceToDevice, C().stream));
+    };
+    expand(a, da);
+    expand(b, db);
+    return da * db;
+  }
+  Matrix c(a.row(), b.col());
+  std::vector<tn_sector_gemm> list(1);
+  list[0] = tn_sector_gemm{(int64_t)a.row(), (int64_t)b.col(), (int64_t)a.col(), 0, 0, 0};
+  tn::run_sector_gemms(C(), contractMode(), list, a.getElem(), b.getElem(), c.getElem());
+  return c;
+}
+
+// ---------------------------------------------------------------- SVD
+namespace {
+struct Solver {
+  cusolverDnHandle_t h = nullptr;
+  gesvdjInfo_t info = nullptr;
+  Solver() {
+    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) tn::fail(TN_ERR_CUDA, "cusolverDnCreate failed");
+    if (cusolverDnCreateGesvdjInfo(&info) != CUSOLVER_STATUS_SUCCESS) tn::fail(TN_ERR_CUDA, "gesvdj info failed");
+  }
+};
+Solver& solver() {
+  static thread_local Solver s;
+  cusolverDnSetStream(s.h, C().stream);
+  return s;
+}
+
+__global__ void transpose_kernel(const double* __restrict__ src, double* __restrict__ dst, int rows, int cols) {
+  // src row-major rows x cols -> dst row-major cols x rows
+  __shared__ double t[32][33];
+  int bx = blockIdx.x * 32, by = blockIdx.y * 32;
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    int r = by + j, c = bx + threadIdx.x;
+    if (r < rows && c < cols) t[j][threadIdx.x] = src[(int64_t)r * cols + c];
+  }
+  __syncthreads();
+  for (int j = threadIdx.y; j < 32; j += 8) {
+    int c = bx + j, r = by + threadIdx.x;
+    if (r < rows && c < cols) dst[(int64_t)c * rows + r] = t[threadIdx.x][j];
+  }
+}
+
+void transpose(const double* src, double* dst, int rows, int cols) {
+  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
+  transpose_kernel<<<grid, block, 0, C().stream>>>(src, dst, rows, cols);
+  TN_CUDA(cudaGetLastError());
+  C().launched();
+}
+}  // namespace
+
+// Block::svd: A (M x N, row-major) = U (M x k) . S (k, diagonal) . VT (k x N),
+// k = min(M, N), singular values descending.  The row-major A is the
+// column-major A^T (N x M); its Jacobi SVD A^T = U' S V'^T gives VT = U'^T
+// (already row-major in U''s column-major buffer) and U = V' (transposed).
+std::vector<Matrix> Block::svd() const {
+  if (diag) throw std::runtime_error("svd of a diagonal matrix is not supported");
+  const int M = (int)Rnum, N = (int)Cnum, k = std::min(M, N);
+  Matrix work(Rnum, Cnum, m_elem, false, true);
+  Matrix U(Rnum, k), S(k, k, true), VT(k, Cnum), V(Rnum, k);
+  Solver& s = solver();
+  int lwork = 0;
+  if (cusolverDnDgesvdj_bufferSize(s.h, CUSOLVER_EIG_MODE_VECTOR, 1, N, M, work.getElem(), N, S.getElem(),
+                                   VT.getElem(), N, V.getElem(), M, &lwork, s.info) != CUSOLVER_STATUS_SUCCESS)
+    tn::fail(TN_ERR_CUDA, "gesvdj buffer size failed");
+  tn::Ctx& c = C();
+  tn::DevBuf wk((size_t)lwork * sizeof(double) + sizeof(int), c);
+  int* dinfo = (int*)((double*)wk.ptr + lwork);
+  if (cusolverDnDgesvdj(s.h, CUSOLVER_EIG_MODE_VECTOR, 1, N, M, work.getElem(), N, S.getElem(), VT.getElem(), N,
+                        V.getElem(), M, (double*)wk.ptr, lwork, dinfo, s.info) != CUSOLVER_STATUS_SUCCESS)
+    tn::fail(TN_ERR_CUDA, "gesvdj failed");
+  c.launched();
+  // V' is column-major M x k == row-major k x M; U = its transpose (M x k)
+  transpose(V.getElem(), U.getElem(), k, M);
+  int hinfo = 0;
+  TN_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+  TN_CUDA(cudaStreamSynchronize(c.stream));
+  if (hinfo < 0) tn::fail(TN_ERR_CUDA, "gesvdj: invalid parameter");
+  std::vector<Matrix> out;
+  out.push_back(U);
+  out.push_back(S);
+  out.push_back(VT);
+  return out;
+}
+
+}  // namespace uni10

@@ -1,0 +1,464 @@
+// uni10::Network: .net parsing (tensor-network/lib/Network.cpp:271-427), the
+// contraction tree from explicit ORDER brackets or the greedy matching/branch
+// planner (:428-506, :602-670, Node::contract/metric :63-135), and launch()
+// = recursive merge with contract(fast=true) + permute to TOUT (:697-739).
+#include <algorithm>
+#include <fstream>
+#include <functional>
+#include <sstream>
+#include <stdexcept>
+
+#include "../../../include/uni10/Network.h"
+
+namespace uni10 {
+
+// ---------------------------------------------------------------- Node
+Node::Node() : T(nullptr), elemNum(0), parent(nullptr), left(nullptr), right(nullptr), point(0) {}
+
+Node::Node(UniTensor* Tp)
+    : T(Tp), elemNum((int64_t)Tp->elemNum()), labels(Tp->label()), bonds(Tp->bond()), parent(nullptr), left(nullptr),
+      right(nullptr), point(0) {
+  if (!(Tp->status & UniTensor::HAVEBOND)) throw std::runtime_error("Cannot create node of a network from tensor without bond.");
+}
+
+Node::Node(const std::vector<Bond>& _bonds, const std::vector<int>& _labels)
+    : T(nullptr), labels(_labels), bonds(_bonds), parent(nullptr), left(nullptr), right(nullptr), point(0) {
+  elemNum = cal_elemNum(bonds);
+}
+
+// bonds/labels of the pairwise result: free(A) as IN, then free(B) as OUT
+static int pair_bonds(const Node& a, const Node& b, std::vector<Bond>& cb, std::vector<int>& lc) {
+  std::vector<int> markB(b.bonds.size(), 0);
+  int con = 0;
+  for (size_t i = 0; i < a.bonds.size(); i++) {
+    bool match = false;
+    for (size_t j = 0; j < b.bonds.size(); j++)
+      if (a.labels[i] == b.labels[j]) {
+        markB[j] = 1;
+        match = true;
+        con++;
+        break;
+      }
+    if (!match) {
+      lc.push_back(a.labels[i]);
+      cb.push_back(a.bonds[i]);
+    }
+  }
+  for (size_t j = 0; j < b.bonds.size(); j++)
+    if (!markB[j]) {
+      lc.push_back(b.labels[j]);
+      cb.push_back(b.bonds[j]);
+    }
+  int rbn = (int)a.bonds.size() - con;
+  for (int i = 0; i < rbn; i++) cb[i].change(BD_IN);
+  for (size_t i = rbn; i < cb.size(); i++) cb[i].change(BD_OUT);
+  return con;
+}
+
+Node Node::contract(Node* nd) {
+  std::vector<Bond> cb;
+  std::vector<int> lc;
+  pair_bonds(*this, *nd, cb, lc);
+  return Node(cb, lc);
+}
+
+// (elemNum(A) + elemNum(B)) / elemNum(result), single precision; -1 when
+// nothing is shared (Network.cpp:103-135)
+float Node::metric(Node* nd) {
+  std::vector<Bond> cb;
+  std::vector<int> lc;
+  int con = pair_bonds(*this, *nd, cb, lc);
+  if (con == 0) return -1;
+  int64_t ne = cal_elemNum(cb);
+  return float(elemNum + nd->elemNum) / ne;
+}
+
+// element count grouping would give these bonds (Network.cpp:137-223)
+int64_t Node::cal_elemNum(const std::vector<Bond>& _bonds) {
+  int rbn = 0, cbn = 0;
+  for (const auto& b : _bonds) (b.type() == BD_IN ? rbn : cbn)++;
+  auto hist = [&](int first, int n) {
+    std::map<Qnum, int64_t> h;
+    std::vector<int> offs(n, 0);
+    if (n == 0) {
+      h[Qnum(0)] = 1;
+      return h;
+    }
+    while (true) {
+      Qnum q(0);
+      int64_t d = 1;
+      for (int b = 0; b < n; b++) {
+        q = q * _bonds[first + b].Qnums[offs[b]];
+        d *= _bonds[first + b].Qdegs[offs[b]];
+      }
+      h[q] += d;
+      int b;
+      for (b = n - 1; b >= 0; b--) {
+        if (++offs[b] < (int)_bonds[first + b].Qnums.size()) break;
+        offs[b] = 0;
+      }
+      if (b < 0) break;
+    }
+    return h;
+  };
+  auto r = hist(0, rbn), c = hist(rbn, cbn);
+  int64_t n = 0;
+  for (auto& kv : c) {
+    auto it = r.find(kv.first);
+    if (it != r.end()) n += it->second * kv.second;
+  }
+  return n;
+}
+
+// ---------------------------------------------------------------- parsing
+static void trim(std::string& s) {
+  size_t a = s.find_first_not_of(" \t\r"), b = s.find_last_not_of(" \t\r");
+  s = (a == std::string::npos) ? std::string() : s.substr(a, b - a + 1);
+}
+
+void Network::fromtext(const std::string& text, const std::string& fname) {
+  std::istringstream in(text);
+  std::string str;
+  const std::string tar("1234567890-");
+  std::vector<std::string> ord;
+  int lnum = 0;
+  while (lnum < 1000 && std::getline(in, str)) {
+    size_t pos = str.find(':');
+    if (pos == std::string::npos) break;
+    std::string name = str.substr(0, pos);
+    trim(name);
+    if (name == "ORDER") {
+      if (str.find('(', pos + 1) == std::string::npos) {
+        const std::string del(" ,;");
+        size_t p = pos;
+        while ((p = str.find_first_not_of(del, p + 1)) != std::string::npos) {
+          size_t e = str.find_first_of(del, p + 1);
+          ord.push_back(e == std::string::npos ? str.substr(p) : str.substr(p, e - p));
+          p = e;
+          if (p == std::string::npos) break;
+        }
+      } else {
+        // each delimiter run before a name gives -(#')') then +(#'('); the run
+        // after the last name gives -(#')')  (Network.cpp:316-357)
+        const std::string del(" ,;*()");
+        size_t endpos = str.find_first_of(del, pos + 1);
+        size_t p = pos;
+        while ((p = str.find_first_not_of(del, p + 1)) != std::string::npos) {
+          std::string bras = str.substr(endpos, p - endpos);
+          int minus = (int)std::count(bras.begin(), bras.end(), ')');
+          int plus = (int)std::count(bras.begin(), bras.end(), '(');
+          if (minus) brakets.push_back(-minus);
+          if (plus) brakets.push_back(plus);
+          endpos = str.find_first_of(del, p + 1);
+          ord.push_back(endpos == std::string::npos ? str.substr(p) : str.substr(p, endpos - p));
+          brakets.push_back(0);
+          p = endpos;
+          if (p == std::string::npos) break;
+        }
+        if (endpos != std::string::npos) {
+          std::string bras = str.substr(endpos);
+          int minus = (int)std::count(bras.begin(), bras.end(), ')');
+          if (minus) brakets.push_back(-minus);
+        }
+        int sum = 0;
+        for (int b : brakets) sum += b;
+        if (sum != 0)
+          throw std::runtime_error("Error in the network file '" + fname +
+                                   "'. There are imbalance brackets when specifying the contraction order.");
+      }
+      break;
+    }
+    name2pos[name] = names.size();
+    names.push_back(name);
+    std::vector<int> labs;
+    int Rnum = -1, cnt = 0;
+    size_t endpos = 0, p = pos;
+    while ((p = str.find_first_of(tar, p + 1)) != std::string::npos) {
+      if (Rnum == -1) {
+        size_t tmp = str.find(';', endpos);
+        if (tmp != std::string::npos && tmp < p) Rnum = cnt;
+      }
+      endpos = str.find_first_not_of(tar, p + 1);
+      std::string lab = (endpos == std::string::npos) ? str.substr(p) : str.substr(p, endpos - p);
+      labs.push_back((int)std::strtol(lab.c_str(), nullptr, 10));
+      p = endpos;
+      if (Rnum == -1) cnt++;
+      if (p == std::string::npos) break;
+    }
+    label_arr.push_back(labs);
+    Rnums.push_back(Rnum == -1 ? (int)labs.size() : Rnum);
+    lnum++;
+  }
+  if (names.empty() || names.back() != "TOUT")
+    throw std::runtime_error("Error in the network file '" + fname +
+                             "'. Missing TOUT tensor. One must specify the bond labels for the resulting tensor by giving TOUT tag.");
+  if (!(names.size() > 2))
+    throw std::runtime_error("Error in the network file '" + fname + "'. There must be at least two tensors in a tensor network.");
+  const int numT = (int)names.size() - 1;
+  order.assign(numT, 0);
+  if (!ord.empty()) {
+    if ((int)ord.size() != numT)
+      throw std::runtime_error("Error in the network file '" + fname + "'. Some tensors are missing in the contraction order.");
+    std::vector<bool> found(numT, false);
+    for (int i = 0; i < numT; i++) {
+      auto it = name2pos.find(ord[i]);
+      if (it == name2pos.end() || (int)it->second >= numT)
+        throw std::runtime_error("Error in the network file '" + fname + "'. '" + ord[i] +
+                                 "' in the contraction order is not in the list of tensors above.");
+      order[i] = (int)it->second;
+      if (found[order[i]])
+        throw std::runtime_error("Error in the network file '" + fname + "'. '" + ord[i] +
+                                 "' appears more than once in the contraction order.");
+      found[order[i]] = true;
+    }
+  } else {
+    for (int i = 0; i < numT; i++) order[i] = i;
+  }
+  leafs.assign(numT, nullptr);
+  tensors.assign(numT, nullptr);
+}
+
+Network::Network(const std::string& fname) {
+  std::ifstream f(fname.c_str());
+  if (!f.is_open()) throw std::runtime_error("Error in opening file '" + fname + "'.");
+  std::stringstream ss;
+  ss << f.rdbuf();
+  fromtext(ss.str(), fname);
+}
+
+Network::Network(const std::string& fname, const std::vector<UniTensor*>& tens) : Network(fname) {
+  if (tens.size() != label_arr.size() - 1)
+    throw std::runtime_error("The size of the input vector of tensors does not match for the number of tensors in the network file '" + fname + "'.");
+  for (size_t i = 0; i < tens.size(); i++) putTensor(i, tens[i]);
+  construct();
+}
+
+Network Network::fromText(const std::string& text) {
+  Network n;
+  n.fromtext(text, "<text>");
+  return n;
+}
+
+Network::Network(Network&& o) noexcept
+    : names(std::move(o.names)), name2pos(std::move(o.name2pos)), label_arr(std::move(o.label_arr)),
+      Rnums(std::move(o.Rnums)), leafs(std::move(o.leafs)), tensors(std::move(o.tensors)), order(std::move(o.order)),
+      brakets(std::move(o.brakets)), root(o.root), load(o.load) {
+  o.root = nullptr;
+  o.load = false;
+}
+
+Network::~Network() {
+  if (load) destruct();
+  for (Node* l : leafs) delete l;
+  for (UniTensor* t : tensors) delete t;
+}
+
+// ---------------------------------------------------------------- tensors
+void Network::putTensor(size_t idx, const UniTensor* UniT, bool force) {
+  if (!(idx < label_arr.size() - 1)) throw std::runtime_error("Index exceeds the number of the tensors in the list of network file.");
+  if (!force && load) destruct();
+  if (!((int)UniT->inBondNum() == Rnums[idx]))
+    throw std::runtime_error("The number of in-coming bonds does not match with the tensor '" + names[idx] +
+                             "' specified in network file");
+  if (leafs[idx] != nullptr) {
+    *(tensors[idx]) = *UniT;
+    tensors[idx]->setLabel(label_arr[idx]);
+    tensors[idx]->setName(names[idx]);
+  } else {
+    UniTensor* t = new UniTensor(*UniT);
+    t->setName(names[idx]);
+    t->setLabel(label_arr[idx]);
+    tensors[idx] = t;
+    leafs[idx] = new Node(t);
+  }
+}
+
+void Network::putTensor(size_t idx, const UniTensor& UniT, bool force) { putTensor(idx, &UniT, force); }
+
+void Network::putTensor(const std::string& name, const UniTensor* UniT, bool force) {
+  auto it = name2pos.find(name);
+  if (it == name2pos.end()) throw std::runtime_error("There is no tensor named '" + name + "' in the network file");
+  putTensor(it->second, UniT, force);
+}
+
+void Network::putTensor(const std::string& name, const UniTensor& UniT, bool force) { putTensor(name, &UniT, force); }
+
+void Network::putTensorT(const std::string& nameT, const UniTensor* UniT, bool force) {
+  auto it = name2pos.find(nameT);
+  if (it == name2pos.end()) throw std::runtime_error("There is no tensor named '" + nameT + "' in the network file");
+  UniTensor t = *UniT;
+  t.transpose();
+  putTensor(it->second, &t, force);
+}
+
+void Network::putTensorT(const std::string& nameT, const UniTensor& UniT, bool force) { putTensorT(nameT, &UniT, force); }
+
+// ---------------------------------------------------------------- tree
+void Network::construct() {
+  for (size_t i = 0; i < leafs.size(); i++)
+    if (leafs[i] == nullptr)
+      throw std::runtime_error("Tensor '" + names[i] + "' has not yet been given.\n  Hint: Use putTensor() to add a tensor to a network.\n");
+  // a leaf mirrors its tensor's current bonds/labels (contract permutes leaves in place)
+  for (size_t i = 0; i < leafs.size(); i++) {
+    leafs[i]->bonds = tensors[i]->bond();
+    leafs[i]->labels = tensors[i]->label();
+    leafs[i]->elemNum = (int64_t)tensors[i]->elemNum();
+  }
+  if (!brakets.empty()) {
+    std::vector<Node*> stack(leafs.size(), nullptr);
+    int cursor = 0, cnt = 0;
+    for (int br : brakets) {
+      if (br < 0) {
+        for (int c = 0; c < -br; c++) {
+          Node* par = new Node(stack[cursor - 2]->contract(stack[cursor - 1]));
+          par->left = stack[cursor - 2];
+          par->right = stack[cursor - 1];
+          par->left->parent = par;
+          par->right->parent = par;
+          stack[cursor - 2] = par;
+          cursor--;
+          if (cursor < 2) break;
+        }
+      } else if (br == 0) {
+        stack[cursor++] = leafs[order[cnt++]];
+      }
+    }
+    while (cursor > 1) {
+      Node* par = new Node(stack[cursor - 2]->contract(stack[cursor - 1]));
+      par->left = stack[cursor - 2];
+      par->right = stack[cursor - 1];
+      par->left->parent = par;
+      par->right->parent = par;
+      stack[cursor - 2] = par;
+      cursor--;
+    }
+    root = stack[0];
+  } else {
+    for (int i : order) matching(leafs[i], root);
+  }
+  const std::vector<int>& tout = label_arr.back();
+  if (root->labels.size() == tout.size()) {
+    for (int l : root->labels)
+      if (std::find(tout.begin(), tout.end(), l) == tout.end())
+        throw std::runtime_error("Error when constructing the network. The labels of the resulting tensor do not match with the labels of 'TOUT' in the network file");
+  } else {
+    throw std::runtime_error("Error when constructing the network. The bond number of the resulting tensor is different from the bond number of 'TOUT'");
+  }
+  load = true;
+}
+
+void Network::branch(Node* sbj, Node* tar) {
+  Node* par = new Node(tar->contract(sbj));
+  if (sbj->parent == nullptr) {
+    if (tar->parent != nullptr) {
+      if (tar->parent->left == tar)
+        tar->parent->left = par;
+      else
+        tar->parent->right = par;
+      par->parent = tar->parent;
+    } else {
+      par->parent = nullptr;
+      root = par;
+    }
+  } else {
+    if (tar->parent->parent != nullptr) {
+      if (tar->parent->parent->left == tar->parent)
+        tar->parent->parent->left = par;
+      else
+        tar->parent->parent->right = par;
+      par->parent = tar->parent->parent;
+    } else {
+      par->parent = nullptr;
+      root = par;
+    }
+    delete tar->parent;
+  }
+  par->left = tar;
+  par->right = sbj;
+  tar->parent = par;
+  sbj->parent = par;
+  par->point = tar->metric(sbj);
+  if (sbj->parent->parent != nullptr) {
+    sbj = sbj->parent;
+    branch(sbj->parent->right, sbj->parent->left);
+  }
+}
+
+void Network::matching(Node* sbj, Node* tar) {
+  if (tar == nullptr) {
+    root = sbj;
+  } else if (tar->T == nullptr) {
+    if (sbj->metric(tar) > 0) {
+      if (!(tar->left != nullptr && tar->right != nullptr))
+        throw std::runtime_error("Fatal error(code = N1). Please contact the developer of the uni10 library.");
+      float tar_p = tar->point;
+      float lft_p = 0, rht_p = 0;
+      if ((lft_p = sbj->metric(tar->left)) > tar_p || (rht_p = sbj->metric(tar->right)) > tar_p) {
+        if (lft_p > rht_p)
+          matching(sbj, tar->left);
+        else
+          matching(sbj, tar->right);
+      } else {
+        branch(sbj, tar);
+      }
+    } else {
+      branch(sbj, tar);
+    }
+  } else {
+    branch(sbj, tar);
+  }
+}
+
+void Network::clean(Node* nd) {
+  if (nd == nullptr || nd->T != nullptr) return;
+  clean(nd->left);
+  clean(nd->right);
+  delete nd;
+}
+
+void Network::destruct() {
+  clean(root);
+  root = nullptr;
+  for (Node* l : leafs)
+    if (l) {
+      l->parent = l->left = l->right = nullptr;
+      l->point = 0;
+    }
+  load = false;
+}
+
+UniTensor Network::merge(Node* nd) {
+  if (nd->left->T == nullptr) {
+    UniTensor lftT = merge(nd->left);
+    if (nd->right->T == nullptr) {
+      UniTensor rhtT = merge(nd->right);
+      return contract(lftT, rhtT, true);
+    }
+    return contract(lftT, *(nd->right->T), true);
+  }
+  if (nd->right->T == nullptr) {
+    UniTensor rhtT = merge(nd->right);
+    return contract(*(nd->left->T), rhtT, true);
+  }
+  return contract(*(nd->left->T), *(nd->right->T), true);
+}
+
+UniTensor Network::launch(const std::string& _name) {
+  if (!load) construct();
+  UniTensor UniT = merge(root);
+  size_t idx = label_arr.size() - 1;
+  if (!label_arr.empty() && label_arr[idx].size() > 1) UniT.permute(label_arr[idx], Rnums[idx]);
+  UniT.setName(_name);
+  return UniT;
+}
+
+std::string Network::tree() {
+  if (!load) construct();
+  std::function<std::string(Node*)> rec = [&](Node* n) -> std::string {
+    if (n->T) return n->T->getName();
+    return "(" + rec(n->left) + " " + rec(n->right) + ")";
+  };
+  return rec(root);
+}
+
+}  // namespace uni10

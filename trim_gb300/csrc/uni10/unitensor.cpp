@@ -1,0 +1,694 @@
+// uni10::UniTensor on the GB300 engine: the sector map comes from the cached
+// grouping, the element buffer lives in HBM, permute/transpose run the permute
+// kernel and contract runs all sector GEMMs of a contraction in one grouped
+// launch.  Semantics follow the reference (tensor-network/lib/UniTensor.cpp,
+// UniTensorReal.cpp, UniTensorTools.cpp) including in-place permutes of
+// contract()'s operands.
+#include <cstdio>
+#include <cstring>
+#include <sstream>
+#include <stdexcept>
+
+#include "../../../include/uni10/UniTensor.h"
+#include "../engine/engine.h"
+
+namespace uni10 {
+
+using tn::DevBuf;
+
+static thread_local int g_mode = TN_MODE_FP64;
+void setContractMode(int mode) {
+  if (mode < TN_MODE_FP64 || mode > TN_MODE_FAST_TF32) throw std::runtime_error("unknown contraction mode");
+  g_mode = mode;
+}
+int contractMode() { return g_mode; }
+
+static tn::Ctx& C() { return *tn::default_ctx(); }
+
+std::vector<tn::BondSig> to_sigs(const std::vector<Bond>& bonds) {
+  std::vector<tn::BondSig> s(bonds.size());
+  for (size_t b = 0; b < bonds.size(); b++) {
+    s[b].type = bonds[b].type();
+    for (size_t i = 0; i < bonds[b].qnums().size(); i++) {
+      const Qnum& q = bonds[b].qnums()[i];
+      s[b].q.push_back(tn::Q{q.U1(), (int)q.prt(), (int)q.prtF()});
+      s[b].deg.push_back(bonds[b].qdegs()[i]);
+    }
+  }
+  return s;
+}
+
+static Qnum to_qnum(const tn::Q& q) { return Qnum((parityFType)q.prtf, q.u1, (parityType)q.prt); }
+
+static std::shared_ptr<DevBuf> alloc_elem(size_t n) {
+  tn::Ctx& c = C();
+  auto b = std::make_shared<DevBuf>(n * sizeof(double), c);
+  return b;
+}
+
+static double* dptr(const std::shared_ptr<DevBuf>& b) { return b ? (double*)b->ptr : nullptr; }
+
+// ---------------------------------------------------------------- construction
+UniTensor::UniTensor() : status(0) {}
+
+UniTensor::UniTensor(double val) : status(0) {
+  initUniT();
+  TN_CUDA(cudaMemcpyAsync(dptr(elem), &val, sizeof(double), cudaMemcpyHostToDevice, C().stream));
+  TN_CUDA(cudaStreamSynchronize(C().stream));
+}
+
+UniTensor::UniTensor(const std::vector<Bond>& _bonds, const std::string& _name) : name(_name), bonds(_bonds), status(0) {
+  initUniT();
+}
+
+UniTensor::UniTensor(const std::vector<Bond>& _bonds, std::vector<int>& _labels, const std::string& _name)
+    : name(_name), bonds(_bonds), status(0) {
+  initUniT();
+  setLabel(_labels);
+}
+
+UniTensor::UniTensor(const std::vector<Bond>& _bonds, int* _labels, const std::string& _name)
+    : name(_name), bonds(_bonds), status(0) {
+  initUniT();
+  setLabel(_labels);
+}
+
+// a tensor whose every element is about to be overwritten (permute output)
+UniTensor::UniTensor(const std::vector<Bond>& _bonds, const std::string& _name, NoFill)
+    : name(_name), bonds(_bonds), status(0) {
+  initUniT(false);
+}
+
+// UniTensorReal.cpp:1323-1363 -- grouping, allocation, zero fill
+void UniTensor::initUniT(bool zero) {
+  if (!bonds.empty()) {
+    smap = tn::get_sectormap(to_sigs(bonds));
+    if (smap->blocks.empty()) {
+      std::ostringstream err;
+      err << "There is no symmetry block with the given bonds:\n";
+      for (const auto& b : bonds) err << "    " << b;
+      throw std::runtime_error(err.str());
+    }
+    m_elemNum = smap->elem_num;
+    RBondNum = smap->rbond_num;
+    labels.resize(bonds.size());
+    for (size_t b = 0; b < bonds.size(); b++) labels[b] = (int)b;
+    status |= HAVEBOND;
+  } else {
+    smap.reset();
+    RBondNum = 0;
+    m_elemNum = 1;
+    status |= HAVEELEM;
+  }
+  elem = alloc_elem(m_elemNum);
+  if (zero) TN_CUDA(cudaMemsetAsync(dptr(elem), 0, m_elemNum * sizeof(double), C().stream));
+}
+
+UniTensor::UniTensor(const UniTensor& o)
+    : name(o.name), bonds(o.bonds), labels(o.labels), RBondNum(o.RBondNum), m_elemNum(o.m_elemNum), status(o.status),
+      smap(o.smap) {
+  if (o.elem) {
+    elem = alloc_elem(m_elemNum);
+    TN_CUDA(cudaMemcpyAsync(dptr(elem), dptr(o.elem), m_elemNum * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
+  }
+}
+
+UniTensor& UniTensor::operator=(const UniTensor& o) {
+  if (this == &o) return *this;
+  name = o.name;
+  bonds = o.bonds;
+  labels = o.labels;
+  RBondNum = o.RBondNum;
+  m_elemNum = o.m_elemNum;
+  status = o.status;
+  smap = o.smap;
+  if (o.elem) {
+    if (!elem || elem->bytes < m_elemNum * sizeof(double)) elem = alloc_elem(m_elemNum);
+    TN_CUDA(cudaMemcpyAsync(dptr(elem), dptr(o.elem), m_elemNum * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
+  } else {
+    elem.reset();
+  }
+  return *this;
+}
+
+UniTensor::~UniTensor() {}
+
+// ---------------------------------------------------------------- elements
+void UniTensor::setElem(const double* e, bool _ongpu) {
+  if (!elem) throw std::runtime_error("Setting elements to an empty tensor is not supported.");
+  tn::Ctx& c = C();
+  TN_CUDA(cudaMemcpyAsync(dptr(elem), e, m_elemNum * sizeof(double),
+                          _ongpu ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c.stream));
+  if (!_ongpu) TN_CUDA(cudaStreamSynchronize(c.stream));  // the caller may reuse its buffer at once
+  status |= HAVEELEM;
+}
+
+void UniTensor::setElem(const std::vector<double>& e, bool _ongpu) {
+  if (e.size() != m_elemNum) {
+    std::ostringstream err;
+    err << "Number of the input elements is: " << e.size() << ", and it doesn't match to the number of elements in the UniTensor: " << m_elemNum;
+    throw std::runtime_error(err.str());
+  }
+  setElem(e.data(), _ongpu);
+}
+
+double* UniTensor::getElem() { return dptr(elem); }
+
+std::vector<double> UniTensor::hostElem() const {
+  std::vector<double> h(m_elemNum);
+  if (elem && m_elemNum) {
+    TN_CUDA(cudaMemcpyAsync(h.data(), dptr(elem), m_elemNum * sizeof(double), cudaMemcpyDeviceToHost, C().stream));
+    TN_CUDA(cudaStreamSynchronize(C().stream));
+  }
+  return h;
+}
+
+double UniTensor::at(size_t idx) const {
+  if (!(idx < m_elemNum)) {
+    std::ostringstream err;
+    err << "Index exceeds the number of elements(" << m_elemNum << ").";
+    throw std::runtime_error(err.str());
+  }
+  double v = 0;
+  TN_CUDA(cudaMemcpyAsync(&v, dptr(elem) + idx, sizeof(double), cudaMemcpyDeviceToHost, C().stream));
+  TN_CUDA(cudaStreamSynchronize(C().stream));
+  return v;
+}
+
+void UniTensor::set_zero() {
+  if (elem) TN_CUDA(cudaMemsetAsync(dptr(elem), 0, m_elemNum * sizeof(double), C().stream));
+  status |= HAVEELEM;
+}
+
+// dense raw layout <-> blocks (UniTensorReal.cpp:96-174, 241-280): the raw
+// index is row-major over all bonds; each bond index = run offset + degeneracy
+// index.  Host-side, for tests and I/O.
+static void raw_map(const tn::SectorMap& m, const std::vector<Bond>& bonds, std::vector<int64_t>& elem_to_raw) {
+  const int n = (int)bonds.size();
+  std::vector<int64_t> racc(n, 1);
+  for (int b = n - 1; b > 0; b--) racc[b - 1] = racc[b] * bonds[b].dim();
+  std::vector<std::vector<int>> offs(n);
+  for (int b = 0; b < n; b++) {
+    int o = 0;
+    for (int d : bonds[b].qdegs()) {
+      offs[b].push_back(o);
+      o += d;
+    }
+  }
+  elem_to_raw.assign(m.elem_num, -1);
+  std::vector<int> qi(n), deg(n), idx(n);
+  for (int64_t qidx : m.qidx_enc) {
+    int64_t tmp = qidx;
+    int64_t roff = 0;
+    for (int b = n - 1; b >= 0; b--) {
+      int64_t qd = (int64_t)bonds[b].qnums().size();
+      qi[b] = (int)(tmp % qd);
+      tmp /= qd;
+    }
+    for (int b = 0; b < n; b++) {
+      roff += racc[b] * offs[b][qi[b]];
+      deg[b] = bonds[b].qdegs()[qi[b]];
+    }
+    int64_t r = qidx / m.cqdim, c = qidx % m.cqdim;
+    const auto& B = m.blocks[m.rq2blk[r]];
+    int64_t e0 = B.off + m.rq2off[r] * B.cols + m.cq2off[c];
+    int64_t rd = m.rq2dim[r], cd = m.cq2dim[c];
+    std::fill(idx.begin(), idx.end(), 0);
+    int64_t ro = roff;
+    for (int64_t sr = 0; sr < rd; sr++)
+      for (int64_t sc = 0; sc < cd; sc++) {
+        elem_to_raw[e0 + sr * B.cols + sc] = ro;
+        for (int b = n - 1; b >= 0; b--) {
+          if (++idx[b] < deg[b]) {
+            ro += racc[b];
+            break;
+          }
+          ro -= racc[b] * (idx[b] - 1);
+          idx[b] = 0;
+        }
+      }
+  }
+}
+
+void UniTensor::setRawElem(const std::vector<double>& raw) {
+  if (!(status & HAVEBOND)) throw std::runtime_error("Setting elements to a tensor without bonds is not supported.");
+  std::vector<int64_t> map;
+  raw_map(*smap, bonds, map);
+  std::vector<double> h(m_elemNum);
+  for (size_t i = 0; i < m_elemNum; i++) {
+    if (map[i] < 0 || (size_t)map[i] >= raw.size()) throw std::runtime_error("raw element vector too short");
+    h[i] = raw[map[i]];
+  }
+  setElem(h.data(), false);
+}
+
+std::vector<double> UniTensor::getRawElem() const {
+  int64_t total = 1;
+  for (const auto& b : bonds) total *= b.dim();
+  std::vector<double> raw(total, 0.0);
+  std::vector<int64_t> map;
+  raw_map(*smap, bonds, map);
+  std::vector<double> h = hostElem();
+  for (size_t i = 0; i < m_elemNum; i++) raw[map[i]] = h[i];
+  return raw;
+}
+
+// ---------------------------------------------------------------- labels / blocks
+void UniTensor::setLabel(const int newLabel, const size_t idx) {
+  if (!(idx < labels.size())) throw std::runtime_error("The bond index is out of the range of vector(labels).");
+  labels[idx] = newLabel;
+}
+
+void UniTensor::setLabel(const std::vector<int>& newLabels) {
+  if (newLabels.size() != bonds.size())
+    throw std::runtime_error("The size of input vector(labels) does not match for the number of bonds.");
+  labels = newLabels;
+}
+
+void UniTensor::setLabel(int* newLabels) { setLabel(std::vector<int>(newLabels, newLabels + bonds.size())); }
+
+size_t UniTensor::blockNum() const { return smap ? smap->blocks.size() : 1; }
+
+std::vector<Qnum> UniTensor::blockQnum() const {
+  std::vector<Qnum> q;
+  if (!smap) {
+    q.push_back(Qnum(0));
+    return q;
+  }
+  for (const auto& b : smap->blocks) q.push_back(to_qnum(b.q));
+  return q;
+}
+
+Qnum UniTensor::blockQnum(size_t idx) const {
+  if (!smap) return Qnum(0);
+  if (!(idx < smap->blocks.size())) throw std::runtime_error("Index exceeds the number of the blocks.");
+  return to_qnum(smap->blocks[idx].q);
+}
+
+Matrix UniTensor::getBlock(bool diag) const { return getBlock(Qnum(0), diag); }
+
+Matrix UniTensor::getBlock(const Qnum& q, bool diag) const {
+  int bi = smap ? smap->find_block(tn::Q{q.U1(), (int)q.prt(), (int)q.prtF()}) : 0;
+  if (bi < 0) {
+    std::ostringstream err;
+    err << "There is no block with the given quantum number " << q;
+    throw std::runtime_error(err.str());
+  }
+  size_t r = smap ? smap->blocks[bi].rows : 1, c = smap ? smap->blocks[bi].cols : 1;
+  const double* src = dptr(elem) + (smap ? smap->blocks[bi].off : 0);
+  if (!diag) return Matrix(r, c, src, false, true);
+  // diagonal of the block
+  Matrix m(r, c, true);
+  size_t n = r < c ? r : c;
+  TN_CUDA(cudaMemcpy2DAsync(m.getElem(), sizeof(double), src, (c + 1) * sizeof(double), sizeof(double), n,
+                            cudaMemcpyDeviceToDevice, C().stream));
+  return m;
+}
+
+void UniTensor::putBlock(const Block& mat) { putBlock(Qnum(0), mat); }
+
+// UniTensorReal.cpp putBlock: a diagonal matrix fills the block's diagonal
+void UniTensor::putBlock(const Qnum& q, const Block& mat) {
+  int bi = smap ? smap->find_block(tn::Q{q.U1(), (int)q.prt(), (int)q.prtF()}) : 0;
+  if (bi < 0) {
+    std::ostringstream err;
+    err << "There is no block with the given quantum number " << q;
+    throw std::runtime_error(err.str());
+  }
+  size_t r = smap ? smap->blocks[bi].rows : 1, c = smap ? smap->blocks[bi].cols : 1;
+  if (!(mat.row() == r && mat.col() == c)) {
+    std::ostringstream err;
+    err << "The dimension of input matrix does not match for the dimension of the block with quantum number " << q
+        << "\n  Hint: Use Matrix::resize(int, int)";
+    throw std::runtime_error(err.str());
+  }
+  double* dst = dptr(elem) + (smap ? smap->blocks[bi].off : 0);
+  tn::Ctx& cx = C();
+  if (mat.isDiag()) {
+    TN_CUDA(cudaMemsetAsync(dst, 0, r * c * sizeof(double), cx.stream));
+    size_t n = mat.elemNum();
+    TN_CUDA(cudaMemcpy2DAsync(dst, (c + 1) * sizeof(double), mat.getElem(), sizeof(double), sizeof(double), n,
+                              cudaMemcpyDeviceToDevice, cx.stream));
+  } else {
+    TN_CUDA(cudaMemcpyAsync(dst, mat.getElem(), r * c * sizeof(double), cudaMemcpyDeviceToDevice, cx.stream));
+  }
+  status |= HAVEELEM;
+}
+
+// ---------------------------------------------------------------- permute
+// UniTensorReal.cpp:532-768
+UniTensor& UniTensor::permute(const std::vector<int>& newLabels, int rowBondNum) {
+  if ((status & HAVEBOND) == 0) throw std::runtime_error("There is no bond in the tensor(scalar) to permute.");
+  if (labels.size() != newLabels.size())
+    throw std::runtime_error("The size of the input new labels does not match for the number of bonds.");
+  const int n = (int)bonds.size();
+  std::vector<int> rsp(n, 0);
+  size_t cnt = 0;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      if (labels[i] == newLabels[j]) {
+        rsp[j] = i;
+        cnt++;
+      }
+  if (cnt != newLabels.size())
+    throw std::runtime_error("The input new labels do not 1-1 correspond to the labels of the tensor.");
+  bool inorder = true;
+  for (int i = 1; i < n; i++)
+    if (rsp[i] != i) {
+      inorder = false;
+      break;
+    }
+  if (inorder && RBondNum == rowBondNum) return *this;
+  std::vector<Bond> outBonds;
+  for (int b = 0; b < n; b++) outBonds.push_back(bonds[rsp[b]]);
+  for (int b = 0; b < n; b++) outBonds[b].change(b < rowBondNum ? BD_IN : BD_OUT);
+  UniTensor out(outBonds, name, NoFill{});
+  if (status & HAVEELEM) {
+    tn::Ctx& c = C();
+    auto plan = tn::get_perm_plan(c, *smap, *out.smap, rsp);
+    tn::run_permute(c, *plan, dptr(elem), dptr(out.elem));
+    out.status |= HAVEELEM;
+  }
+  // take over the permuted tensor (buffers are moved, not copied)
+  bonds = std::move(out.bonds);
+  smap = std::move(out.smap);
+  elem = std::move(out.elem);
+  RBondNum = out.RBondNum;
+  m_elemNum = out.m_elemNum;
+  status = out.status;
+  labels = newLabels;
+  return *this;
+}
+
+UniTensor& UniTensor::permute(int* newLabels, int rowBondNum) {
+  return permute(std::vector<int>(newLabels, newLabels + bonds.size()), rowBondNum);
+}
+
+UniTensor& UniTensor::permute(int rowBondNum) {
+  std::vector<int> l = labels;
+  return permute(l, rowBondNum);
+}
+
+// UniTensorReal.cpp:448-506: swap the row/column bond groups (types set, not
+// negated) and transpose every block
+UniTensor& UniTensor::transpose() {
+  if (!(status & HAVEBOND)) throw std::runtime_error("There is no bond in the tensor(scalar) to perform transposition.");
+  const int n = (int)bonds.size();
+  int rbn = 0;
+  for (int b = 0; b < n; b++) {
+    if (bonds[b].type() == BD_IN)
+      rbn++;
+    else
+      break;
+  }
+  int cbn = n - rbn;
+  std::vector<int> rsp(n);
+  for (int b = 0; b < n; b++) rsp[b] = (b < cbn) ? rbn + b : b - cbn;
+  std::vector<int> outLabels(n);
+  std::vector<Bond> outBonds;
+  for (int b = 0; b < n; b++) {
+    outBonds.push_back(bonds[rsp[b]]);
+    outLabels[b] = labels[rsp[b]];
+  }
+  for (int b = 0; b < n; b++) outBonds[b].dummy_change(b < cbn ? BD_IN : BD_OUT);
+  UniTensor out(outBonds, name, NoFill{});
+  if (status & HAVEELEM) {
+    tn::Ctx& c = C();
+    auto plan = tn::get_transpose_plan(c, *smap, *out.smap);
+    tn::run_permute(c, *plan, dptr(elem), dptr(out.elem));
+    out.status |= HAVEELEM;
+  }
+  bonds = std::move(out.bonds);
+  smap = std::move(out.smap);
+  elem = std::move(out.elem);
+  RBondNum = out.RBondNum;
+  m_elemNum = out.m_elemNum;
+  status = out.status;
+  labels = outLabels;
+  return *this;
+}
+
+// UniTensorReal.cpp:791-866: permute the combined bonds next to each other,
+// then reinterpret the same element buffer with the fused bond
+UniTensor& UniTensor::combineBond(const std::vector<int>& cmbLabels) {
+  if ((status & HAVEBOND) == 0) throw std::runtime_error("There is no bond in the tensor to be combined.");
+  if (!(cmbLabels.size() > 1)) return *this;
+  const size_t n = labels.size();
+  std::vector<int> rsp_labels(n, 0), reduced(n - cmbLabels.size() + 1, 0), marked(n, 0), picked(cmbLabels.size(), 0);
+  for (size_t p = 0; p < cmbLabels.size(); p++)
+    for (size_t l = 0; l < n; l++)
+      if (cmbLabels[p] == labels[l]) {
+        picked[p] = (int)l;
+        marked[l] = 1;
+        break;
+      }
+  size_t mark = 0;
+  for (int m : marked) mark += m;
+  if (mark != cmbLabels.size()) throw std::runtime_error("The input labels do not match for the labels of the tensor.");
+  int enc = 0, enc_r = 0, RBnum = 0;
+  std::vector<Bond> newBonds;
+  for (size_t l = 0; l < n; l++) {
+    if (marked[l] && (int)l == picked[0]) {
+      for (size_t ll = 0; ll < cmbLabels.size(); ll++) rsp_labels[enc++] = cmbLabels[ll];
+      std::vector<Bond> tmp;
+      for (int p : picked) tmp.push_back(bonds[p]);
+      if (bonds[picked[0]].type() == BD_IN) RBnum += (int)picked.size();
+      newBonds.push_back(combine(tmp));
+      reduced[enc_r++] = labels[l];
+    } else if (marked[l] == 0) {
+      rsp_labels[enc++] = labels[l];
+      reduced[enc_r++] = labels[l];
+      if (bonds[l].type() == BD_IN) RBnum++;
+      newBonds.push_back(bonds[l]);
+    }
+  }
+  permute(rsp_labels, RBnum);
+  UniTensor out(newBonds, reduced, name);
+  if (out.m_elemNum != m_elemNum) throw std::runtime_error("combineBond: element counts differ");
+  bonds = std::move(out.bonds);
+  smap = std::move(out.smap);
+  RBondNum = out.RBondNum;
+  labels = reduced;
+  // the element buffer is reused as it lies
+  return *this;
+}
+
+UniTensor& UniTensor::operator*=(double a) {
+  if (elem) tn::launch_scale(dptr(elem), (int64_t)m_elemNum, a, C().stream);
+  C().launched();
+  return *this;
+}
+
+UniTensor operator*(const UniTensor& Ta, double a) {
+  UniTensor t(Ta);
+  t *= a;
+  return t;
+}
+
+UniTensor operator*(double a, const UniTensor& Ta) { return Ta * a; }
+
+UniTensor operator*(const UniTensor& Ta, const UniTensor& Tb) {
+  UniTensor a(Ta), b(Tb);
+  return contract(a, b, true);
+}
+
+UniTensor& UniTensor::operator*=(const UniTensor& Tb) {
+  *this = *this * Tb;
+  return *this;
+}
+
+// ---------------------------------------------------------------- contract
+// UniTensorTools.cpp:124-244
+UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast) {
+  if (!(Ta.status & Tb.status & UniTensor::HAVEELEM))
+    throw std::runtime_error("Cannot perform contraction of two tensors before setting their elements.");
+  if (&Ta == &Tb) {
+    UniTensor tmp = Tb;
+    return contract(Ta, tmp, fast);
+  }
+  if ((Ta.status & UniTensor::HAVEBOND) && (Tb.status & UniTensor::HAVEBOND)) {
+    const int an = (int)Ta.bonds.size(), bn = (int)Tb.bonds.size();
+    std::vector<int> oldLabelA = Ta.labels, oldLabelB = Tb.labels;
+    int oldRnumA = Ta.RBondNum, oldRnumB = Tb.RBondNum;
+    std::vector<int> newLabelA, interLabel, newLabelB, newLabelC, markB(bn, 0);
+    for (int a = 0; a < an; a++) {
+      bool match = false;
+      for (int b = 0; b < bn; b++)
+        if (Ta.labels[a] == Tb.labels[b]) {
+          markB[b] = 1;
+          interLabel.push_back(Ta.labels[a]);
+          newLabelB.push_back(Tb.labels[b]);
+          if (!(Ta.bonds[a].dim() == Tb.bonds[b].dim()))
+            throw std::runtime_error("Cannot contract two bonds having different dimensions");
+          match = true;
+          break;
+        }
+      if (!match) {
+        newLabelA.push_back(Ta.labels[a]);
+        newLabelC.push_back(Ta.labels[a]);
+      }
+    }
+    for (int l : interLabel) newLabelA.push_back(l);
+    for (int b = 0; b < bn; b++)
+      if (markB[b] == 0) {
+        newLabelB.push_back(Tb.labels[b]);
+        newLabelC.push_back(Tb.labels[b]);
+      }
+    const int conBond = (int)interLabel.size();
+    Ta.permute(newLabelA, an - conBond);
+    Tb.permute(newLabelB, conBond);
+    std::vector<Bond> cBonds;
+    for (int i = 0; i < an - conBond; i++) cBonds.push_back(Ta.bonds[i]);
+    for (int i = conBond; i < bn; i++) cBonds.push_back(Tb.bonds[i]);
+    UniTensor Tc(cBonds);
+    if (!cBonds.empty()) Tc.setLabel(newLabelC);
+    // every block of Ta with a block of the same charge in Tb is one sector GEMM
+    std::vector<tn_sector_gemm> list;
+    const tn::SectorMap* ma = Ta.smap.get();
+    const tn::SectorMap* mb = Tb.smap.get();
+    const tn::SectorMap* mc = Tc.smap.get();
+    for (const auto& ba : ma->blocks) {
+      int ib = mb->find_block(ba.q);
+      if (ib < 0) continue;
+      const auto& bb = mb->blocks[ib];
+      int ic = mc ? mc->find_block(ba.q) : 0;
+      int64_t crow = mc ? (ic >= 0 ? mc->blocks[ic].rows : -1) : 1;
+      int64_t ccol = mc ? (ic >= 0 ? mc->blocks[ic].cols : -1) : 1;
+      if (!(ba.rows == crow && bb.cols == ccol && ba.cols == bb.rows))
+        throw std::runtime_error("The dimensions the bonds to be contracted out are different.");
+      tn_sector_gemm g;
+      g.M = ba.rows;
+      g.N = bb.cols;
+      g.K = ba.cols;
+      g.a_off = ba.off;
+      g.b_off = bb.off;
+      g.c_off = mc ? mc->blocks[ic].off : 0;
+      list.push_back(g);
+    }
+    tn::run_sector_gemms(C(), g_mode, list, dptr(Ta.elem), dptr(Tb.elem), dptr(Tc.elem));
+    Tc.status |= UniTensor::HAVEELEM;
+    if (conBond == 0) {  // outer product (UniTensorTools.cpp:206-225)
+      int idx = 0;
+      for (int i = 0; i < oldRnumA; i++) newLabelC[idx++] = oldLabelA[i];
+      for (int i = 0; i < oldRnumB; i++) newLabelC[idx++] = oldLabelB[i];
+      for (int i = oldRnumA; i < an; i++) newLabelC[idx++] = oldLabelA[i];
+      for (int i = oldRnumB; i < bn; i++) newLabelC[idx++] = oldLabelB[i];
+      Tc.permute(newLabelC, oldRnumA + oldRnumB);
+    }
+    if (!fast) {
+      Ta.permute(oldLabelA, oldRnumA);
+      Tb.permute(oldLabelB, oldRnumB);
+    }
+    return Tc;
+  } else if (Ta.status & UniTensor::HAVEBOND) {
+    return Ta * Tb.at(0);
+  } else if (Tb.status & UniTensor::HAVEBOND) {
+    return Ta.at(0) * Tb;
+  }
+  return UniTensor(Ta.at(0) * Tb.at(0));
+}
+
+// UniTensorTools.cpp:96-122
+UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb) {
+  UniTensor T1 = Ta, T2 = Tb;
+  std::vector<int> label1(T1.bondNum()), label2(T2.bondNum());
+  for (size_t i = 0; i < T1.bondNum(); i++)
+    label1[i] = (i < T1.inBondNum()) ? (int)i : (int)(T2.inBondNum() + i);
+  for (size_t i = 0; i < T2.bondNum(); i++)
+    label2[i] = (i < T2.inBondNum()) ? (int)(i + T1.inBondNum()) : (int)(i + T1.bondNum());
+  T1.setLabel(label1);
+  T2.setLabel(label2);
+  return contract(T1, T2, true);
+}
+
+// ---------------------------------------------------------------- binary I/O
+// UniTensor::save layout (UniTensor.cpp:922-986)
+void UniTensor::save(const std::string& fname) const {
+  if ((status & HAVEBOND) == 0) throw std::runtime_error("Saving a tensor without bonds(scalar) is not supported.");
+  FILE* fp = std::fopen(fname.c_str(), "wb");
+  if (!fp) throw std::runtime_error("Error in writing to file '" + fname + "'.");
+  int rflag = 1, cflag = 0, namelen = (int)name.size(), st = status, bn = (int)bonds.size();
+  size_t qsz = sizeof(Qnum);
+  std::fwrite(&rflag, 4, 1, fp);
+  std::fwrite(&cflag, 4, 1, fp);
+  std::fwrite(&namelen, 4, 1, fp);
+  if (namelen) std::fwrite(name.data(), 1, namelen, fp);
+  std::fwrite(&st, 4, 1, fp);
+  std::fwrite(&bn, 4, 1, fp);
+  std::fwrite(&qsz, sizeof(size_t), 1, fp);
+  for (const auto& b : bonds) {
+    int t = b.type(), nq = (int)b.qnums().size();
+    std::fwrite(&t, 4, 1, fp);
+    std::fwrite(&nq, 4, 1, fp);
+    std::fwrite(b.qnums().data(), sizeof(Qnum), nq, fp);
+    std::fwrite(b.qdegs().data(), sizeof(int), nq, fp);
+  }
+  int nl = (int)labels.size();
+  std::fwrite(&nl, 4, 1, fp);
+  std::fwrite(labels.data(), sizeof(int), nl, fp);
+  if (status & HAVEELEM) {
+    size_t ne = m_elemNum;
+    std::fwrite(&ne, sizeof(size_t), 1, fp);
+    std::vector<double> h = hostElem();
+    std::fwrite(h.data(), sizeof(double), ne, fp);
+  }
+  std::fclose(fp);
+}
+
+UniTensor::UniTensor(const std::string& fname) : status(0) {
+  FILE* fp = std::fopen(fname.c_str(), "rb");
+  if (!fp) throw std::runtime_error("Error in opening file '" + fname + "'.");
+  auto rd = [&](void* p, size_t sz, size_t n) {
+    if (std::fread(p, sz, n, fp) != n) {
+      std::fclose(fp);
+      throw std::runtime_error("Error in reading file '" + fname + "' in.");
+    }
+  };
+  int rflag, cflag, namelen, st, bn;
+  size_t qsz;
+  rd(&rflag, 4, 1);
+  rd(&cflag, 4, 1);
+  rd(&namelen, 4, 1);
+  name.assign(namelen, ' ');
+  if (namelen) rd(&name[0], 1, namelen);
+  rd(&st, 4, 1);
+  rd(&bn, 4, 1);
+  rd(&qsz, sizeof(size_t), 1);
+  if (qsz != sizeof(Qnum) || rflag != 1) {
+    std::fclose(fp);
+    throw std::runtime_error("Error in reading file '" + fname + "' in.");
+  }
+  for (int b = 0; b < bn; b++) {
+    int t, nq;
+    rd(&t, 4, 1);
+    rd(&nq, 4, 1);
+    std::vector<Qnum> qn(nq);
+    std::vector<int> qd(nq);
+    rd(qn.data(), sizeof(Qnum), nq);
+    rd(qd.data(), sizeof(int), nq);
+    std::vector<Qnum> tot;
+    for (int q = 0; q < nq; q++)
+      for (int d = 0; d < qd[q]; d++) tot.push_back(qn[q]);
+    bonds.push_back(Bond((bondType)t, tot));
+  }
+  initUniT();
+  int nl;
+  rd(&nl, 4, 1);
+  std::vector<int> lab(nl);
+  rd(lab.data(), sizeof(int), nl);
+  if ((size_t)nl != bonds.size()) {
+    std::fclose(fp);
+    throw std::runtime_error("Error in reading file '" + fname + "' in.");
+  }
+  labels = lab;
+  if (st & HAVEELEM) {
+    size_t ne;
+    rd(&ne, sizeof(size_t), 1);
+    std::vector<double> h(m_elemNum);
+    rd(h.data(), sizeof(double), m_elemNum);
+    setElem(h.data(), false);
+  }
+  std::fclose(fp);
+}
+
+}  // namespace uni10

@@ -1,0 +1,227 @@
+"""Python mirror of the reference's UniTensor / Network operations on this
+path (the calls the reference's SWIG module, pyUni10, exposes), over the C
+ABI.  Bonds use the run-length form ``(btype, [(u1, prt, prtf, deg), ...])``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import capi
+from .capi import MODES, call, int_array, pack_bonds
+
+
+def _mode(mode) -> int:
+    return MODES[mode] if isinstance(mode, str) else int(mode)
+
+
+class SectorMap:
+    """Cached sector map of a bond signature (UniTensor::grouping)."""
+
+    def __init__(self, bonds):
+        self.bonds = bonds
+        h = C.c_void_p()
+        call("tn_sectormap_build", None, *pack_bonds(bonds), C.byref(h))
+        self.h = h
+        n, nb, rb = C.c_int64(), C.c_int(), C.c_int()
+        call("tn_sectormap_query", h, C.byref(n), C.byref(nb), C.byref(rb))
+        self.elem_num, self.nblocks, self.rbond_num = n.value, nb.value, rb.value
+
+    def blocks(self):
+        nb = self.nblocks
+        q = (C.c_int * (3 * nb))()
+        r, c, o = (C.c_int64 * nb)(), (C.c_int64 * nb)(), (C.c_int64 * nb)()
+        call("tn_sectormap_blocks", self.h, q, r, c, o)
+        return [((q[3 * i], q[3 * i + 1], q[3 * i + 2]), r[i], c[i], o[i]) for i in range(nb)]
+
+    def __del__(self):
+        try:
+            capi.lib().tn_sectormap_destroy(self.h)
+        except Exception:
+            pass
+
+
+def plan_check_permute(src: SectorMap, dst: SectorMap, rsp, src_host: np.ndarray) -> tuple[np.ndarray, int]:
+    """Run the permute kernel's tile walk on the CPU (no GPU)."""
+    s = np.ascontiguousarray(src_host, dtype=np.float64)
+    d = np.full(dst.elem_num, np.nan)
+    w = C.c_int64()
+    call("tn_plan_check_permute", src.h, dst.h, int_array(rsp), s.ctypes.data, d.ctypes.data, C.byref(w))
+    return d, w.value
+
+
+def permute_device(src: SectorMap, dst: SectorMap, rsp, src_ptr: int, dst_ptr: int) -> None:
+    call("tn_permute", None, src.h, dst.h, int_array(rsp), src_ptr, dst_ptr)
+
+
+def contract_sectors(mode, gemms, a_ptr: int, b_ptr: int, c_ptr: int) -> None:
+    arr = (capi.SectorGemm * max(1, len(gemms)))(*[capi.SectorGemm(*g) for g in gemms])
+    call("tn_contract_sectors", None, _mode(mode), len(gemms), arr, a_ptr, b_ptr, c_ptr)
+
+
+def sync() -> None:
+    call("tn_ctx_sync", None)
+
+
+def set_stream(stream_handle: int) -> None:
+    call("tn_ctx_set_stream", None, C.c_void_p(stream_handle))
+
+
+def prof_enable(on: bool) -> None:
+    call("tn_prof_enable", None, int(bool(on)))
+
+
+def prof_read() -> dict:
+    cap = 64
+    names = C.create_string_buffer(32 * cap)
+    ms, by, fl = (C.c_double * cap)(), (C.c_double * cap)(), (C.c_double * cap)()
+    la = (C.c_int64 * cap)()
+    n = C.c_int()
+    call("tn_prof_read", None, cap, names, ms, la, by, fl, C.byref(n))
+    out = {}
+    for i in range(n.value):
+        nm = names.raw[32 * i : 32 * i + 32].split(b"\0")[0].decode()
+        out[nm] = {"ms": ms[i], "launches": la[i], "bytes": by[i], "flops": fl[i]}
+    return out
+
+
+def launch_count() -> int:
+    n = C.c_int64()
+    call("tn_ctx_launch_count", None, C.byref(n))
+    return n.value
+
+
+class UniTensor:
+    """Handle to a device-resident uni10::UniTensor."""
+
+    def __init__(self, bonds=None, labels=None, elem=None, _h=None):
+        if _h is not None:
+            self.h = _h
+        else:
+            h = C.c_void_p()
+            call("tn_tensor_create", None, *pack_bonds(bonds), C.byref(h))
+            self.h = h
+            if labels is not None:
+                self.set_label(labels)
+            if elem is not None:
+                self.set_elem(elem)
+
+    def __del__(self):
+        try:
+            if getattr(self, "h", None):
+                capi.lib().tn_tensor_destroy(self.h)
+        except Exception:
+            pass
+
+    # -- elements
+    def elem_num(self) -> int:
+        n = C.c_int64()
+        call("tn_tensor_device_elem", self.h, None, C.byref(n))
+        return n.value
+
+    def device_ptr(self) -> int:
+        p = C.c_void_p()
+        call("tn_tensor_device_elem", self.h, C.byref(p), None)
+        return p.value or 0
+
+    def set_elem(self, a) -> None:
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        call("tn_tensor_set_elem", self.h, a.ctypes.data, a.size)
+
+    def set_elem_host_ptr(self, ptr: int, n: int) -> None:
+        call("tn_tensor_set_elem", self.h, ptr, n)
+
+    def get_elem(self) -> np.ndarray:
+        out = np.empty(self.elem_num())
+        call("tn_tensor_get_elem", self.h, out.ctypes.data, out.size)
+        return out
+
+    # -- labels / bonds
+    def set_label(self, labels) -> None:
+        call("tn_tensor_set_label", self.h, len(labels), int_array(labels))
+
+    def labels(self) -> list[int]:
+        n = C.c_int()
+        call("tn_tensor_get_labels", self.h, None, C.byref(n))
+        buf = (C.c_int * max(1, n.value))()
+        call("tn_tensor_get_labels", self.h, buf, C.byref(n))
+        return list(buf[: n.value])
+
+    def bonds(self):
+        nb = C.c_int()
+        cap = 4096
+        bt, nq = (C.c_int * 64)(), (C.c_int * 64)()
+        q, d = (C.c_int * (3 * cap))(), (C.c_int * cap)()
+        call("tn_tensor_bonds", self.h, C.byref(nb), bt, nq, q, d, cap)
+        out, r = [], 0
+        for b in range(nb.value):
+            runs = []
+            for _ in range(nq[b]):
+                runs.append((q[3 * r], q[3 * r + 1], q[3 * r + 2], d[r]))
+                r += 1
+            out.append((bt[b], runs))
+        return out
+
+    def sector_map(self) -> SectorMap:
+        return SectorMap(self.bonds())
+
+    # -- the path
+    def permute(self, new_labels, in_bond_num: int) -> "UniTensor":
+        call("tn_tensor_permute", self.h, len(new_labels), int_array(new_labels), in_bond_num)
+        return self
+
+    def transpose(self) -> "UniTensor":
+        call("tn_tensor_transpose", self.h)
+        return self
+
+    def combine_bond(self, labels) -> "UniTensor":
+        call("tn_tensor_combine_bond", self.h, len(labels), int_array(labels))
+        return self
+
+    def copy(self) -> "UniTensor":
+        h = C.c_void_p()
+        call("tn_tensor_copy", self.h, C.byref(h))
+        return UniTensor(_h=h)
+
+    def scale(self, a: float) -> "UniTensor":
+        call("tn_tensor_scale", self.h, C.c_double(a))
+        return self
+
+
+def contract(a: UniTensor, b: UniTensor, fast: bool = False, mode="fp64") -> UniTensor:
+    h = C.c_void_p()
+    call("tn_contract", a.h, b.h, int(bool(fast)), _mode(mode), C.byref(h))
+    return UniTensor(_h=h)
+
+
+def otimes(a: UniTensor, b: UniTensor, mode="fp64") -> UniTensor:
+    h = C.c_void_p()
+    call("tn_otimes", a.h, b.h, _mode(mode), C.byref(h))
+    return UniTensor(_h=h)
+
+
+class Network:
+    def __init__(self, text: str):
+        h = C.c_void_p()
+        call("tn_network_create", None, text.encode(), C.byref(h))
+        self.h = h
+
+    def __del__(self):
+        try:
+            capi.lib().tn_network_destroy(self.h)
+        except Exception:
+            pass
+
+    def put_tensor(self, name: str, t: UniTensor) -> None:
+        call("tn_network_put_tensor", self.h, name.encode(), t.h)
+
+    def launch(self, mode="fp64") -> UniTensor:
+        h = C.c_void_p()
+        call("tn_network_launch", self.h, _mode(mode), C.byref(h))
+        return UniTensor(_h=h)
+
+    def tree(self) -> str:
+        buf = C.create_string_buffer(4096)
+        call("tn_network_tree", self.h, buf, 4096)
+        return buf.value.decode()
