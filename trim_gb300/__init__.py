@@ -11,6 +11,6 @@ __all__ = ["capi", "build"]
 
 
 def build(verbose: bool = False) -> str:
-    from .build import build as _b
+    from .buildlib import build as _b
 
     return _b(verbose=verbose)

@@ -1,7 +1,7 @@
 """ctypes binding of the C ABI in include/trim_gb300.h.
 
 The product path: every call goes into the in-tree libtrim_gb300.so (built by
-trim_gb300/build.py).  There is no fallback -- if the library is missing the
+trim_gb300/buildlib.py).  There is no fallback -- if the library is missing the
 import fails loudly.
 """
 from __future__ import annotations
@@ -94,7 +94,7 @@ def lib() -> C.CDLL:
     global _lib
     if _lib is None:
         if not os.path.exists(LIB_PATH):
-            raise ImportError(f"trim_gb300 extension not built: {LIB_PATH} missing (run trim_gb300/build.py)")
+            raise ImportError(f"trim_gb300 extension not built: {LIB_PATH} missing (run trim_gb300/buildlib.py)")
         L = C.CDLL(LIB_PATH)
         for name, (res, args) in _PROTOS.items():
             fn = getattr(L, name)
