@@ -119,6 +119,24 @@ int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const do
 int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A,
                         const double* B, double* C);
 
+/* Fixed-scratch variant of tn_contract_sectors in TN_MODE_FP64, for callers
+ * that cannot allocate device memory (a host framework that has reserved the
+ * GPU for its own allocator under a hard cap, a latency-critical loop that
+ * must not enter the allocator, a plugin host that forbids device allocation
+ * after start-up).  It has no counterpart in the reference.
+ * Its tile list and split-K partial tiles live in one file-scope device array
+ * of TN_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library until
+ * the process exits; it calls no cudaMalloc/cudaFree or allocating library
+ * routine.  The caller passes A, B, C (device) and the stream (NULL: legacy
+ * default stream).  The first call on a device looks up the array's device
+ * address (cudaGetSymbolAddress, that device current): make it before any
+ * stream capture.  Work that needs more output tiles than the array holds is
+ * rejected with TN_ERR_ARG.  All calls share the array: calls that overlap on
+ * the GPU race, so order them (one stream). */
+#define TN_NOALLOC_SCRATCH_BYTES (8u << 20)
+int tn_contract_sectors_fp64_noalloc(void* cuda_stream, int n, const tn_sector_gemm* list, const double* A,
+                                     const double* B, double* C);
+
 /* ---- tensor level (UniTensor, tensor-network/UniTensor.h) -------------- */
 /* UniTensor(const std::vector<Bond>&, const std::string& name) (UniTensor.h:326) */
 int tn_tensor_create(tn_ctx_t ctx, int nbonds, const int* btype, const int* nq, const int* qnum,

@@ -56,6 +56,7 @@ _PROTOS = {
     "tn_permute": (_I, [_P, _P, _P, _IP, _DP, _DP]),
     "tn_plan_check_permute": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
     "tn_contract_sectors": (_I, [_P, _I, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
+    "tn_contract_sectors_fp64_noalloc": (_I, [_P, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
     "tn_tensor_create": (_I, [_P, _I, _IP, _IP, _IP, _IP, C.POINTER(_P)]),
     "tn_tensor_destroy": (_I, [_P]),
     "tn_tensor_copy": (_I, [_P, C.POINTER(_P)]),

@@ -17,6 +17,8 @@ std::vector<tn::BondSig> to_sigs(const std::vector<Bond>& bonds);
 }
 namespace tn {
 Ctx* create_ctx(int device);
+void contract_sectors_fp64_noalloc(cudaStream_t stream, const std::vector<tn_sector_gemm>& list, const double* A,
+                                   const double* B, double* C);
 }
 
 struct tn_smap_s {
@@ -253,6 +255,17 @@ int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* lis
     need(list, "list");
     std::vector<tn_sector_gemm> l(list, list + n);
     tn::run_sector_gemms(*tn::as_ctx(ctx), mode, l, A, B, C);
+  });
+}
+
+int tn_contract_sectors_fp64_noalloc(void* stream, int n, const tn_sector_gemm* list, const double* A,
+                                     const double* B, double* C) {
+  return guard([&] {
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative sector count");
+    if (n == 0) return;
+    need(list, "list");
+    std::vector<tn_sector_gemm> l(list, list + n);
+    tn::contract_sectors_fp64_noalloc((cudaStream_t)stream, l, A, B, C);
   });
 }
 

@@ -197,6 +197,12 @@ void run_permute(Ctx& ctx, const PermPlan& plan, const double* src, double* dst)
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A,
                       const double* B, double* C);
 
+// FP64 tile plan: 16x32 output tiles, K split until ~4 items per SM; with
+// ws_cap_elems >= 0 the split is dropped when its partial tiles would need
+// more workspace than that (ws_elems receives the workspace needed).
+std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num_sms, int64_t ws_cap_elems,
+                                int64_t* ws_elems);
+
 // kernel launchers (defined in the .cu files)
 void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles,
                            const double* src, double* dst, int grid, cudaStream_t s);

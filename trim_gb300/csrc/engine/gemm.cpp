@@ -15,7 +15,8 @@ void run_split_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list
 namespace {
 constexpr int kTileM = 16, kTileN = 32;
 
-std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num_sms, int64_t* ws_elems) {
+std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, int num_sms, bool allow_split,
+                                      int64_t* ws_elems) {
   int64_t tiles = 0, work = 0;
   for (const auto& g : list) {
     int64_t t = ((g.M + kTileM - 1) / kTileM) * ((g.N + kTileN - 1) / kTileN);
@@ -29,7 +30,7 @@ std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX || g.N > INT32_MAX || g.K > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large");
     int nsplit = 1;
-    if (tiles < target) {
+    if (allow_split && tiles < target) {
       // spread the K loop so the whole chip shares the FP64 work
       nsplit = (int)std::min<int64_t>((target + tiles - 1) / tiles, (g.K + 15) / 16);
       nsplit = std::max(1, std::min(nsplit, 64));
@@ -68,6 +69,13 @@ std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num
 }
 }  // namespace
 
+std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num_sms, int64_t ws_cap_elems,
+                                int64_t* ws_elems) {
+  std::vector<GemmTile> t = plan_fp64_split(list, num_sms, true, ws_elems);
+  if (ws_cap_elems >= 0 && *ws_elems > ws_cap_elems) t = plan_fp64_split(list, num_sms, false, ws_elems);
+  return t;
+}
+
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
                       double* C) {
   if (list.empty()) return;
@@ -77,7 +85,7 @@ void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& lis
   }
   if (mode != TN_MODE_FP64) fail(TN_ERR_ARG, "unknown contraction mode");
   int64_t ws_elems = 0;
-  std::vector<GemmTile> tiles = plan_fp64(list, ctx.num_sms, &ws_elems);
+  std::vector<GemmTile> tiles = plan_fp64(list, ctx.num_sms, -1, &ws_elems);
   if (tiles.empty()) return;
   DevBuf dtiles(tiles.size() * sizeof(GemmTile), ctx);
   TN_CUDA(cudaMemcpyAsync(dtiles.ptr, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice,
