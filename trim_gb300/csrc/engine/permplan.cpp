@@ -37,16 +37,19 @@ void choose_tile(PermSub& ps) {
       if (y < 0 || ps.sstride[i] < ps.sstride[y]) y = i;
     if (y >= 0 && ps.sstride[y] > ps.sstride[x]) y = -1;
   }
+  // tiles hold at most 4096 elements (16 per thread of a 256-thread CTA);
+  // transpose tiles also fit a 64 x 65 shared-memory array
   if (y >= 0) {
     ps.mode = 1;
     ps.ydim = y;
-    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 32);
-    ps.ty = (int32_t)std::min<int64_t>(ps.dims[y], std::min<int64_t>(512, std::max<int64_t>(32, 1024 / ps.tx)));
+    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 64);
+    int64_t ty = std::min<int64_t>(4096 / ps.tx, (64 * 65) / (ps.tx + 1));
+    ps.ty = (int32_t)std::min<int64_t>(ps.dims[y], std::min<int64_t>(ty, 1024));
   } else {
-    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 1024);
+    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 4096);
     if (n >= 2) {
       ps.ydim = n - 2;
-      ps.ty = (int32_t)std::min<int64_t>(ps.dims[n - 2], std::max<int64_t>(1, 2048 / ps.tx));
+      ps.ty = (int32_t)std::min<int64_t>(ps.dims[n - 2], std::max<int64_t>(1, 4096 / ps.tx));
     } else {
       ps.ty = 1;
     }
@@ -242,7 +245,8 @@ static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermS
 
 void run_permute(Ctx& ctx, const PermPlan& plan, const double* src, double* dst) {
   if (plan.ntiles == 0) return;
-  int64_t grid = std::min<int64_t>(plan.ntiles, (int64_t)ctx.num_sms * 8);
+  // persistent: two resident CTAs per SM (100 KB of staging shared memory each)
+  int64_t grid = std::min<int64_t>(plan.ntiles, (int64_t)ctx.num_sms * 2);
   ProfScope ps(ctx, "permute", 16.0 * plan.elem_num, 0);
   launch_permute_kernel((const PermSub*)plan.subs->ptr, (const int64_t*)plan.tile_start->ptr, plan.nsub, plan.ntiles,
                         src, dst, (int)grid, ctx.stream);

@@ -14,8 +14,8 @@ namespace tn {
 namespace {
 
 constexpr int kThreads = 256;
-constexpr int kPerThread = 8;  // tile <= 2048 elements
-constexpr int kSmem = 1600;    // >= max ty * (tx + 1) over the tile shapes
+constexpr int kPerThread = 16;  // tile <= 4096 elements: 16 loads in flight per thread
+constexpr int kSmem = 64 * 65;  // >= ty * (tx + 1) of every transpose tile (checked on the host)
 
 struct TileInfo {
   int64_t bs, bd;     // base offsets of the tile origin
@@ -50,16 +50,32 @@ __host__ __device__ inline TileInfo decode_tile(const PermSub& P, int64_t local)
     w.mode = 0;
   } else {
     const int x = n - 1, y = P.ydim;
-    int64_t xt = local % P.ntx;
-    local /= P.ntx;
-    int64_t yt = local % P.nty;
-    local /= P.nty;
-    for (int i = n - 1; i >= 0; --i) {  // outer dims, innermost first
-      if (i == x || i == y) continue;
-      int64_t c = local % P.dims[i];
-      local /= P.dims[i];
-      bs += c * P.sstride[i];
-      bd += c * P.dstride[i];
+    int64_t xt, yt;
+    if (local < 0x7fffffffLL) {  // 32-bit division is several times cheaper
+      uint32_t l = (uint32_t)local;
+      xt = l % (uint32_t)P.ntx;
+      l /= (uint32_t)P.ntx;
+      yt = l % (uint32_t)P.nty;
+      l /= (uint32_t)P.nty;
+      for (int i = n - 1; i >= 0 && l; --i) {  // outer dims, innermost first
+        if (i == x || i == y) continue;
+        uint32_t c = l % (uint32_t)P.dims[i];
+        l /= (uint32_t)P.dims[i];
+        bs += (int64_t)c * P.sstride[i];
+        bd += (int64_t)c * P.dstride[i];
+      }
+    } else {
+      xt = local % P.ntx;
+      local /= P.ntx;
+      yt = local % P.nty;
+      local /= P.nty;
+      for (int i = n - 1; i >= 0; --i) {
+        if (i == x || i == y) continue;
+        int64_t c = local % P.dims[i];
+        local /= P.dims[i];
+        bs += c * P.sstride[i];
+        bd += c * P.dstride[i];
+      }
     }
     int64_t x0 = xt * P.tx;
     bs += x0 * P.sstride[x];
@@ -88,75 +104,133 @@ __host__ __device__ inline TileInfo decode_tile(const PermSub& P, int64_t local)
   return w;
 }
 
-__global__ void __launch_bounds__(kThreads) permute_kernel(const PermSub* __restrict__ subs,
-                                                           const int64_t* __restrict__ tile_start, int nsub,
-                                                           int64_t ntiles, const double* __restrict__ src,
-                                                           double* __restrict__ dst) {
-  __shared__ double tile[kSmem];
-  __shared__ TileInfo ti;
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    if (threadIdx.x == 0) {
-      const PermSub& P = subs[find_sub(tile_start, nsub, t)];
-      ti = decode_tile(P, t - P.tile_begin);
-    }
-    __syncthreads();
-    const TileInfo w = ti;
+__device__ __forceinline__ void cp_async8(double* smem, const double* gmem) {
+  unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+constexpr int kStages = 3;  // tiles in flight per CTA: 2 loading while 1 is stored
+
+// Issue the asynchronous loads of tile t into one stage buffer.  Mode 0 keeps
+// the tile as [y][x] (pitch tx), mode 1 as [y][x] with pitch tx + 1; loads
+// run with lanes along x (mode 0) or along y, the source-contiguous dim
+// (mode 1).  Thread 0 records the tile's decode for the store phase.
+__device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, const int64_t* __restrict__ tile_start,
+                                           int nsub, int64_t ntiles, int64_t t, const double* __restrict__ src,
+                                           double* buf, TileInfo* info) {
+  if (t < ntiles) {
+    const PermSub& P = subs[find_sub(tile_start, nsub, t)];
+    const TileInfo w = decode_tile(P, t - P.tile_begin);
+    if (threadIdx.x == 0) *info = w;
     if (w.mode == 0) {
-      // lanes along x for both sides; linear walk of the (y, x) tile in steps
-      // of kThreads = q rows + r columns
       const int q = kThreads / w.tx, r = kThreads - q * w.tx;
       const int y0 = threadIdx.x / w.tx, x0 = threadIdx.x - y0 * w.tx;
-      double v[kPerThread];
-      int yy = y0, xx = x0;
-#pragma unroll
-      for (int k = 0; k < kPerThread; k++) {
-        if (yy < w.ny && xx < w.nx) v[k] = src[w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx];
-        xx += r;
-        yy += q;
-        if (xx >= w.tx) { xx -= w.tx; yy++; }
-      }
-      yy = y0;
-      xx = x0;
-#pragma unroll
-      for (int k = 0; k < kPerThread; k++) {
-        if (yy < w.ny && xx < w.nx) dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx] = w.neg ? -v[k] : v[k];
-        xx += r;
-        yy += q;
-        if (xx >= w.tx) { xx -= w.tx; yy++; }
-      }
-    } else {
-      // load with lanes along y (source-contiguous) into tile[y][x] ...
-      const int pitch = w.tx + 1;
-      {
-        const int q = kThreads / w.ty, r = kThreads - q * w.ty;
-        int xx = threadIdx.x / w.ty, yy = threadIdx.x - xx * w.ty;
-#pragma unroll
-        for (int k = 0; k < kPerThread; k++) {
-          if (xx < w.nx && yy < w.ny) tile[yy * pitch + xx] = src[w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx];
-          yy += r;
-          xx += q;
-          if (yy >= w.ty) { yy -= w.ty; xx++; }
+      if (r == 0) {  // constant step: q whole rows
+        if (x0 < w.nx) {
+          const double* g = src + w.bs + (int64_t)y0 * w.sy + (int64_t)x0 * w.sx;
+          const int64_t gstep = (int64_t)q * w.sy;
+          double* sp = buf + y0 * w.tx + x0;
+          const int sstep = q * w.tx;
+          for (int y = y0; y < w.ny; y += q, g += gstep, sp += sstep) cp_async8(sp, g);
         }
-      }
-      __syncthreads();
-      // ... store with lanes along x (destination-contiguous)
-      {
-        const int q = kThreads / w.tx, r = kThreads - q * w.tx;
-        int yy = threadIdx.x / w.tx, xx = threadIdx.x - yy * w.tx;
-#pragma unroll
+      } else {
+        int yy = y0, xx = x0;
+#pragma unroll 4
         for (int k = 0; k < kPerThread; k++) {
-          if (yy < w.ny && xx < w.nx) {
-            double v = tile[yy * pitch + xx];
-            dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx] = w.neg ? -v : v;
-          }
+          if (yy < w.ny && xx < w.nx) cp_async8(buf + yy * w.tx + xx, src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx);
           xx += r;
           yy += q;
           if (xx >= w.tx) { xx -= w.tx; yy++; }
         }
       }
+    } else {
+      const int pitch = w.tx + 1;
+      const int q = kThreads / w.ty, r = kThreads - q * w.ty;
+      const int x0 = threadIdx.x / w.ty, y0 = threadIdx.x - x0 * w.ty;
+      if (r == 0) {  // constant step: q whole columns
+        if (y0 < w.ny) {
+          const double* g = src + w.bs + (int64_t)y0 * w.sy + (int64_t)x0 * w.sx;
+          const int64_t gstep = (int64_t)q * w.sx;
+          double* sp = buf + y0 * pitch + x0;
+          for (int x = x0; x < w.nx; x += q, g += gstep, sp += q) cp_async8(sp, g);
+        }
+      } else {
+        int xx = x0, yy = y0;
+#pragma unroll 4
+        for (int k = 0; k < kPerThread; k++) {
+          if (xx < w.nx && yy < w.ny) cp_async8(buf + yy * pitch + xx, src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx);
+          yy += r;
+          xx += q;
+          if (yy >= w.ty) { yy -= w.ty; xx++; }
+        }
+      }
     }
-    __syncthreads();  // ti and tile are rewritten by the next tile
   }
+  cp_async_commit();  // one group per issue, empty past the end, so the counting stays uniform
+}
+
+// Store a landed tile from shared memory with lanes along x (destination-contiguous).
+__device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf, double* __restrict__ dst) {
+  const int pitch = w.mode == 0 ? w.tx : w.tx + 1;
+  const int q = kThreads / w.tx, r = kThreads - q * w.tx;
+  const int y0 = threadIdx.x / w.tx, x0 = threadIdx.x - y0 * w.tx;
+  if (r == 0) {  // constant step: q whole rows
+    if (x0 < w.nx) {
+      const double* sp = buf + y0 * pitch + x0;
+      const int sstep = q * pitch;
+      double* g = dst + w.bd + (int64_t)y0 * w.dy + (int64_t)x0 * w.dx;
+      const int64_t gstep = (int64_t)q * w.dy;
+      if (w.neg) {
+        for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = -*sp;
+      } else {
+        for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = *sp;
+      }
+    }
+    return;
+  }
+  int yy = y0, xx = x0;
+#pragma unroll 4
+  for (int k = 0; k < kPerThread; k++) {
+    if (yy < w.ny && xx < w.nx) {
+      double v = buf[yy * pitch + xx];
+      dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx] = w.neg ? -v : v;
+    }
+    xx += r;
+    yy += q;
+    if (xx >= w.tx) { xx -= w.tx; yy++; }
+  }
+}
+
+// Persistent pipeline over the tiles t = blockIdx.x + i * gridDim.x: the
+// loads of tiles i+1 and i+2 are in flight while tile i is written out.
+__global__ void __launch_bounds__(kThreads, 2) permute_kernel(const PermSub* __restrict__ subs,
+                                                              const int64_t* __restrict__ tile_start, int nsub,
+                                                              int64_t ntiles, const double* __restrict__ src,
+                                                              double* __restrict__ dst) {
+  extern __shared__ double smem[];  // kStages * kSmem doubles
+  __shared__ TileInfo info[kStages];
+  const int64_t G = gridDim.x;
+  int64_t t_issue = blockIdx.x;
+#pragma unroll
+  for (int s = 0; s < kStages - 1; s++, t_issue += G)
+    issue_tile(subs, tile_start, nsub, ntiles, t_issue, src, smem + s * kSmem, &info[s]);
+  int stage = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += G) {
+    const int ns = (stage + kStages - 1) % kStages;  // stored in the previous iteration
+    issue_tile(subs, tile_start, nsub, ntiles, t_issue, src, smem + ns * kSmem, &info[ns]);
+    t_issue += G;
+    cp_async_wait<kStages - 1>();  // this thread's loads of tile t have landed
+    __syncthreads();               // ... and every other thread's
+    store_tile(info[stage], smem + stage * kSmem, dst);
+    __syncthreads();  // the stage is reloaded in the next iteration
+    stage = (stage + 1) % kStages;
+  }
+  cp_async_wait<0>();
 }
 
 __global__ void fill_kernel(double* __restrict__ p, int64_t n, double v) {
@@ -195,7 +269,13 @@ int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double*
 
 void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles,
                            const double* src, double* dst, int grid, cudaStream_t s) {
-  permute_kernel<<<grid, kThreads, 0, s>>>(subs, tile_start, nsub, ntiles, src, dst);
+  const size_t smem = (size_t)kStages * kSmem * sizeof(double);
+  static bool attr = false;  // once per process; the attribute is per function
+  if (!attr) {
+    TN_CUDA(cudaFuncSetAttribute(permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr = true;
+  }
+  permute_kernel<<<grid, kThreads, smem, s>>>(subs, tile_start, nsub, ntiles, src, dst);
   TN_CUDA(cudaGetLastError());
 }
 
