@@ -1,0 +1,150 @@
+"""Tensor-core sector GEMMs (tcgen05): split precision must stay within
+1e-12 relative Frobenius error of FP64 on every workload; the fast BF16 mode
+is reported with its (BF16-level) error."""
+import numpy as np
+import pytest
+
+from tests import golden_data as G
+from trim_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+SPLIT_TOL = 1e-12
+
+
+@pytest.fixture(scope="module")
+def env():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from trim_gb300 import capi
+    from trim_gb300 import uni10 as tu
+
+    tu.set_stream(torch.cuda.current_stream().cuda_stream)
+    return torch, capi, tu
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300))
+
+
+def _sectors(shapes):
+    out, ao, bo, co = [], 0, 0, 0
+    for m, n, k in shapes:
+        out.append((m, n, k, ao, bo, co))
+        ao += m * k
+        bo += k * n
+        co += m * n
+    return out, ao, bo, co
+
+
+def _grouped(env, mode, shapes, seed, dist="uniform"):
+    torch, capi, tu = env
+    gemms, na, nb, nc = _sectors(shapes)
+    rng = np.random.default_rng(seed)
+    if dist == "uniform":
+        a, b = rng.uniform(-1, 1, na), rng.uniform(-1, 1, nb)
+    else:
+        a, b = rng.standard_normal(na), rng.standard_normal(nb)
+    A = torch.from_numpy(a).cuda()
+    B = torch.from_numpy(b).cuda()
+    Cd = torch.zeros(nc, dtype=torch.float64, device="cuda")
+    tu.contract_sectors(mode, gemms, A.data_ptr(), B.data_ptr(), Cd.data_ptr())
+    tu.sync()
+    c = Cd.cpu().numpy()
+    errs = []
+    for m, n, k, ao, bo, co in gemms:
+        want = a[ao:ao + m * k].reshape(m, k) @ b[bo:bo + k * n].reshape(k, n)
+        errs.append(rel(c[co:co + m * n].reshape(m, n), want))
+    return errs
+
+
+def test_split_single_tile(env):
+    errs = _grouped(env, "split", [(128, 64, 64)], 1)
+    assert errs[0] <= SPLIT_TOL, errs
+
+
+def test_split_ragged_shapes(env):
+    shapes = [(1, 1, 1), (2, 3, 5), (33, 17, 9), (130, 70, 65), (127, 63, 129)]
+    errs = _grouped(env, "split", shapes, 2)
+    assert max(errs) <= SPLIT_TOL, errs
+
+
+def test_split_long_k_chunks(env):
+    # several 256-k exact-accumulation chunks and a Gaussian operand
+    errs = _grouped(env, "split", [(200, 150, 700), (64, 64, 3000)], 3, dist="normal")
+    assert max(errs) <= SPLIT_TOL, errs
+
+
+def test_split_wide_dynamic_range(env):
+    torch, capi, tu = env
+    m, n, k = 96, 80, 300
+    rng = np.random.default_rng(4)
+    a = rng.uniform(-1, 1, (m, k)) * np.exp2(rng.integers(-30, 30, (m, 1)))  # rows at very different scales
+    b = rng.uniform(-1, 1, (k, n)) * np.exp2(rng.integers(-30, 30, (1, n)))
+    A = torch.from_numpy(a.ravel()).cuda()
+    B = torch.from_numpy(b.ravel()).cuda()
+    Cd = torch.zeros(m * n, dtype=torch.float64, device="cuda")
+    tu.contract_sectors("split", [(m, n, k, 0, 0, 0)], A.data_ptr(), B.data_ptr(), Cd.data_ptr())
+    tu.sync()
+    c = Cd.cpu().numpy().reshape(m, n)
+    want = a @ b
+    # per-row/column scaling keeps every entry accurate relative to its row x
+    # column scale: each operand carries 49 bits below its row/column maximum,
+    # so an entry's error stays under K * 2^-46 of (row max * column max)
+    scale = np.abs(a).max(1, keepdims=True) * np.abs(b).max(0, keepdims=True)
+    assert np.max(np.abs(c - want) / scale) <= k * 2.0 ** -46
+    assert rel(c, want) <= SPLIT_TOL
+
+
+def test_fast_bf16_reports_bf16_level_error(env):
+    errs = _grouped(env, "bf16", [(128, 64, 256), (50, 40, 30)], 5)
+    assert max(errs) <= 1e-2, errs
+
+
+def test_split_contract_golden_cases(env):
+    torch, capi, tu = env
+    for case in [c for c in G.cases().values() if c["kind"] == "contract"]:
+        a = tu.UniTensor(G.bonds_of(case["A"]), case["A"]["labels"], G.arr(case["id"], "A"))
+        b = tu.UniTensor(G.bonds_of(case["B"]), case["B"]["labels"], G.arr(case["id"], "B"))
+        c = tu.contract(a, b, mode="split")
+        assert rel(c.get_elem(), G.arr(case["id"], "C")) <= SPLIT_TOL, case["id"]
+
+
+def test_split_itebd_network(env):
+    torch, capi, tu = env
+    spec = wl.itebd()
+    rng = np.random.default_rng(spec["seed"])
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    net = tu.Network(spec["net"])
+    keep = []
+    for s in spec["tensors"]:
+        t = tu.UniTensor(s.bonds, s.labels, els[s.name])
+        keep.append(t)
+        net.put_tensor(s.name, t)
+    th = net.launch(mode="split")
+    assert rel(th.get_elem(), G.arr("itebd", "TH")) <= SPLIT_TOL
+
+
+def test_split_mera_and_ipeps_small(env):
+    torch, capi, tu = env
+    c = G.cases()["mera_small"]
+    spec = wl.mera(**c["params"])
+    rng = np.random.default_rng(0)
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    for dname, netx in spec["nets"].items():
+        net = tu.Network(netx)
+        keep = []
+        for s in spec["tensors"]:
+            t = tu.UniTensor(s.bonds, s.labels, els[s.name])
+            keep.append(t)
+            net.put_tensor(s.name, t)
+        r = net.launch(mode="split")
+        assert rel(r.get_elem(), G.arr("mera_small", dname)) <= SPLIT_TOL, dname
+    c = G.cases()["batched_small"]
+    spec = wl.batched(**c["params"])
+    for i, (t1, t2) in enumerate(spec["pairs"]):
+        a = tu.UniTensor(t1.bonds, t1.labels, G.arr("batched_small", t1.name))
+        b = tu.UniTensor(t2.bonds, t2.labels, G.arr("batched_small", t2.name))
+        r = tu.contract(a, b, mode="split")
+        assert rel(r.get_elem(), G.arr("batched_small", f"C{i}")) <= SPLIT_TOL

@@ -118,7 +118,7 @@ int tn_ctx_set_stream(tn_ctx_t ctx, void* stream) {
   });
 }
 
-int tn_ctx_sync(tn_ctx_t ctx) { return guard([&] { TN_CUDA(cudaStreamSynchronize(tn::as_ctx(ctx)->stream)); }); }
+int tn_ctx_sync(tn_ctx_t ctx) { return guard([&] { tn::as_ctx(ctx)->check_device_error(); }); }
 
 int tn_ctx_launch_count(tn_ctx_t ctx, int64_t* count) {
   return guard([&] {
@@ -307,7 +307,7 @@ int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n) {
     need(host, "host");
     tn::Ctx* c = tn::default_ctx();
     TN_CUDA(cudaMemcpyAsync(host, t->t.getElem(), n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    TN_CUDA(cudaStreamSynchronize(c->stream));
+    c->check_device_error();
   });
 }
 

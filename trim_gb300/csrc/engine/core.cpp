@@ -231,6 +231,25 @@ ProfScope::~ProfScope() {
   c->prof_recs.push_back(rec);
 }
 
+int* Ctx::device_error_word() {
+  if (!err_word) {
+    err_word = std::make_shared<DevBuf>(sizeof(int), *this);
+    TN_CUDA(cudaMemsetAsync(err_word->ptr, 0, sizeof(int), stream));
+  }
+  return (int*)err_word->ptr;
+}
+
+void Ctx::check_device_error() {
+  TN_CUDA(cudaStreamSynchronize(stream));
+  if (!err_word) return;
+  int e = 0;
+  TN_CUDA(cudaMemcpy(&e, err_word->ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e) {
+    TN_CUDA(cudaMemset(err_word->ptr, 0, sizeof(int)));
+    fail(e, "a device-side wait gave up (bounded spin limit reached); results of the last kernels are invalid");
+  }
+}
+
 static std::mutex g_ctx_mu;
 static std::map<int, Ctx*> g_default;
 

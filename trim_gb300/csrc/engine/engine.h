@@ -146,6 +146,16 @@ struct GemmTile {
   int64_t ws_off;               // partial-tile slot in the workspace (elements), -1 if nsplit==1
 };
 
+// Tensor-core sector GEMM (split precision / fast BF16): one contraction's
+// sectors, their slice images in the workspace and their scale exponents.
+struct TcSector {
+  int64_t a_off, b_off, c_off;  // operand / output element offsets
+  int64_t a_img, b_img;         // byte offsets of the slice images in the workspace
+  int64_t ea_off, eb_off;       // offsets of the row / column maxima (IEEE bits, uint64)
+  int32_t M, N, K;
+  int32_t nmt, nnt, nkt;        // 128-row, 64-column and 64-k tile counts
+};
+
 // ---------------------------------------------------------------- context
 // Per-kernel timing with CUDA events on the context's stream (enabled on
 // demand; used by bench.py for the roofline of the dominant kernel).
@@ -176,6 +186,9 @@ struct Ctx {
   DevBufP ensure_workspace(size_t bytes);
   bool prof = false;
   std::vector<ProfRec> prof_recs;
+  DevBufP err_word;  // device status word written by kernels with bounded waits
+  int* device_error_word();
+  void check_device_error();  // syncs the stream; throws TN_ERR_TIMEOUT if a wait gave up
   void launched(int n = 1) { launches += n; }
 };
 Ctx* default_ctx();  // lazily created context on the current device
@@ -211,6 +224,17 @@ void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const 
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
                           cudaStream_t s);
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s);
+void launch_tc_maxima(const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
+                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
+                      unsigned long long* amax, unsigned long long* bmax, int num_sms, cudaStream_t s);
+void launch_tc_slices(int ns, const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
+                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
+                      const unsigned long long* ea, const unsigned long long* eb, uint8_t* ws, int num_sms,
+                      cudaStream_t s);
+size_t tc_gemm_smem(int ns);
+void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems, const uint8_t* ws,
+                    const unsigned long long* ea, const unsigned long long* eb, double* C, int* err, int grid,
+                    cudaStream_t s);
 void launch_scale(double* p, int64_t n, double a, cudaStream_t s);
 
 }  // namespace tn

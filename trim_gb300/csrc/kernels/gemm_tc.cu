@@ -1,0 +1,519 @@
+// Tensor-core sector GEMMs for sm_103a (tcgen05 + TMEM + bulk copies).
+//
+// Split precision (TN_MODE_SPLIT): every FP64 operand element is written in
+// fixed point against its row's (A) or column's (B) power-of-two scale,
+// rounded to 49 bits, and cut into NS = 7 balanced signed digits of 7 bits
+// (d_0 in [-129, 129], d_1..d_6 in [-64, 63]); digit s is stored as the BF16
+// value d * 2^-7s, exact.  C = 2^(ea+eb-14) * sum_{s+t<=7} A_s B_t (34 of the
+// 49 digit products).  The products of one level l = s+t are integers times
+// 2^-7l and stay below 2^15 per k for l <= 4, so levels 0..4 accumulate
+// exactly in FP32 over a chunk of 512 k; they get their own TMEM
+// accumulators and are drained into a double-float (hi, lo) FP32 sum per
+// chunk.  Levels 5..7 share one accumulator (their FP32 rounding is far
+// below 2^-53 of the result).  The dropped levels 8..12 and the operand
+// rounding bound the error near 2^-50 relative to row/column maxima.
+// Fast BF16 (TN_MODE_FAST_BF16): one slice, the BF16 rounding of each scaled
+// element, FP32 accumulation over the whole K.
+//
+// Layout: operand tiles are written by the slicing kernels as exact images of
+// the tcgen05 shared-memory operand layout (K-major, 128-byte swizzle), so the
+// GEMM moves each tile with one 1-D bulk copy.  A tile: 128 rows x 64 k
+// (16 KB per slice); B tile: 64 columns x 64 k (8 KB per slice).
+//
+// GEMM CTA (192 threads): warp 0 = loads (bulk copies), warp 1 = MMA issue +
+// TMEM allocation, warps 2..5 = epilogue (TMEM lane quadrants 2,3,0,1).
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "../engine/engine.h"
+#include "sm103_ptx.cuh"
+
+namespace tn {
+namespace {
+
+using namespace ptx;
+
+constexpr int kTM = 128, kTN = 64, kTK = 64;
+constexpr int kATile = kTM * kTK * 2;  // bytes of one A slice tile
+constexpr int kBTile = kTN * kTK * 2;  // bytes of one B slice tile
+constexpr int kARing = 4, kBRing = 2;
+constexpr int kChunkTiles = 8;  // 512 k per exact-accumulation chunk
+constexpr int kLevels = 6;      // exact levels 0..4 + one shared accumulator for 5..7
+constexpr int kMaxLevel = 7;    // digit products with s + t <= 7 are kept
+constexpr int kThreadsTc = 192;
+
+__device__ __forceinline__ uint32_t swz_off(int r, int c) {  // row r (0..), 16-byte chunk c (0..7)
+  return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
+}
+
+__device__ __forceinline__ int find_seg(const int64_t* __restrict__ start, int n, int64_t v) {
+  int lo = 0, hi = n - 1;  // largest i with start[i] <= v
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (start[mid] <= v)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// power-of-two exponent e with |x| < 2^e for every x of a row/column whose
+// largest magnitude has bit pattern maxbits (0 -> 0)
+__device__ __forceinline__ int exp_of(uint64_t maxbits) {
+  if (maxbits == 0) return 0;
+  int ef = (int)(maxbits >> 52);
+  if (ef == 0) return (63 - __clzll((long long)maxbits)) - 1073;  // subnormal: |x| < 2^(msb+1-1074)
+  return ef - 1022;
+}
+
+// ---------------------------------------------------------------- exponents
+// Largest |x| per row of A and per column of B, kept as IEEE bit patterns
+// (for non-negative doubles the bit order is the value order), reduced per
+// operand tile and merged with 64-bit atomicMax.  The arrays start at zero.
+__global__ void __launch_bounds__(256) tc_max_a(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
+                                                int nsec, int64_t ntiles, const double* __restrict__ A,
+                                                unsigned long long* __restrict__ amax) {
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int g = find_seg(tstart, nsec, t);
+    const TcSector& S = secs[g];
+    const int64_t local = t - tstart[g];
+    const int mt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
+    // 8 lanes per row, each 8 consecutive k: 32 rows per pass of the CTA
+    for (int r0 = 0; r0 < kTM; r0 += 32) {
+      const int r = r0 + (threadIdx.x >> 3), c = threadIdx.x & 7;
+      const int64_t i = (int64_t)mt * kTM + r;
+      unsigned long long m = 0;
+      if (i < S.M) {
+        const unsigned long long* src = (const unsigned long long*)(A + S.a_off + i * S.K);
+        const int k0 = kt * kTK + c * 8;
+#pragma unroll
+        for (int q = 0; q < 8; q++)
+          if (k0 + q < S.K) {
+            const unsigned long long v = __ldg(src + k0 + q) & 0x7FFFFFFFFFFFFFFFull;
+            m = v > m ? v : m;
+          }
+      }
+#pragma unroll
+      for (int o = 4; o; o >>= 1) {
+        const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+        m = v > m ? v : m;
+      }
+      if (c == 0 && i < S.M && m) atomicMax(amax + S.ea_off + i, m);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(256) tc_max_b(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
+                                                int nsec, int64_t ntiles, const double* __restrict__ B,
+                                                unsigned long long* __restrict__ bmax) {
+  __shared__ unsigned long long part[4][kTN];
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int g = find_seg(tstart, nsec, t);
+    const TcSector& S = secs[g];
+    const int64_t local = t - tstart[g];
+    const int nt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
+    const int r = threadIdx.x % kTN, kq = threadIdx.x / kTN;  // lanes along the columns
+    const int64_t j = (int64_t)nt * kTN + r;
+    unsigned long long m = 0;
+    if (j < S.N) {
+      const unsigned long long* src = (const unsigned long long*)(B + S.b_off + j);
+      for (int k = kt * kTK + kq; k < min(S.K, (kt + 1) * kTK); k += 4) {
+        const unsigned long long v = __ldg(src + (int64_t)k * S.N) & 0x7FFFFFFFFFFFFFFFull;
+        m = v > m ? v : m;
+      }
+    }
+    part[kq][r] = m;
+    __syncthreads();
+    if (kq == 0 && j < S.N) {
+      unsigned long long v = part[0][r];
+      for (int q = 1; q < 4; q++) v = part[q][r] > v ? part[q][r] : v;
+      if (v) atomicMax(bmax + S.eb_off + j, v);
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------- slicing
+__constant__ float kDigitScale[8] = {1.0f, 0x1p-7f, 0x1p-14f, 0x1p-21f, 0x1p-28f, 0x1p-35f, 0x1p-42f, 0x1p-49f};
+
+// 8 consecutive-k values of one row -> NS slices of 8 bf16 (packed in uint4)
+template <int NS>
+__device__ __forceinline__ void make_slices(const double (&x)[8], int e, uint4 (&out)[NS]) {
+  uint32_t w[NS][4];
+#pragma unroll
+  for (int s = 0; s < NS; s++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) w[s][q] = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const uint64_t bits = (uint64_t)__double_as_longlong(x[i]);
+    const uint32_t sign = (uint32_t)(bits >> 63);
+    (void)sign;
+    if (NS == 1) {
+      // fast mode: round-to-nearest BF16 of x * 2^(7-e)
+      const float f = (float)ldexp(x[i], 7 - e);
+      const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(f));
+      w[0][i >> 1] |= h << ((i & 1) * 16);
+    } else {
+      const int ef = (int)((bits >> 52) & 0x7FF);
+      uint64_t mant = bits & ((1ull << 52) - 1);
+      int E = -1022;
+      if (ef) {
+        mant |= 1ull << 52;
+        E = ef - 1023;
+      }
+      // X = |x| * 2^(7*NS - e) rounded to the nearest integer (at most 2^(7*NS))
+      const int sh = 52 + e - E - 7 * NS;
+      const uint64_t X = (sh >= 64) ? 0ull
+                         : (sh > 0 ? ((mant + (1ull << (sh - 1))) >> sh) : (mant << (-sh)));
+      // balanced digits, least significant first: d in [-64, 63], top digit
+      // |d_0| <= 129 -- every one exact in BF16
+      long long V = sign ? -(long long)X : (long long)X;
+      int d[NS];
+#pragma unroll
+      for (int s = NS - 1; s > 0; s--) {
+        const int low = (int)(V & 127);
+        d[s] = low >= 64 ? low - 128 : low;
+        V = (V - d[s]) >> 7;
+      }
+      d[0] = (int)V;
+#pragma unroll
+      for (int s = 0; s < NS; s++) {
+        const float f = __int2float_rn(d[s]) * kDigitScale[s];
+        const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(f));
+        w[s][i >> 1] |= h << ((i & 1) * 16);
+      }
+    }
+  }
+#pragma unroll
+  for (int s = 0; s < NS; s++) out[s] = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
+}
+
+// A tiles: (sector, mt, kt) -> NS images of 128 rows x 64 k; one CTA per tile
+template <int NS>
+__global__ void __launch_bounds__(256) tc_slice_a(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
+                                                  int nsec, int64_t ntiles, const double* __restrict__ A,
+                                                  const unsigned long long* __restrict__ ea, uint8_t* __restrict__ ws) {
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int g = find_seg(tstart, nsec, t);
+    const TcSector& S = secs[g];
+    const int64_t local = t - tstart[g];
+    const int mt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
+    uint8_t* img = ws + S.a_img + (int64_t)local * NS * kATile;
+    for (int u = threadIdx.x; u < kTM * 8; u += blockDim.x) {
+      const int r = u >> 3, c = u & 7;  // row within tile, 8-element chunk
+      const int64_t i = (int64_t)mt * kTM + r;
+      const int k0 = kt * kTK + c * 8;
+      double x[8];
+      int e = 0;
+      if (i < S.M) {
+        e = exp_of(ea[S.ea_off + i]);
+        const double* src = A + S.a_off + i * S.K;
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = (k0 + q < S.K) ? __ldg(src + k0 + q) : 0.0;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = 0.0;
+      }
+      uint4 o[NS];
+      make_slices<NS>(x, e, o);
+      const uint32_t off = swz_off(r, c);
+#pragma unroll
+      for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * kATile + off) = o[s];
+    }
+  }
+}
+
+// B tiles: (sector, nt, kt) -> NS images of 64 columns (rows of the image) x 64 k
+template <int NS>
+__global__ void __launch_bounds__(256) tc_slice_b(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
+                                                  int nsec, int64_t ntiles, const double* __restrict__ B,
+                                                  const unsigned long long* __restrict__ eb, uint8_t* __restrict__ ws) {
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    const int g = find_seg(tstart, nsec, t);
+    const TcSector& S = secs[g];
+    const int64_t local = t - tstart[g];
+    const int nt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
+    uint8_t* img = ws + S.b_img + (int64_t)local * NS * kBTile;
+    for (int u = threadIdx.x; u < kTN * 8; u += blockDim.x) {
+      const int r = u % kTN, c = u / kTN;  // lanes run along the columns: coalesced loads of B rows
+      const int64_t j = (int64_t)nt * kTN + r;
+      const int k0 = kt * kTK + c * 8;
+      double x[8];
+      int e = 0;
+      if (j < S.N) {
+        e = exp_of(eb[S.eb_off + j]);
+        const double* src = B + S.b_off + j;
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = (k0 + q < S.K) ? __ldg(src + (int64_t)(k0 + q) * S.N) : 0.0;
+      } else {
+#pragma unroll
+        for (int q = 0; q < 8; q++) x[q] = 0.0;
+      }
+      uint4 o[NS];
+      make_slices<NS>(x, e, o);
+      const uint32_t off = swz_off(r, c);
+#pragma unroll
+      for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * kBTile + off) = o[s];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- GEMM
+struct __align__(8) TcShared {
+  uint64_t fullA[kARing], emptyA[kARing], fullB[kBRing], emptyB[kBRing];
+  uint64_t acc_full, acc_empty, mma_done;
+  uint32_t tmem_base;
+  int abort;
+};
+
+__device__ __forceinline__ void raise_timeout(TcShared& sh, int* err) {
+  sh.abort = 1;
+  atomicExch(err, TN_ERR_TIMEOUT);
+}
+
+__device__ __forceinline__ void two_sum_add(float& hi, float& lo, float v) {
+  const float s = hi + v;
+  const float bb = s - hi;
+  lo += (hi - (s - bb)) + (v - bb);
+  hi = s;
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restrict__ secs,
+                                                         const int4* __restrict__ items, int nitems,
+                                                         const uint8_t* __restrict__ ws,
+                                                         const unsigned long long* __restrict__ ea,
+                                                         const unsigned long long* __restrict__ eb,
+                                                         double* __restrict__ C,
+                                                         int* __restrict__ err) {
+  constexpr int LV = (NS == 1) ? 1 : kLevels;
+  constexpr int kChunk = (NS == 1) ? 1 << 20 : kChunkTiles;  // fast mode: one chunk over all of K
+  extern __shared__ uint8_t dyn[];
+  __shared__ TcShared sh;
+  // 1024-byte aligned operand buffers (the swizzle is anchored to 1024 B)
+  uint8_t* base = (uint8_t*)(((uintptr_t)dyn + 1023) & ~(uintptr_t)1023);
+  uint8_t* abuf = base;                                    // kARing x 16 KB
+  uint8_t* bbuf = base + kARing * kATile;                  // kBRing x NS x 8 KB
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < kARing; i++) {
+      mbar_init(&sh.fullA[i], 1);
+      mbar_init(&sh.emptyA[i], 1);
+    }
+    for (int i = 0; i < kBRing; i++) {
+      mbar_init(&sh.fullB[i], 1);
+      mbar_init(&sh.emptyB[i], 1);
+    }
+    mbar_init(&sh.acc_full, 1);
+    mbar_init(&sh.acc_empty, 4);
+    mbar_init(&sh.mma_done, 1);
+    sh.abort = 0;
+    fence_mbar_init();
+  }
+  if (warp == 1) {
+    tmem_alloc(&sh.tmem_base, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sh.tmem_base;
+
+  if (warp == 0) {
+    // ------------------------------------------------ producer: bulk copies
+    if (lane == 0) {
+      uint32_t na = 0, nb = 0;
+      bool ok = true;
+      for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+        const int4 w = items[it];
+        const TcSector& S = secs[w.x];
+        const uint8_t* a_src = ws + S.a_img + (int64_t)w.y * S.nkt * NS * kATile;
+        const uint8_t* b_src = ws + S.b_img + (int64_t)w.z * S.nkt * NS * kBTile;
+        for (int kt = 0; kt < S.nkt && ok; kt++) {
+          const int sb = nb % kBRing;
+          if (!mbar_wait(&sh.emptyB[sb], ((nb / kBRing) & 1) ^ 1, &sh.abort)) { ok = false; break; }
+          mbar_arrive_expect_tx(&sh.fullB[sb], NS * kBTile);
+          bulk_g2s(bbuf + sb * NS * kBTile, b_src + (int64_t)kt * NS * kBTile, NS * kBTile, &sh.fullB[sb]);
+          nb++;
+          for (int s = 0; s < NS; s++) {
+            const int sa = na % kARing;
+            if (!mbar_wait(&sh.emptyA[sa], ((na / kARing) & 1) ^ 1, &sh.abort)) { ok = false; break; }
+            mbar_arrive_expect_tx(&sh.fullA[sa], kATile);
+            bulk_g2s(abuf + sa * kATile, a_src + ((int64_t)kt * NS + s) * kATile, kATile, &sh.fullA[sa]);
+            na++;
+          }
+        }
+      }
+      if (!ok) raise_timeout(sh, err);
+      // the copies already issued must land before the CTA's shared memory goes away
+      for (int i = 0; i < kARing; i++) {
+        const uint32_t uses = na / kARing + (i < (int)(na % kARing) ? 1 : 0);
+        if (uses) mbar_wait(&sh.fullA[i], (uses - 1) & 1, &sh.abort);
+      }
+      for (int i = 0; i < kBRing; i++) {
+        const uint32_t uses = nb / kBRing + (i < (int)(nb % kBRing) ? 1 : 0);
+        if (uses) mbar_wait(&sh.fullB[i], (uses - 1) & 1, &sh.abort);
+      }
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issue
+    if (lane == 0) {
+      const uint32_t idesc = idesc_bf16_f32(kTM, kTN);
+      uint32_t na = 0, nb = 0, nchunk = 0;
+      bool ok = true;
+      for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+        const int4 w = items[it];
+        const TcSector& S = secs[w.x];
+        for (int k0 = 0; k0 < S.nkt && ok; k0 += kChunk) {
+          const int k1 = min(S.nkt, k0 + kChunk);
+          if (!mbar_wait(&sh.acc_empty, (nchunk & 1) ^ 1, &sh.abort)) { ok = false; break; }
+          tc_fence_after();
+          uint32_t touched = 0;
+          for (int kt = k0; kt < k1 && ok; kt++) {
+            const int sb = nb % kBRing;
+            if (!mbar_wait(&sh.fullB[sb], (nb / kBRing) & 1, &sh.abort)) { ok = false; break; }
+            tc_fence_after();
+            const uint32_t b_addr = smem_u32(bbuf + sb * NS * kBTile);
+            for (int s = 0; s < NS; s++) {
+              const int sa = na % kARing;
+              if (!mbar_wait(&sh.fullA[sa], (na / kARing) & 1, &sh.abort)) { ok = false; break; }
+              tc_fence_after();
+              const uint64_t adesc = desc_sw128(smem_u32(abuf + sa * kATile));
+              for (int t = 0; t < NS && s + t <= (NS == 1 ? 0 : kMaxLevel); t++) {
+                const int lvl = min(s + t, LV - 1);
+                const uint64_t bdesc = desc_sw128(b_addr + t * kBTile);
+                const uint32_t d = tmem + lvl * kTN;
+#pragma unroll
+                for (int kk = 0; kk < kTK / 16; kk++) {
+                  // advancing K by 16 bf16 = 32 bytes inside the swizzle atom: +2 in the address field
+                  mma_bf16(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
+                  touched |= 1u << lvl;
+                }
+              }
+              mma_commit(&sh.emptyA[sa]);
+              na++;
+            }
+            mma_commit(&sh.emptyB[sb]);
+            nb++;
+          }
+          mma_commit(&sh.acc_full);
+          nchunk++;
+        }
+      }
+      if (!ok) raise_timeout(sh, err);
+      // every MMA issued must complete before the tensor memory is released
+      mma_commit(&sh.mma_done);
+      mbar_wait(&sh.mma_done, 0, &sh.abort);
+    }
+  } else {
+    // ------------------------------------------------ epilogue
+    const int quad = warp & 3;  // TMEM lanes 32*quad .. +31
+    const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
+    uint32_t nchunk = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+      const int4 w = items[it];
+      const TcSector& S = secs[w.x];
+      float hi[kTN], lo[kTN];
+#pragma unroll
+      for (int j = 0; j < kTN; j++) hi[j] = lo[j] = 0.f;
+      for (int k0 = 0; k0 < S.nkt; k0 += kChunk) {
+        if (!mbar_wait(&sh.acc_full, nchunk & 1, &sh.abort)) { ok = false; break; }
+        tc_fence_after();
+#pragma unroll
+        for (int l = 0; l < LV; l++) {
+#pragma unroll
+          for (int cg = 0; cg < kTN / 16; cg++) {
+            float v[16];
+            tmem_ld16(lane_addr + l * kTN + cg * 16, v);
+#pragma unroll
+            for (int q = 0; q < 16; q++) two_sum_add(hi[cg * 16 + q], lo[cg * 16 + q], v[q]);
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&sh.acc_empty);
+        nchunk++;
+      }
+      if (!ok) break;
+      const int64_t i = (int64_t)w.y * kTM + quad * 32 + lane;
+      if (i < S.M) {
+        const int e_i = exp_of(ea[S.ea_off + i]);
+        double* crow = C + S.c_off + i * S.N;
+#pragma unroll
+        for (int j = 0; j < kTN; j++) {
+          const int64_t jj = (int64_t)w.z * kTN + j;
+          if (jj < S.N) crow[jj] = ldexp((double)hi[j] + (double)lo[j], e_i + exp_of(eb[S.eb_off + jj]) - 14);
+        }
+      }
+    }
+    if (!ok) raise_timeout(sh, err);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 1) tmem_dealloc(tmem, 512);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------- launchers
+void launch_tc_maxima(const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
+                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
+                      unsigned long long* amax, unsigned long long* bmax, int num_sms, cudaStream_t s) {
+  if (a_tiles) {
+    int g = (int)std::min<int64_t>(a_tiles, (int64_t)num_sms * 8);
+    tc_max_a<<<g, 256, 0, s>>>(secs, a_tstart, nsec, a_tiles, A, amax);
+  }
+  if (b_tiles) {
+    int g = (int)std::min<int64_t>(b_tiles, (int64_t)num_sms * 8);
+    tc_max_b<<<g, 256, 0, s>>>(secs, b_tstart, nsec, b_tiles, B, bmax);
+  }
+  TN_CUDA(cudaGetLastError());
+}
+
+void launch_tc_slices(int ns, const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
+                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
+                      const unsigned long long* ea, const unsigned long long* eb, uint8_t* ws, int num_sms,
+                      cudaStream_t s) {
+  int ga = (int)std::min<int64_t>(a_tiles, (int64_t)num_sms * 8);
+  int gb = (int)std::min<int64_t>(b_tiles, (int64_t)num_sms * 8);
+  if (ns == 7) {
+    if (a_tiles) tc_slice_a<7><<<ga, 256, 0, s>>>(secs, a_tstart, nsec, a_tiles, A, ea, ws);
+    if (b_tiles) tc_slice_b<7><<<gb, 256, 0, s>>>(secs, b_tstart, nsec, b_tiles, B, eb, ws);
+  } else {
+    if (a_tiles) tc_slice_a<1><<<ga, 256, 0, s>>>(secs, a_tstart, nsec, a_tiles, A, ea, ws);
+    if (b_tiles) tc_slice_b<1><<<gb, 256, 0, s>>>(secs, b_tstart, nsec, b_tiles, B, eb, ws);
+  }
+  TN_CUDA(cudaGetLastError());
+}
+
+size_t tc_gemm_smem(int ns) { return (size_t)kARing * kATile + (size_t)kBRing * ns * kBTile + 1024; }
+
+void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems, const uint8_t* ws,
+                    const unsigned long long* ea, const unsigned long long* eb, double* C, int* err, int grid,
+                    cudaStream_t s) {
+  const size_t smem = tc_gemm_smem(ns);
+  if (ns == 7) {
+    static bool attr = false;
+    if (!attr) {
+      TN_CUDA(cudaFuncSetAttribute(tc_gemm<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = true;
+    }
+    tc_gemm<7><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, err);
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      TN_CUDA(cudaFuncSetAttribute(tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = true;
+    }
+    tc_gemm<1><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, err);
+  }
+  TN_CUDA(cudaGetLastError());
+}
+
+}  // namespace tn
