@@ -155,6 +155,29 @@ def reference_main(args, rank, world):
 
 
 # ----------------------------------------------------------------- GPU arm
+def _itebd_device(tu, spec, els):
+    names = [s.name for s in spec["tensors"]]
+    dev = {s.name: tu.UniTensor(s.bonds, s.labels, els[s.name]) for s in spec["tensors"]}
+    net = tu.Network(spec["net"])
+    for n in names:
+        net.put_tensor(n, dev[n])
+    return names, dev, net
+
+
+def _time_steps(torch, stream, flush, steps, fn):
+    """CUDA-event time per step on the library stream, L2 flushed between steps."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    for k in range(steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))  # between timed steps, outside the events
+        starts[k].record(stream)
+        fn()
+        ends[k].record(stream)
+    torch.cuda.synchronize()
+    return sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / steps
+
+
 def gpu_main(args, rank, local, world):
     import torch
 
@@ -164,143 +187,139 @@ def gpu_main(args, rank, local, world):
     stream = torch.cuda.Stream()
     tu.set_stream(stream.cuda_stream)
     spec, els = itebd_inputs()
-    names = [s.name for s in spec["tensors"]]
-    dev = {s.name: tu.UniTensor(s.bonds, s.labels, els[s.name]) for s in spec["tensors"]}
-    net = tu.Network(spec["net"])
-    mode = args.mode
-
-    def step():
-        for n in names:
-            net.put_tensor(n, dev[n])
-        return net.launch(mode)
-
-    # correctness against FP64 on the device (reported, checked in tests)
-    th64 = None
-    for _ in range(max(1, args.warmup)):
-        th = step()
-    ref_net = tu.Network(spec["net"])
-    for n in names:
-        ref_net.put_tensor(n, dev[n])
-    th64 = ref_net.launch("fp64").get_elem()
-    thm = th.get_elem()
-    err = float(np.linalg.norm(thm - th64) / np.linalg.norm(th64))
-
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    if world > 1:
-        torch.distributed.barrier()
-    torch.cuda.synchronize()
-    l0 = tu.launch_count()
-    with ClockSampler(local) as clk:
+    modes = ["fp64"] + ([args.mode] if args.mode != "fp64" else [])
+    res = {}
+    ref64 = None
+    for mode in modes:
+        names, dev, net = _itebd_device(tu, spec, els)
+        for _ in range(args.warmup):
+            th = net.launch(mode)
+        vals = th.get_elem()
+        if mode == "fp64":
+            ref64 = vals
+        err = float(np.linalg.norm(vals - ref64) / np.linalg.norm(ref64))
+        net.capture(mode)  # the whole Network::launch as one CUDA graph
+        out = net.output()
+        for _ in range(args.warmup):
+            net.replay()
+        tu.sync()
+        graph_ok = bool(np.array_equal(out.get_elem(), vals))
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        l0 = tu.launch_count()
+        with ClockSampler(local) as clk:
+            ms_graph = _time_steps(torch, stream, flush, args.steps, net.replay)
+        launches = (tu.launch_count() - l0) // args.steps
+        ms_eager = _time_steps(torch, stream, flush, args.steps, lambda: net.launch(mode))
+        # per-kernel times: eager pass with events around every launch
+        tu.prof_enable(True)
         for k in range(args.steps):
             with torch.cuda.stream(stream):
-                flush.fill_(float(k))  # L2 flush between timed steps, outside the events
-            starts[k].record(stream)
-            step()
-            ends[k].record(stream)
-        torch.cuda.synchronize()
-    launches = (tu.launch_count() - l0) // args.steps
+                flush.fill_(float(k))
+            net.launch(mode)
+        prof = tu.prof_read()
+        tu.prof_enable(False)
+        flops = sum(v["flops"] for k_, v in prof.items() if "gemm" in k_) / args.steps
+        # end to end through the C ABI: pinned host inputs -> device tensors ->
+        # network, graph replay, theta -> pinned host
+        pinned = {n: torch.from_numpy(els[n]).pin_memory() for n in names}
+        out_host = torch.empty(vals.size, dtype=torch.float64).pin_memory()
+        e2e = []
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(float(k))
+            torch.cuda.synchronize()
+            w0 = time.perf_counter()
+            for n in names:
+                dev[n].set_elem_host_ptr(pinned[n].data_ptr(), els[n].size)
+                net.put_tensor(n, dev[n])
+            net.replay()
+            tu.capi.call("tn_tensor_get_elem", out.h, out_host.data_ptr(), vals.size)
+            e2e.append((time.perf_counter() - w0) * 1e3)
+        res[mode] = {"ms_graph": ms_graph, "ms_eager": ms_eager, "flops": flops, "err_vs_fp64": err,
+                     "graph_matches_eager": graph_ok, "launches": int(launches), "clocks": clk.summary(),
+                     "e2e_ms": statistics.median(e2e), "prof": prof,
+                     "h2d": sum(8 * els[n].size for n in names), "d2h": 8 * vals.size}
     if world > 1:
-        torch.distributed.barrier()
-    dt_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends)) / args.steps
-    if world > 1:
-        t = torch.tensor([dt_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dt_ms = float(t.item())
+        for m in res:
+            t = torch.tensor([res[m]["ms_graph"], res[m]["e2e_ms"]], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            res[m]["ms_graph"], res[m]["e2e_ms"] = float(t[0]), float(t[1])
 
-    # per-kernel timing pass (events on the library stream around each launch)
-    tu.prof_enable(True)
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(k))
-        step()
-    prof = tu.prof_read()
-    tu.prof_enable(False)
-    flops = sum(v["flops"] for k_, v in prof.items() if k_.startswith("gemm")) / args.steps
-    value = world * flops / (dt_ms * 1e-3) / 1e12
-
-    # end to end through the C ABI: pinned host inputs -> device, theta -> host
-    pinned = {n: torch.from_numpy(els[n]).pin_memory() for n in names}
-    out_host = torch.empty(th64.size, dtype=torch.float64).pin_memory()
-    h2d = sum(8 * els[n].size for n in names)
-    d2h = 8 * th64.size
-    torch.cuda.synchronize()
-    t0 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    t1 = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    e2e_ms = []
-    for k in range(args.steps):
-        with torch.cuda.stream(stream):
-            flush.fill_(float(k))
-        torch.cuda.synchronize()
-        w0 = time.perf_counter()
-        for n in names:
-            dev[n].set_elem_host_ptr(pinned[n].data_ptr(), els[n].size)
-            net.put_tensor(n, dev[n])
-        th = net.launch(mode)
-        tu.capi.call("tn_tensor_get_elem", th.h, out_host.data_ptr(), th64.size)
-        e2e_ms.append((time.perf_counter() - w0) * 1e3)
-    e2e_step = statistics.median(e2e_ms)
-    e2e_val = world * flops / (e2e_step * 1e-3) / 1e12
-
-    # roofline of the dominant kernel
-    dom = max(prof.items(), key=lambda kv: kv[1]["ms"])
+    head = modes[-1]
+    R = res[head]
+    flops = R["flops"]
+    value = world * flops / (R["ms_graph"] * 1e-3) / 1e12
+    prof = R["prof"]
+    # roofline of the dominant kernel of the headline mode
+    dname, d = max(prof.items(), key=lambda kv: kv[1]["ms"])
     peaks = {}
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
             peaks = json.load(f)
     except OSError:
         pass
-    dname, d = dom
     avg_ms = d["ms"] / d["launches"]
     if dname == "permute":
         ach = d["bytes"] / d["launches"] / (avg_ms * 1e-3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
-        roof = {"kernel": dname, "bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
-    elif dname.startswith("gemm_fp64"):
+    elif dname == "gemm_fp64":
         ach = d["flops"] / d["launches"] / (avg_ms * 1e-3) / 1e12
-        peak = 1.25
-        roof = {"kernel": dname, "bound": "fp64", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
+        roof = {"bound": "fp64", "achieved": ach, "peak": 1.25, "unit": "TFLOP/s",
                 "peak_source": "nominal FP64 rate (no measured FP64 figure)"}
-    else:
-        ach = d["flops"] / d["launches"] / (avg_ms * 1e-3) / 1e12
+    elif dname == "tc_slice":
+        ach = d["bytes"] / d["launches"] / (avg_ms * 1e-3) / 1e9
+        peak = peaks.get("hbm_gbs", 6800.0)
+        roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",
+                "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
+    else:  # tensor-core GEMM: tensor-pipe work = 34 BF16 digit products per FP64-equivalent flop
+        pairs = 34 if "split" in dname else 1
+        ach = pairs * d["flops"] / d["launches"] / (avg_ms * 1e-3) / 1e12
         peak = peaks.get("bf16_tflops", 1900.0)
-        roof = {"kernel": dname, "bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s", "frac": ach / peak,
-                "peak_source": "measured" if "bf16_tflops" in peaks else "fallback"}
-    roof["avg_launch_ms"] = avg_ms
-    roof["traffic"] = None
-    kernels = {k_: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps} for k_, v in prof.items()}
+        roof = {"bound": "tensor", "achieved": ach, "peak": peak, "unit": "TFLOP/s",
+                "peak_source": "measured (burst)" if "bf16_tflops" in peaks else "fallback",
+                "work": "BF16 tensor flops (34 digit products per FP64-equivalent flop)" if pairs > 1 else "BF16 flops"}
+    roof.update({"kernel": dname, "frac": roof["achieved"] / roof["peak"], "avg_launch_ms": avg_ms, "traffic": None})
+    kernels = {k_: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps}
+               for k_, v in prof.items()}
     pbytes = prof.get("permute", {}).get("bytes", 0.0)
     pms = prof.get("permute", {}).get("ms", 0.0)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
-        budget = args.cpu_seconds
-        n = 1
         f_, dt1 = run_reference_steps(1, 1)
-        n = max(3, int(budget / max(dt1, 1e-4)))
+        n = max(3, int(args.cpu_seconds / max(dt1, 1e-4)))
         f_, dtc = run_reference_steps(n, 0)
         cpu = {"value": f_ / dtc / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
                "sample": f"{n} full iTEBD network steps (the whole workload), numpy BLAS on {os.cpu_count()} host threads"}
 
     if rank == 0:
+        modes_out = {m: {k: v for k, v in r.items() if k != "prof"} for m, r in res.items()}
+        for m, r in modes_out.items():
+            r["tflops_graph"] = world * r["flops"] / (r["ms_graph"] * 1e-3) / 1e12
         print(json.dumps({
             "metric": METRIC, "value": value, "unit": "TFLOP/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": dt_ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64" if mode == "fp64" else "f64 (bf16 slices on tcgen05)",
+            "warmup": args.warmup, "ms_per_step": R["ms_graph"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64" if head == "fp64" else "f64 (bf16 digit slices on tcgen05)",
             "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "chi": 512, "sectors": 17, "mode": mode, "flops_per_step": flops,
+            "config": {"workload": WORKLOAD, "chi": 512, "sectors": 17, "mode": head, "flops_per_step": flops,
+                       "execution": "Network::launch captured as one CUDA graph, replayed per step",
                        "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"},
-            "error_vs_fp64": err,
+            "error_vs_fp64": R["err_vs_fp64"],
+            "speedup_vs_fp64_gpu": res["fp64"]["ms_graph"] / R["ms_graph"],
+            "modes": modes_out,
             "permute": {"gb_s": (pbytes / (pms * 1e-3) / 1e9) if pms else None, "bytes_per_step": pbytes / args.steps},
             "kernels": kernels,
             "roofline": roof,
             "cpu_baseline": cpu,
-            "e2e": {"value": e2e_val, "unit": "TFLOP/s", "ms_per_step": e2e_step, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h},
-            "clocks": clk.summary(),
-            "gpu_launches": int(launches),
+            "e2e": {"value": world * flops / (R["e2e_ms"] * 1e-3) / 1e12, "unit": "TFLOP/s", "ms_per_step": R["e2e_ms"],
+                    "h2d_bytes_per_step": R["h2d"], "d2h_bytes_per_step": R["d2h"]},
+            "clocks": R["clocks"],
+            "gpu_launches": R["launches"],
         }))
 
 
@@ -434,7 +453,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="fp64", choices=["fp64", "split", "bf16", "tf32"])
+    ap.add_argument("--mode", default="split", choices=["fp64", "split", "bf16"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--workload", default="itebd", choices=["itebd", "permute", "mera"])

@@ -53,7 +53,11 @@ enum {
   TN_MODE_FP64 = 0,      /* plain FP64 GEMM per sector: the drop-in form */
   TN_MODE_SPLIT = 1,     /* split-precision: BF16 slices on tcgen05, FP64-level error */
   TN_MODE_FAST_BF16 = 2, /* one BF16 slice, FP32 accumulation */
-  TN_MODE_FAST_TF32 = 3  /* TF32 operands, FP32 accumulation */
+  TN_MODE_FAST_TF32 = 3, /* TF32 operands, FP32 accumulation */
+  /* flag: in the tensor-core modes, send every sector to the tensor cores
+   * (by default a contraction under 5e7 FLOP, or a sector with K < 16 or
+   * under 16K multiply-adds, runs on the exact FP64 kernel instead) */
+  TN_MODE_TC_ONLY = 0x100
 };
 
 typedef struct tn_ctx_s* tn_ctx_t;
@@ -179,6 +183,13 @@ int tn_network_put_tensor(tn_network_t net, const char* name, tn_tensor_t t);
 int tn_network_launch(tn_network_t net, int mode, tn_tensor_t* out);
 /* the contraction tree as a bracket string, e.g. "((A B) C)" */
 int tn_network_tree(tn_network_t net, char* buf, int cap);
+/* Record launch() in this mode as a CUDA graph on the default context's
+ * stream (one eager launch first builds every plan); replay() reruns it on
+ * the tensors currently put, which must keep their bonds; output() returns a
+ * handle sharing the graph's persistent output buffer. */
+int tn_network_capture(tn_network_t net, int mode);
+int tn_network_replay(tn_network_t net);
+int tn_network_output(tn_network_t net, tn_tensor_t* out);
 
 #ifdef __cplusplus
 }

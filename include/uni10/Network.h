@@ -47,6 +47,16 @@ class Network {
   UniTensor launch(const std::string& name = "");
   // contraction tree as brackets of tensor names, e.g. "((A B) C)"
   std::string tree();
+  // Record launch() (in the current contraction mode) as a CUDA graph: one
+  // eager launch builds every plan and sizes the workspace, then the launch
+  // is captured with its intermediates as graph memory nodes and the result
+  // copied into a persistent output tensor.  replay() reruns the graph on the
+  // tensors currently put in the network, which must keep the signatures
+  // they had at capture; output() is that persistent tensor.
+  void capture();
+  void replay();
+  const UniTensor& output() const;
+  bool captured() const { return graph_exec != nullptr; }
 
  private:
   Network() = default;
@@ -67,6 +77,12 @@ class Network {
   std::vector<int> brakets;
   Node* root = nullptr;
   bool load = false;
+  void* graph_exec = nullptr;  // cudaGraphExec_t
+  void* graph = nullptr;       // cudaGraph_t
+  UniTensor graph_out;
+  std::vector<std::string> graph_sigs;
+  int64_t graph_kernels = 0;
+  void drop_graph();
 };
 
 }  // namespace uni10

@@ -36,8 +36,12 @@ class UniTensor {
   UniTensor(const std::vector<Bond>& _bonds, std::vector<int>& labels, const std::string& _name = "");
   UniTensor(const std::vector<Bond>& _bonds, int* labels, const std::string& _name = "");
   UniTensor(const UniTensor& UniT);
+  UniTensor(UniTensor&& UniT) noexcept = default;
   explicit UniTensor(const std::string& fname);  // UniTensor::save layout (UniTensor.cpp:486-583)
   UniTensor& operator=(const UniTensor& UniT);
+  UniTensor& operator=(UniTensor&& UniT) noexcept = default;
+  // a second handle on the same element buffer (no copy)
+  static UniTensor alias(const UniTensor& t);
   ~UniTensor();
 
   // elements
@@ -79,6 +83,9 @@ class UniTensor {
   UniTensor& transpose();
   UniTensor& combineBond(const std::vector<int>& combined_labels);
   friend UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast);
+  // contraction that leaves both operands untouched (permuted operands are
+  // temporaries); Network::launch uses it so its leaves keep their buffers
+  friend UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb);
   friend UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
 
   UniTensor& operator*=(double a);
@@ -97,6 +104,8 @@ class UniTensor {
  private:
   struct NoFill {};
   UniTensor(const std::vector<Bond>& _bonds, const std::string& _name, NoFill);
+  static UniTensor permuted(const UniTensor& src, const std::vector<int>& newLabels, int rowBondNum);
+  static UniTensor contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool mutate);
   void initUniT(bool zero = true);
   std::string name;
   std::vector<Bond> bonds;
@@ -111,6 +120,7 @@ class UniTensor {
 };
 
 UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast = false);
+UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb);
 UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
 UniTensor operator*(const UniTensor& Ta, double a);
 UniTensor operator*(double a, const UniTensor& Ta);

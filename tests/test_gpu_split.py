@@ -60,19 +60,19 @@ def _grouped(env, mode, shapes, seed, dist="uniform"):
 
 
 def test_split_single_tile(env):
-    errs = _grouped(env, "split", [(128, 64, 64)], 1)
+    errs = _grouped(env, "split_tc", [(128, 64, 64)], 1)
     assert errs[0] <= SPLIT_TOL, errs
 
 
 def test_split_ragged_shapes(env):
     shapes = [(1, 1, 1), (2, 3, 5), (33, 17, 9), (130, 70, 65), (127, 63, 129)]
-    errs = _grouped(env, "split", shapes, 2)
+    errs = _grouped(env, "split_tc", shapes, 2)
     assert max(errs) <= SPLIT_TOL, errs
 
 
 def test_split_long_k_chunks(env):
     # several 256-k exact-accumulation chunks and a Gaussian operand
-    errs = _grouped(env, "split", [(200, 150, 700), (64, 64, 3000)], 3, dist="normal")
+    errs = _grouped(env, "split_tc", [(200, 150, 700), (64, 64, 3000)], 3, dist="normal")
     assert max(errs) <= SPLIT_TOL, errs
 
 
@@ -85,7 +85,7 @@ def test_split_wide_dynamic_range(env):
     A = torch.from_numpy(a.ravel()).cuda()
     B = torch.from_numpy(b.ravel()).cuda()
     Cd = torch.zeros(m * n, dtype=torch.float64, device="cuda")
-    tu.contract_sectors("split", [(m, n, k, 0, 0, 0)], A.data_ptr(), B.data_ptr(), Cd.data_ptr())
+    tu.contract_sectors("split_tc", [(m, n, k, 0, 0, 0)], A.data_ptr(), B.data_ptr(), Cd.data_ptr())
     tu.sync()
     c = Cd.cpu().numpy().reshape(m, n)
     want = a @ b
@@ -98,7 +98,7 @@ def test_split_wide_dynamic_range(env):
 
 
 def test_fast_bf16_reports_bf16_level_error(env):
-    errs = _grouped(env, "bf16", [(128, 64, 256), (50, 40, 30)], 5)
+    errs = _grouped(env, "bf16_tc", [(128, 64, 256), (50, 40, 30)], 5)
     assert max(errs) <= 1e-2, errs
 
 
@@ -107,7 +107,7 @@ def test_split_contract_golden_cases(env):
     for case in [c for c in G.cases().values() if c["kind"] == "contract"]:
         a = tu.UniTensor(G.bonds_of(case["A"]), case["A"]["labels"], G.arr(case["id"], "A"))
         b = tu.UniTensor(G.bonds_of(case["B"]), case["B"]["labels"], G.arr(case["id"], "B"))
-        c = tu.contract(a, b, mode="split")
+        c = tu.contract(a, b, mode="split_tc")
         assert rel(c.get_elem(), G.arr(case["id"], "C")) <= SPLIT_TOL, case["id"]
 
 
@@ -122,8 +122,9 @@ def test_split_itebd_network(env):
         t = tu.UniTensor(s.bonds, s.labels, els[s.name])
         keep.append(t)
         net.put_tensor(s.name, t)
-    th = net.launch(mode="split")
-    assert rel(th.get_elem(), G.arr("itebd", "TH")) <= SPLIT_TOL
+    for mode in ("split", "split_tc"):
+        th = net.launch(mode=mode)
+        assert rel(th.get_elem(), G.arr("itebd", "TH")) <= SPLIT_TOL, mode
 
 
 def test_split_mera_and_ipeps_small(env):
@@ -139,12 +140,40 @@ def test_split_mera_and_ipeps_small(env):
             t = tu.UniTensor(s.bonds, s.labels, els[s.name])
             keep.append(t)
             net.put_tensor(s.name, t)
-        r = net.launch(mode="split")
+        r = net.launch(mode="split_tc")
         assert rel(r.get_elem(), G.arr("mera_small", dname)) <= SPLIT_TOL, dname
     c = G.cases()["batched_small"]
     spec = wl.batched(**c["params"])
     for i, (t1, t2) in enumerate(spec["pairs"]):
         a = tu.UniTensor(t1.bonds, t1.labels, G.arr("batched_small", t1.name))
         b = tu.UniTensor(t2.bonds, t2.labels, G.arr("batched_small", t2.name))
-        r = tu.contract(a, b, mode="split")
+        r = tu.contract(a, b, mode="split_tc")
         assert rel(r.get_elem(), G.arr("batched_small", f"C{i}")) <= SPLIT_TOL
+
+
+def test_network_graph_capture_replay(env):
+    """Network::launch recorded as a CUDA graph: replay after new inputs are
+    put gives the eager result bit for bit (same kernels, same plans)."""
+    torch, capi, tu = env
+    spec = wl.itebd()
+    rng = np.random.default_rng(spec["seed"])
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    for mode in ("fp64", "split"):
+        net = tu.Network(spec["net"])
+        ts = {s.name: tu.UniTensor(s.bonds, s.labels, els[s.name]) for s in spec["tensors"]}
+        for n, t in ts.items():
+            net.put_tensor(n, t)
+        net.capture(mode)
+        out = net.output()
+        eager0 = net.launch(mode).get_elem()
+        net.replay()
+        assert np.array_equal(out.get_elem(), eager0)
+        # new element values in the same tensors: put, replay, compare
+        els2 = {n: v * (1.0 + 0.25 * (i + 1)) for i, (n, v) in enumerate(els.items())}
+        for n, t in ts.items():
+            t.set_elem(els2[n])
+            net.put_tensor(n, t)
+        net.replay()
+        eager = net.launch(mode).get_elem()
+        assert np.array_equal(out.get_elem(), eager)
+        assert not np.array_equal(eager, eager0)

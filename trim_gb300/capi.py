@@ -18,7 +18,9 @@ HEADER = os.path.join(ROOT, "include", "trim_gb300.h")
 TN_OK = 0
 TN_ERR = {1: "ARG", 2: "OOM", 3: "TIMEOUT", 4: "CUDA", 5: "SHAPE", 6: "LABEL", 7: "UNSUPPORTED", 8: "NOBLOCK", 9: "FILE"}
 MODE_FP64, MODE_SPLIT, MODE_FAST_BF16, MODE_FAST_TF32 = 0, 1, 2, 3
-MODES = {"fp64": MODE_FP64, "split": MODE_SPLIT, "bf16": MODE_FAST_BF16, "tf32": MODE_FAST_TF32}
+MODE_TC_ONLY = 0x100
+MODES = {"fp64": MODE_FP64, "split": MODE_SPLIT, "bf16": MODE_FAST_BF16, "tf32": MODE_FAST_TF32,
+         "split_tc": MODE_SPLIT | MODE_TC_ONLY, "bf16_tc": MODE_FAST_BF16 | MODE_TC_ONLY}
 
 
 class TnError(RuntimeError):
@@ -79,6 +81,9 @@ _PROTOS = {
     "tn_network_put_tensor": (_I, [_P, C.c_char_p, _P]),
     "tn_network_launch": (_I, [_P, _I, C.POINTER(_P)]),
     "tn_network_tree": (_I, [_P, C.c_char_p, _I]),
+    "tn_network_capture": (_I, [_P, _I]),
+    "tn_network_replay": (_I, [_P]),
+    "tn_network_output": (_I, [_P, C.POINTER(_P)]),
 }
 
 _lib = None

@@ -458,6 +458,29 @@ int tn_network_launch(tn_network_t net, int mode, tn_tensor_t* out) {
   });
 }
 
+int tn_network_capture(tn_network_t net, int mode) {
+  return guard([&] {
+    need(net, "net");
+    ModeScope ms(mode);
+    net->net->capture();
+  });
+}
+
+int tn_network_replay(tn_network_t net) {
+  return guard([&] {
+    need(net, "net");
+    net->net->replay();
+  });
+}
+
+int tn_network_output(tn_network_t net, tn_tensor_t* out) {
+  return guard([&] {
+    need(net, "net");
+    need(out, "out");
+    *out = new tn_tensor_s{uni10::UniTensor::alias(net->net->output())};
+  });
+}
+
 int tn_network_tree(tn_network_t net, char* buf, int cap) {
   return guard([&] {
     need(net, "net");

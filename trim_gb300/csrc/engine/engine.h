@@ -181,6 +181,7 @@ struct Ctx {
   int64_t launches = 0;
   std::mutex mu;
   std::unordered_map<std::string, PermPlanP> perm_cache;
+  std::unordered_map<uint64_t, std::shared_ptr<void>> gemm_cache, tc_cache;  // device work lists
   std::unordered_map<std::string, SectorMapP> smap_refs;  // keep cached maps alive per ctx
   DevBufP workspace;  // scratch for split-K partial tiles and operand slices
   DevBufP ensure_workspace(size_t bytes);
@@ -206,6 +207,7 @@ PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num);  // tiles assi
 int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double* dst);
 void run_permute(Ctx& ctx, const PermPlan& plan, const double* src, double* dst);
 
+uint64_t hash_list(const std::vector<tn_sector_gemm>& list, int tag);
 // sector GEMMs: C_i = A_i . B_i for every item, all in one grouped launch
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A,
                       const double* B, double* C);
@@ -224,13 +226,9 @@ void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const 
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
                           cudaStream_t s);
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s);
-void launch_tc_maxima(const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
-                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
-                      unsigned long long* amax, unsigned long long* bmax, int num_sms, cudaStream_t s);
-void launch_tc_slices(int ns, const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
-                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
-                      const unsigned long long* ea, const unsigned long long* eb, uint8_t* ws, int num_sms,
-                      cudaStream_t s);
+void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
+                    int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,
+                    unsigned long long* bmax, int64_t nmax, uint8_t* images, int num_sms, cudaStream_t s);
 size_t tc_gemm_smem(int ns);
 void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems, const uint8_t* ws,
                     const unsigned long long* ea, const unsigned long long* eb, double* C, int* err, int grid,

@@ -9,9 +9,6 @@
 
 namespace tn {
 
-void run_split_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
-                     double* C);
-
 namespace {
 constexpr int kTileM = 16, kTileN = 32;
 
@@ -76,40 +73,92 @@ std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num
   return t;
 }
 
+struct Fp64Plan {
+  std::vector<tn_sector_gemm> list;
+  DevBufP tiles;
+  int ntiles = 0;
+  int64_t ws_elems = 0;
+  double flops = 0, bytes = 0;
+};
+
+static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list) {
+  const uint64_t key = hash_list(list, 64);
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.gemm_cache.find(key);
+    if (it != ctx.gemm_cache.end()) {
+      auto P = std::static_pointer_cast<Fp64Plan>(it->second);
+      if (P->list.size() == list.size() &&
+          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0)
+        return P;
+    }
+  }
+  auto P = std::make_shared<Fp64Plan>();
+  P->list = list;
+  std::vector<GemmTile> tiles = plan_fp64(list, ctx.num_sms, -1, &P->ws_elems);
+  P->ntiles = (int)tiles.size();
+  for (const auto& g : list) {
+    P->flops += 2.0 * g.M * g.N * g.K;
+    P->bytes += 8.0 * (g.M * g.K + g.K * g.N + g.M * g.N);
+  }
+  if (!tiles.empty()) {
+    P->tiles = std::make_shared<DevBuf>(tiles.size() * sizeof(GemmTile), ctx);
+    TN_CUDA(cudaMemcpyAsync(P->tiles->ptr, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice,
+                            ctx.stream));
+    TN_CUDA(cudaStreamSynchronize(ctx.stream));  // the host copy dies here
+  }
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  if (ctx.gemm_cache.size() > 4096) ctx.gemm_cache.clear();
+  ctx.gemm_cache[key] = P;
+  return P;
+}
+
+static void run_fp64(Ctx& ctx, const std::vector<tn_sector_gemm>& list, const double* A, const double* B, double* C) {
+  auto P = get_fp64_plan(ctx, list);
+  if (!P->ntiles) return;
+  double* ws = nullptr;
+  if (P->ws_elems > 0) ws = (double*)ctx.ensure_workspace(P->ws_elems * sizeof(double))->ptr;
+  int grid = (int)std::min<int64_t>((int64_t)P->ntiles, (int64_t)ctx.num_sms * 16);
+  {
+    ProfScope ps(ctx, "gemm_fp64", P->bytes, P->flops);
+    launch_gemm_fp64((const GemmTile*)P->tiles->ptr, P->ntiles, A, B, C, ws, grid, ctx.stream);
+    ctx.launched();
+  }
+  if (P->ws_elems > 0) {
+    ProfScope ps(ctx, "splitk_reduce", 0, 0);
+    launch_splitk_reduce((const GemmTile*)P->tiles->ptr, P->ntiles, ws, C, grid, ctx.stream);
+    ctx.launched();
+  }
+}
+
+void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
+                  double* C);
+
+// Tensor-core modes route work where the tensor-core path cannot pay for its
+// fixed cost (operand slicing + a second launch, ~70 us measured on GB300) --
+// a whole contraction under 5e7 FLOP, or a sector with K < 16 or under 16K
+// multiply-adds -- to the FP64 kernel, which is exact and at that size no
+// slower; the rest goes to the tcgen05 kernel.
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
                       double* C) {
   if (list.empty()) return;
-  if (mode == TN_MODE_SPLIT || mode == TN_MODE_FAST_BF16 || mode == TN_MODE_FAST_TF32) {
-    run_split_gemms(ctx, mode, list, A, B, C);
+  const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0;
+  mode &= ~TN_MODE_TC_ONLY;
+  if (mode == TN_MODE_FP64) {
+    run_fp64(ctx, list, A, B, C);
     return;
   }
-  if (mode != TN_MODE_FP64) fail(TN_ERR_ARG, "unknown contraction mode");
-  int64_t ws_elems = 0;
-  std::vector<GemmTile> tiles = plan_fp64(list, ctx.num_sms, -1, &ws_elems);
-  if (tiles.empty()) return;
-  DevBuf dtiles(tiles.size() * sizeof(GemmTile), ctx);
-  TN_CUDA(cudaMemcpyAsync(dtiles.ptr, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice,
-                          ctx.stream));
-  double* ws = nullptr;
-  if (ws_elems > 0) ws = (double*)ctx.ensure_workspace(ws_elems * sizeof(double))->ptr;
-  int grid = (int)std::min<int64_t>((int64_t)tiles.size(), (int64_t)ctx.num_sms * 16);
-  double flops = 0, bytes = 0;
+  if (mode == TN_MODE_FAST_TF32) fail(TN_ERR_UNSUPPORTED, "TF32 fast mode is not built; use TN_MODE_FAST_BF16");
+  if (mode != TN_MODE_SPLIT && mode != TN_MODE_FAST_BF16) fail(TN_ERR_ARG, "unknown contraction mode");
+  double total = 0;
+  for (const auto& g : list) total += 2.0 * g.M * g.N * g.K;
+  std::vector<tn_sector_gemm> tc, f64;
   for (const auto& g : list) {
-    flops += 2.0 * g.M * g.N * g.K;
-    bytes += 8.0 * (g.M * g.K + g.K * g.N + g.M * g.N);
+    const bool small = !tc_only && (total < 5.0e7 || g.K < 16 || (double)g.M * g.N * g.K < 16384.0);
+    (small ? f64 : tc).push_back(g);
   }
-  {
-    ProfScope ps(ctx, "gemm_fp64", bytes, flops);
-    launch_gemm_fp64((const GemmTile*)dtiles.ptr, (int)tiles.size(), A, B, C, ws, grid, ctx.stream);
-    ctx.launched();
-  }
-  if (ws_elems > 0) {
-    ProfScope ps(ctx, "splitk_reduce", 0, 0);
-    launch_splitk_reduce((const GemmTile*)dtiles.ptr, (int)tiles.size(), ws, C, grid, ctx.stream);
-    ctx.launched();
-  }
-  // the pageable source of the work list was staged by cudaMemcpyAsync before
-  // it returned; dtiles is released stream-ordered after the kernels
+  if (!f64.empty()) run_fp64(ctx, f64, A, B, C);
+  if (!tc.empty()) run_tc_gemms(ctx, mode == TN_MODE_SPLIT ? 7 : 1, tc, A, B, C);
 }
 
 }  // namespace tn

@@ -1,7 +1,9 @@
 // Planning and dispatch of the tensor-core sector GEMMs (split precision and
-// fast BF16).  Per contraction: exponents of A's rows and B's columns, the
+// fast BF16).  Per contraction: the maxima of A's rows and B's columns, the
 // operand slice images (tcgen05 shared-memory layout), then one persistent
 // grouped GEMM launch over all (sector, 128-row tile, 64-column tile) items.
+// Device work lists are built once per sector list and cached on the context,
+// so a repeated contraction (and a captured CUDA graph) uploads nothing.
 #include <algorithm>
 #include <cstring>
 
@@ -14,15 +16,33 @@ constexpr int kTM = 128, kTN = 64, kTK = 64;
 int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 }  // namespace
 
-void run_split_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
-                     double* C) {
-  if (mode == TN_MODE_FAST_TF32) fail(TN_ERR_UNSUPPORTED, "TF32 fast mode is not built; use TN_MODE_FAST_BF16");
-  const int ns = (mode == TN_MODE_SPLIT) ? 7 : 1;
+struct TcPlan {
+  std::vector<tn_sector_gemm> list;
+  int ns = 7;
+  DevBufP meta;
+  size_t off_secs = 0, off_rb = 0, off_cb = 0, off_at = 0, off_bt = 0, off_it = 0;
+  int nsec = 0, nitems = 0;
+  int64_t rows = 0, cols = 0, nrb = 0, ncb = 0, a_tiles = 0, b_tiles = 0, img = 0;
+  double flops = 0, in_bytes = 0;
+};
+
+uint64_t hash_list(const std::vector<tn_sector_gemm>& list, int tag) {
+  uint64_t h = 1469598103934665603ull ^ (uint64_t)tag;
+  const unsigned char* p = (const unsigned char*)list.data();
+  for (size_t i = 0; i < list.size() * sizeof(tn_sector_gemm); i++) {
+    h ^= p[i];
+    h *= 1099511628211ull;
+  }
+  return h ^ (list.size() << 1);
+}
+
+static std::shared_ptr<TcPlan> build_tc_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns) {
+  auto P = std::make_shared<TcPlan>();
+  P->list = list;
+  P->ns = ns;
   std::vector<TcSector> secs;
-  std::vector<int64_t> row_start(1, 0), col_start(1, 0), a_ts(1, 0), b_ts(1, 0);
+  std::vector<int64_t> rb(1, 0), cb(1, 0), ats(1, 0), bts(1, 0);
   std::vector<int4> items;
-  int64_t rows = 0, cols = 0, img = 0, at = 0, bt = 0;
-  double flops = 0;
   for (const auto& g : list) {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX / 2 || g.N > INT32_MAX / 2 || g.K > INT32_MAX / 2)
@@ -38,70 +58,95 @@ void run_split_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list
     s.nmt = (int32_t)cdiv(g.M, kTM);
     s.nnt = (int32_t)cdiv(g.N, kTN);
     s.nkt = (int32_t)cdiv(g.K, kTK);
-    s.ea_off = rows;
-    s.eb_off = cols;
-    rows += g.M;
-    cols += g.N;
-    s.a_img = img;
-    img += (int64_t)s.nmt * s.nkt * ns * kTM * kTK * 2;
-    s.b_img = img;
-    img += (int64_t)s.nnt * s.nkt * ns * kTN * kTK * 2;
-    at += (int64_t)s.nmt * s.nkt;
-    bt += (int64_t)s.nnt * s.nkt;
+    s.ea_off = P->rows;
+    s.eb_off = P->cols;
+    P->rows += g.M;
+    P->cols += g.N;
+    s.a_img = P->img;
+    P->img += (int64_t)s.nmt * s.nkt * ns * kTM * kTK * 2;
+    s.b_img = P->img;
+    P->img += (int64_t)s.nnt * s.nkt * ns * kTN * kTK * 2;
+    P->nrb += s.nmt;
+    P->ncb += s.nnt;
+    P->a_tiles += (int64_t)s.nmt * s.nkt;
+    P->b_tiles += (int64_t)s.nnt * s.nkt;
     const int idx = (int)secs.size();
     for (int mt = 0; mt < s.nmt; mt++)
       for (int nt = 0; nt < s.nnt; nt++) items.push_back(make_int4(idx, mt, nt, 0));
     secs.push_back(s);
-    row_start.push_back(rows);
-    col_start.push_back(cols);
-    a_ts.push_back(at);
-    b_ts.push_back(bt);
-    flops += 2.0 * g.M * g.N * g.K;
+    rb.push_back(P->nrb);
+    cb.push_back(P->ncb);
+    ats.push_back(P->a_tiles);
+    bts.push_back(P->b_tiles);
+    P->flops += 2.0 * g.M * g.N * g.K;
+    P->in_bytes += 8.0 * ((double)g.M * g.K + (double)g.K * g.N);
   }
-  if (secs.empty()) return;
-  const int nsec = (int)secs.size();
-  // metadata: sectors | row_start | col_start | a_ts | b_ts | items
-  size_t off_secs = 0;
-  size_t off_rs = off_secs + nsec * sizeof(TcSector);
-  size_t off_cs = off_rs + (nsec + 1) * sizeof(int64_t);
-  size_t off_at = off_cs + (nsec + 1) * sizeof(int64_t);
-  size_t off_bt = off_at + (nsec + 1) * sizeof(int64_t);
-  size_t off_it = (off_bt + (nsec + 1) * sizeof(int64_t) + 15) & ~(size_t)15;
-  size_t meta_bytes = off_it + items.size() * sizeof(int4);
-  std::vector<uint8_t> meta(meta_bytes);
-  std::memcpy(meta.data() + off_secs, secs.data(), nsec * sizeof(TcSector));
-  std::memcpy(meta.data() + off_rs, row_start.data(), (nsec + 1) * sizeof(int64_t));
-  std::memcpy(meta.data() + off_cs, col_start.data(), (nsec + 1) * sizeof(int64_t));
-  std::memcpy(meta.data() + off_at, a_ts.data(), (nsec + 1) * sizeof(int64_t));
-  std::memcpy(meta.data() + off_bt, b_ts.data(), (nsec + 1) * sizeof(int64_t));
-  std::memcpy(meta.data() + off_it, items.data(), items.size() * sizeof(int4));
-  DevBuf dmeta(meta_bytes, ctx);
-  TN_CUDA(cudaMemcpyAsync(dmeta.ptr, meta.data(), meta_bytes, cudaMemcpyHostToDevice, ctx.stream));
-  const uint8_t* mb = (const uint8_t*)dmeta.ptr;
-  const TcSector* dsecs = (const TcSector*)(mb + off_secs);
-  // workspace: row / column maxima (uint64, zeroed) then the slice images
-  size_t exp_bytes = (((size_t)(rows + cols)) * sizeof(unsigned long long) + 1023) & ~(size_t)1023;
-  uint8_t* ws = (uint8_t*)ctx.ensure_workspace(exp_bytes + (size_t)img)->ptr;
+  P->nsec = (int)secs.size();
+  P->nitems = (int)items.size();
+  if (!P->nsec) return P;
+  const int n1 = P->nsec + 1;
+  P->off_secs = 0;
+  P->off_rb = P->off_secs + P->nsec * sizeof(TcSector);
+  P->off_cb = P->off_rb + n1 * sizeof(int64_t);
+  P->off_at = P->off_cb + n1 * sizeof(int64_t);
+  P->off_bt = P->off_at + n1 * sizeof(int64_t);
+  P->off_it = (P->off_bt + n1 * sizeof(int64_t) + 15) & ~(size_t)15;
+  size_t bytes = P->off_it + items.size() * sizeof(int4);
+  std::vector<uint8_t> meta(bytes);
+  std::memcpy(meta.data() + P->off_secs, secs.data(), P->nsec * sizeof(TcSector));
+  std::memcpy(meta.data() + P->off_rb, rb.data(), n1 * sizeof(int64_t));
+  std::memcpy(meta.data() + P->off_cb, cb.data(), n1 * sizeof(int64_t));
+  std::memcpy(meta.data() + P->off_at, ats.data(), n1 * sizeof(int64_t));
+  std::memcpy(meta.data() + P->off_bt, bts.data(), n1 * sizeof(int64_t));
+  std::memcpy(meta.data() + P->off_it, items.data(), items.size() * sizeof(int4));
+  P->meta = std::make_shared<DevBuf>(bytes, ctx);
+  TN_CUDA(cudaMemcpyAsync(P->meta->ptr, meta.data(), bytes, cudaMemcpyHostToDevice, ctx.stream));
+  TN_CUDA(cudaStreamSynchronize(ctx.stream));  // the host copy dies here
+  return P;
+}
+
+static std::shared_ptr<TcPlan> get_tc_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns) {
+  const uint64_t key = hash_list(list, 100 + ns);
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.tc_cache.find(key);
+    if (it != ctx.tc_cache.end()) {
+      auto P = std::static_pointer_cast<TcPlan>(it->second);
+      if (P->ns == ns && P->list.size() == list.size() &&
+          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0)
+        return P;
+    }
+  }
+  auto P = build_tc_plan(ctx, list, ns);
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  if (ctx.tc_cache.size() > 1024) ctx.tc_cache.clear();
+  ctx.tc_cache[key] = P;
+  return P;
+}
+
+void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
+                  double* C) {
+  auto P = get_tc_plan(ctx, list, ns);
+  if (!P->nsec) return;
+  const uint8_t* mb = (const uint8_t*)P->meta->ptr;
+  const TcSector* dsecs = (const TcSector*)(mb + P->off_secs);
+  // workspace: row / column maxima (uint64) then the slice images
+  size_t max_bytes = (((size_t)(P->rows + P->cols)) * sizeof(unsigned long long) + 1023) & ~(size_t)1023;
+  uint8_t* ws = (uint8_t*)ctx.ensure_workspace(max_bytes + (size_t)P->img)->ptr;
   unsigned long long* ea = (unsigned long long*)ws;
-  unsigned long long* eb = ea + rows;
-  uint8_t* images = ws + exp_bytes;
+  unsigned long long* eb = ea + P->rows;
+  uint8_t* images = ws + max_bytes;
   int* err = ctx.device_error_word();
   {
-    double in_bytes = 0;
-    for (const auto& g : secs) in_bytes += 8.0 * ((double)g.M * g.K + (double)g.K * g.N);
-    ProfScope ps(ctx, "tc_slice", 2 * in_bytes + (double)img, 0);
-    TN_CUDA(cudaMemsetAsync(ws, 0, (size_t)(rows + cols) * sizeof(unsigned long long), ctx.stream));
-    launch_tc_maxima(dsecs, nsec, (const int64_t*)(mb + off_at), at, (const int64_t*)(mb + off_bt), bt, A, B, ea, eb,
-                     ctx.num_sms, ctx.stream);
-    launch_tc_slices(ns, dsecs, nsec, (const int64_t*)(mb + off_at), at, (const int64_t*)(mb + off_bt), bt, A, B, ea,
-                     eb, images, ctx.num_sms, ctx.stream);
-    ctx.launched(4);
+    ProfScope ps(ctx, "tc_slice", 2 * P->in_bytes + (double)P->img, 0);
+    launch_tc_prep(ns, dsecs, P->nsec, (const int64_t*)(mb + P->off_at), P->a_tiles, (const int64_t*)(mb + P->off_bt),
+                   P->b_tiles, A, B, ea, eb, P->rows + P->cols, images, ctx.num_sms, ctx.stream);
+    ctx.launched(2);
   }
   {
-    ProfScope ps(ctx, ns == 7 ? "tc_gemm_split" : "tc_gemm_bf16", 0, flops);
-    int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)ctx.num_sms);
-    launch_tc_gemm(ns, dsecs, (const int4*)(mb + off_it), (int)items.size(), images, ea, eb, C, err, grid,
-                   ctx.stream);
+    ProfScope ps(ctx, ns == 7 ? "tc_gemm_split" : "tc_gemm_bf16", 0, P->flops);
+    int grid = (int)std::min<int64_t>((int64_t)P->nitems, (int64_t)ctx.num_sms);
+    launch_tc_gemm(ns, dsecs, (const int4*)(mb + P->off_it), P->nitems, images, ea, eb, C, err, grid, ctx.stream);
     ctx.launched();
   }
 }

@@ -70,68 +70,68 @@ __device__ __forceinline__ int exp_of(uint64_t maxbits) {
 
 // ---------------------------------------------------------------- exponents
 // Largest |x| per row of A and per column of B, kept as IEEE bit patterns
-// (for non-negative doubles the bit order is the value order), reduced per
-// operand tile and merged with 64-bit atomicMax.  The arrays start at zero.
-__global__ void __launch_bounds__(256) tc_max_a(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
-                                                int nsec, int64_t ntiles, const double* __restrict__ A,
-                                                unsigned long long* __restrict__ amax) {
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int g = find_seg(tstart, nsec, t);
-    const TcSector& S = secs[g];
-    const int64_t local = t - tstart[g];
-    const int mt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
-    // 8 lanes per row, each 8 consecutive k: 32 rows per pass of the CTA
-    for (int r0 = 0; r0 < kTM; r0 += 32) {
-      const int r = r0 + (threadIdx.x >> 3), c = threadIdx.x & 7;
-      const int64_t i = (int64_t)mt * kTM + r;
-      unsigned long long m = 0;
-      if (i < S.M) {
-        const unsigned long long* src = (const unsigned long long*)(A + S.a_off + i * S.K);
-        const int k0 = kt * kTK + c * 8;
-#pragma unroll
-        for (int q = 0; q < 8; q++)
-          if (k0 + q < S.K) {
-            const unsigned long long v = __ldg(src + k0 + q) & 0x7FFFFFFFFFFFFFFFull;
-            m = v > m ? v : m;
-          }
-      }
-#pragma unroll
-      for (int o = 4; o; o >>= 1) {
-        const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
-        m = v > m ? v : m;
-      }
-      if (c == 0 && i < S.M && m) atomicMax(amax + S.ea_off + i, m);
-    }
-  }
-}
-
-__global__ void __launch_bounds__(256) tc_max_b(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
-                                                int nsec, int64_t ntiles, const double* __restrict__ B,
-                                                unsigned long long* __restrict__ bmax) {
+// (for non-negative doubles the bit order is the value order).  Every operand
+// tile (the same tiling as the slicing) reduces its part and merges it with a
+// 64-bit atomicMax, so large-K operands spread over the whole GPU; the arrays
+// are zeroed first.
+__global__ void __launch_bounds__(256) tc_maxima(const TcSector* __restrict__ secs, const int64_t* __restrict__ a_ts,
+                                                 const int64_t* __restrict__ b_ts, int nsec, int64_t a_tiles,
+                                                 int64_t b_tiles, const double* __restrict__ A,
+                                                 const double* __restrict__ B, unsigned long long* __restrict__ amax,
+                                                 unsigned long long* __restrict__ bmax) {
   __shared__ unsigned long long part[4][kTN];
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
-    const int g = find_seg(tstart, nsec, t);
-    const TcSector& S = secs[g];
-    const int64_t local = t - tstart[g];
-    const int nt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
-    const int r = threadIdx.x % kTN, kq = threadIdx.x / kTN;  // lanes along the columns
-    const int64_t j = (int64_t)nt * kTN + r;
-    unsigned long long m = 0;
-    if (j < S.N) {
-      const unsigned long long* src = (const unsigned long long*)(B + S.b_off + j);
-      for (int k = kt * kTK + kq; k < min(S.K, (kt + 1) * kTK); k += 4) {
-        const unsigned long long v = __ldg(src + (int64_t)k * S.N) & 0x7FFFFFFFFFFFFFFFull;
-        m = v > m ? v : m;
+  for (int64_t t = blockIdx.x; t < a_tiles + b_tiles; t += gridDim.x) {
+    if (t < a_tiles) {
+      const int g = find_seg(a_ts, nsec, t);
+      const TcSector& S = secs[g];
+      const int64_t local = t - a_ts[g];
+      const int mt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
+      for (int r0 = 0; r0 < kTM; r0 += 32) {  // 8 lanes per row, 32 rows per pass
+        const int r = r0 + (threadIdx.x >> 3), c = threadIdx.x & 7;
+        const int64_t i = (int64_t)mt * kTM + r;
+        unsigned long long m = 0;
+        if (i < S.M) {
+          const unsigned long long* src = (const unsigned long long*)(A + S.a_off + i * S.K);
+          const int k0 = kt * kTK + c * 8;
+#pragma unroll
+          for (int q = 0; q < 8; q++)
+            if (k0 + q < S.K) {
+              const unsigned long long v = __ldg(src + k0 + q) & 0x7FFFFFFFFFFFFFFFull;
+              m = v > m ? v : m;
+            }
+        }
+#pragma unroll
+        for (int o = 4; o; o >>= 1) {
+          const unsigned long long v = __shfl_xor_sync(0xffffffffu, m, o);
+          m = v > m ? v : m;
+        }
+        if (c == 0 && i < S.M && m) atomicMax(amax + S.ea_off + i, m);
       }
+    } else {
+      const int64_t u = t - a_tiles;
+      const int g = find_seg(b_ts, nsec, u);
+      const TcSector& S = secs[g];
+      const int64_t local = u - b_ts[g];
+      const int nt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
+      const int r = threadIdx.x % kTN, kq = threadIdx.x / kTN;  // lanes along the columns
+      const int64_t j = (int64_t)nt * kTN + r;
+      unsigned long long m = 0;
+      if (j < S.N) {
+        const unsigned long long* src = (const unsigned long long*)(B + S.b_off + j);
+        for (int k = kt * kTK + kq; k < min(S.K, (kt + 1) * kTK); k += 4) {
+          const unsigned long long v = __ldg(src + (int64_t)k * S.N) & 0x7FFFFFFFFFFFFFFFull;
+          m = v > m ? v : m;
+        }
+      }
+      part[kq][r] = m;
+      __syncthreads();
+      if (kq == 0 && j < S.N) {
+        unsigned long long v = part[0][r];
+        for (int q = 1; q < 4; q++) v = part[q][r] > v ? part[q][r] : v;
+        if (v) atomicMax(bmax + S.eb_off + j, v);
+      }
+      __syncthreads();
     }
-    part[kq][r] = m;
-    __syncthreads();
-    if (kq == 0 && j < S.N) {
-      unsigned long long v = part[0][r];
-      for (int q = 1; q < 4; q++) v = part[q][r] > v ? part[q][r] : v;
-      if (v) atomicMax(bmax + S.eb_off + j, v);
-    }
-    __syncthreads();
   }
 }
 
@@ -191,12 +191,12 @@ __device__ __forceinline__ void make_slices(const double (&x)[8], int e, uint4 (
   for (int s = 0; s < NS; s++) out[s] = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
 }
 
-// A tiles: (sector, mt, kt) -> NS images of 128 rows x 64 k; one CTA per tile
+// A tile t: (sector, mt, kt) -> NS images of 128 rows x 64 k
 template <int NS>
-__global__ void __launch_bounds__(256) tc_slice_a(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
-                                                  int nsec, int64_t ntiles, const double* __restrict__ A,
-                                                  const unsigned long long* __restrict__ ea, uint8_t* __restrict__ ws) {
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+__device__ __forceinline__ void slice_a_tile(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
+                                             int nsec, int64_t t, const double* __restrict__ A,
+                                             const unsigned long long* __restrict__ ea, uint8_t* __restrict__ ws) {
+  {
     const int g = find_seg(tstart, nsec, t);
     const TcSector& S = secs[g];
     const int64_t local = t - tstart[g];
@@ -226,12 +226,12 @@ __global__ void __launch_bounds__(256) tc_slice_a(const TcSector* __restrict__ s
   }
 }
 
-// B tiles: (sector, nt, kt) -> NS images of 64 columns (rows of the image) x 64 k
+// B tile t: (sector, nt, kt) -> NS images of 64 columns (rows of the image) x 64 k
 template <int NS>
-__global__ void __launch_bounds__(256) tc_slice_b(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
-                                                  int nsec, int64_t ntiles, const double* __restrict__ B,
-                                                  const unsigned long long* __restrict__ eb, uint8_t* __restrict__ ws) {
-  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+__device__ __forceinline__ void slice_b_tile(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
+                                             int nsec, int64_t t, const double* __restrict__ B,
+                                             const unsigned long long* __restrict__ eb, uint8_t* __restrict__ ws) {
+  {
     const int g = find_seg(tstart, nsec, t);
     const TcSector& S = secs[g];
     const int64_t local = t - tstart[g];
@@ -258,6 +258,21 @@ __global__ void __launch_bounds__(256) tc_slice_b(const TcSector* __restrict__ s
 #pragma unroll
       for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * kBTile + off) = o[s];
     }
+  }
+}
+
+// every A tile, then every B tile, in one launch
+template <int NS>
+__global__ void __launch_bounds__(256) tc_slices(const TcSector* __restrict__ secs, const int64_t* __restrict__ a_ts,
+                                                 const int64_t* __restrict__ b_ts, int nsec, int64_t a_tiles,
+                                                 int64_t b_tiles, const double* __restrict__ A,
+                                                 const double* __restrict__ B, const unsigned long long* __restrict__ ea,
+                                                 const unsigned long long* __restrict__ eb, uint8_t* __restrict__ ws) {
+  for (int64_t t = blockIdx.x; t < a_tiles + b_tiles; t += gridDim.x) {
+    if (t < a_tiles)
+      slice_a_tile<NS>(secs, a_ts, nsec, t, A, ea, ws);
+    else
+      slice_b_tile<NS>(secs, b_ts, nsec, t - a_tiles, B, eb, ws);
   }
 }
 
@@ -462,33 +477,18 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
-void launch_tc_maxima(const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
-                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
-                      unsigned long long* amax, unsigned long long* bmax, int num_sms, cudaStream_t s) {
-  if (a_tiles) {
-    int g = (int)std::min<int64_t>(a_tiles, (int64_t)num_sms * 8);
-    tc_max_a<<<g, 256, 0, s>>>(secs, a_tstart, nsec, a_tiles, A, amax);
-  }
-  if (b_tiles) {
-    int g = (int)std::min<int64_t>(b_tiles, (int64_t)num_sms * 8);
-    tc_max_b<<<g, 256, 0, s>>>(secs, b_tstart, nsec, b_tiles, B, bmax);
-  }
+void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
+                    int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,
+                    unsigned long long* bmax, int64_t nmax, uint8_t* images, int num_sms, cudaStream_t s) {
+  TN_CUDA(cudaMemsetAsync(amax, 0, (size_t)nmax * sizeof(unsigned long long), s));  // bmax follows amax
+  int g1 = (int)std::min<int64_t>(a_tiles + b_tiles, (int64_t)num_sms * 8);
+  tc_maxima<<<g1, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax);
   TN_CUDA(cudaGetLastError());
-}
-
-void launch_tc_slices(int ns, const TcSector* secs, int nsec, const int64_t* a_tstart, int64_t a_tiles,
-                      const int64_t* b_tstart, int64_t b_tiles, const double* A, const double* B,
-                      const unsigned long long* ea, const unsigned long long* eb, uint8_t* ws, int num_sms,
-                      cudaStream_t s) {
-  int ga = (int)std::min<int64_t>(a_tiles, (int64_t)num_sms * 8);
-  int gb = (int)std::min<int64_t>(b_tiles, (int64_t)num_sms * 8);
-  if (ns == 7) {
-    if (a_tiles) tc_slice_a<7><<<ga, 256, 0, s>>>(secs, a_tstart, nsec, a_tiles, A, ea, ws);
-    if (b_tiles) tc_slice_b<7><<<gb, 256, 0, s>>>(secs, b_tstart, nsec, b_tiles, B, eb, ws);
-  } else {
-    if (a_tiles) tc_slice_a<1><<<ga, 256, 0, s>>>(secs, a_tstart, nsec, a_tiles, A, ea, ws);
-    if (b_tiles) tc_slice_b<1><<<gb, 256, 0, s>>>(secs, b_tstart, nsec, b_tiles, B, eb, ws);
-  }
+  int g2 = (int)std::min<int64_t>(a_tiles + b_tiles, (int64_t)num_sms * 8);
+  if (ns == 7)
+    tc_slices<7><<<g2, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax, images);
+  else
+    tc_slices<1><<<g2, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax, images);
   TN_CUDA(cudaGetLastError());
 }
 

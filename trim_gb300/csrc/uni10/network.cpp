@@ -8,7 +8,10 @@
 #include <sstream>
 #include <stdexcept>
 
+#include <cuda_runtime.h>
+
 #include "../../../include/uni10/Network.h"
+#include "../engine/engine.h"
 
 namespace uni10 {
 
@@ -242,12 +245,16 @@ Network Network::fromText(const std::string& text) {
 Network::Network(Network&& o) noexcept
     : names(std::move(o.names)), name2pos(std::move(o.name2pos)), label_arr(std::move(o.label_arr)),
       Rnums(std::move(o.Rnums)), leafs(std::move(o.leafs)), tensors(std::move(o.tensors)), order(std::move(o.order)),
-      brakets(std::move(o.brakets)), root(o.root), load(o.load) {
+      brakets(std::move(o.brakets)), root(o.root), load(o.load), graph_exec(o.graph_exec), graph(o.graph),
+      graph_out(std::move(o.graph_out)), graph_sigs(std::move(o.graph_sigs)) {
   o.root = nullptr;
   o.load = false;
+  o.graph_exec = nullptr;
+  o.graph = nullptr;
 }
 
 Network::~Network() {
+  drop_graph();
   if (load) destruct();
   for (Node* l : leafs) delete l;
   for (UniTensor* t : tensors) delete t;
@@ -427,20 +434,23 @@ void Network::destruct() {
   load = false;
 }
 
+// Network.cpp:719-739 contracts with fast=true, leaving the leaves permuted;
+// here the leaves are never modified (same result, and their buffers stay
+// where a captured graph expects them).
 UniTensor Network::merge(Node* nd) {
   if (nd->left->T == nullptr) {
     UniTensor lftT = merge(nd->left);
     if (nd->right->T == nullptr) {
       UniTensor rhtT = merge(nd->right);
-      return contract(lftT, rhtT, true);
+      return contract_const(lftT, rhtT);
     }
-    return contract(lftT, *(nd->right->T), true);
+    return contract_const(lftT, *(nd->right->T));
   }
   if (nd->right->T == nullptr) {
     UniTensor rhtT = merge(nd->right);
-    return contract(*(nd->left->T), rhtT, true);
+    return contract_const(*(nd->left->T), rhtT);
   }
-  return contract(*(nd->left->T), *(nd->right->T), true);
+  return contract_const(*(nd->left->T), *(nd->right->T));
 }
 
 UniTensor Network::launch(const std::string& _name) {
@@ -450,6 +460,77 @@ UniTensor Network::launch(const std::string& _name) {
   if (!label_arr.empty() && label_arr[idx].size() > 1) UniT.permute(label_arr[idx], Rnums[idx]);
   UniT.setName(_name);
   return UniT;
+}
+
+// ---------------------------------------------------------------- CUDA graph
+void Network::drop_graph() {
+  if (graph_exec) cudaGraphExecDestroy((cudaGraphExec_t)graph_exec);
+  if (graph) cudaGraphDestroy((cudaGraph_t)graph);
+  graph_exec = nullptr;
+  graph = nullptr;
+}
+
+void Network::capture() {
+  drop_graph();
+  UniTensor warm = launch();  // plans, workspace and tree in place
+  graph_out = warm;           // persistent output buffer, allocated outside the graph
+  graph_sigs.clear();
+  for (UniTensor* t : tensors) graph_sigs.push_back(t->sectorMap() ? t->sectorMap()->key : std::string());
+  tn::Ctx& c = *tn::default_ctx();
+  c.device_error_word();
+  TN_CUDA(cudaStreamSynchronize(c.stream));
+  // capture on a private stream (the context's may be the legacy default
+  // stream, which cannot be captured); the graph is replayed on c.stream
+  cudaStream_t orig = c.stream, cap = nullptr;
+  TN_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  cudaGraph_t g = nullptr;
+  const int64_t l0 = c.launches;
+  c.stream = cap;
+  cudaError_t began = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  if (began != cudaSuccess) {
+    c.stream = orig;
+    cudaStreamDestroy(cap);
+    TN_CUDA(began);
+  }
+  try {
+    UniTensor r = launch();
+    TN_CUDA(cudaMemcpyAsync(graph_out.getElem(), r.getElem(), r.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
+                            cap));
+  } catch (...) {
+    cudaStreamEndCapture(cap, &g);
+    if (g) cudaGraphDestroy(g);
+    c.stream = orig;
+    cudaStreamDestroy(cap);
+    cudaGetLastError();
+    throw;
+  }
+  cudaError_t ended = cudaStreamEndCapture(cap, &g);
+  c.stream = orig;
+  cudaStreamDestroy(cap);
+  TN_CUDA(ended);
+  cudaGraphExec_t e = nullptr;
+  TN_CUDA(cudaGraphInstantiate(&e, g, 0));
+  graph = g;
+  graph_exec = e;
+  graph_kernels = c.launches - l0;  // kernels inside the graph
+  c.launches = l0;
+}
+
+void Network::replay() {
+  if (!graph_exec) throw std::runtime_error("Network::replay: no captured graph (call capture() first)");
+  for (size_t i = 0; i < tensors.size(); i++) {
+    const std::string k = tensors[i]->sectorMap() ? tensors[i]->sectorMap()->key : std::string();
+    if (k != graph_sigs[i])
+      throw std::runtime_error("Network::replay: tensor '" + names[i] + "' changed its bonds since capture(); capture again");
+  }
+  tn::Ctx& c = *tn::default_ctx();
+  TN_CUDA(cudaGraphLaunch((cudaGraphExec_t)graph_exec, c.stream));
+  c.launched((int)graph_kernels);
+}
+
+const UniTensor& Network::output() const {
+  if (!graph_exec) throw std::runtime_error("Network::output: no captured graph");
+  return graph_out;
 }
 
 std::string Network::tree() {

@@ -18,7 +18,8 @@ using tn::DevBuf;
 
 static thread_local int g_mode = TN_MODE_FP64;
 void setContractMode(int mode) {
-  if (mode < TN_MODE_FP64 || mode > TN_MODE_FAST_TF32) throw std::runtime_error("unknown contraction mode");
+  const int m = mode & ~TN_MODE_TC_ONLY;
+  if (m < TN_MODE_FP64 || m > TN_MODE_FAST_TF32) throw std::runtime_error("unknown contraction mode");
   g_mode = mode;
 }
 int contractMode() { return g_mode; }
@@ -336,17 +337,31 @@ void UniTensor::putBlock(const Qnum& q, const Block& mat) {
 }
 
 // ---------------------------------------------------------------- permute
-// UniTensorReal.cpp:532-768
-UniTensor& UniTensor::permute(const std::vector<int>& newLabels, int rowBondNum) {
-  if ((status & HAVEBOND) == 0) throw std::runtime_error("There is no bond in the tensor(scalar) to permute.");
-  if (labels.size() != newLabels.size())
+UniTensor UniTensor::alias(const UniTensor& t) {
+  UniTensor a;
+  a.name = t.name;
+  a.bonds = t.bonds;
+  a.labels = t.labels;
+  a.RBondNum = t.RBondNum;
+  a.m_elemNum = t.m_elemNum;
+  a.status = t.status;
+  a.smap = t.smap;
+  a.elem = t.elem;  // shared buffer
+  return a;
+}
+
+// The permuted tensor as a new tensor; src is not modified
+// (UniTensorReal.cpp:532-768 computes the same and then assigns it to *this).
+UniTensor UniTensor::permuted(const UniTensor& src, const std::vector<int>& newLabels, int rowBondNum) {
+  if ((src.status & HAVEBOND) == 0) throw std::runtime_error("There is no bond in the tensor(scalar) to permute.");
+  if (src.labels.size() != newLabels.size())
     throw std::runtime_error("The size of the input new labels does not match for the number of bonds.");
-  const int n = (int)bonds.size();
+  const int n = (int)src.bonds.size();
   std::vector<int> rsp(n, 0);
   size_t cnt = 0;
   for (int i = 0; i < n; i++)
     for (int j = 0; j < n; j++)
-      if (labels[i] == newLabels[j]) {
+      if (src.labels[i] == newLabels[j]) {
         rsp[j] = i;
         cnt++;
       }
@@ -358,25 +373,33 @@ UniTensor& UniTensor::permute(const std::vector<int>& newLabels, int rowBondNum)
       inorder = false;
       break;
     }
-  if (inorder && RBondNum == rowBondNum) return *this;
+  if (inorder && src.RBondNum == rowBondNum) {
+    UniTensor same = alias(src);
+    same.labels = newLabels;
+    return same;
+  }
   std::vector<Bond> outBonds;
-  for (int b = 0; b < n; b++) outBonds.push_back(bonds[rsp[b]]);
+  for (int b = 0; b < n; b++) outBonds.push_back(src.bonds[rsp[b]]);
   for (int b = 0; b < n; b++) outBonds[b].change(b < rowBondNum ? BD_IN : BD_OUT);
-  UniTensor out(outBonds, name, NoFill{});
-  if (status & HAVEELEM) {
+  UniTensor out(outBonds, src.name, NoFill{});
+  if (src.status & HAVEELEM) {
     tn::Ctx& c = C();
-    auto plan = tn::get_perm_plan(c, *smap, *out.smap, rsp);
-    tn::run_permute(c, *plan, dptr(elem), dptr(out.elem));
+    auto plan = tn::get_perm_plan(c, *src.smap, *out.smap, rsp);
+    tn::run_permute(c, *plan, dptr(src.elem), dptr(out.elem));
     out.status |= HAVEELEM;
   }
-  // take over the permuted tensor (buffers are moved, not copied)
-  bonds = std::move(out.bonds);
-  smap = std::move(out.smap);
-  elem = std::move(out.elem);
-  RBondNum = out.RBondNum;
-  m_elemNum = out.m_elemNum;
-  status = out.status;
-  labels = newLabels;
+  out.labels = newLabels;
+  return out;
+}
+
+// UniTensorReal.cpp:532-768 (in place)
+UniTensor& UniTensor::permute(const std::vector<int>& newLabels, int rowBondNum) {
+  UniTensor out = permuted(*this, newLabels, rowBondNum);
+  if (out.elem == elem) {  // already in this order
+    labels = newLabels;
+    return *this;
+  }
+  *this = std::move(out);
   return *this;
 }
 
@@ -499,12 +522,21 @@ UniTensor& UniTensor::operator*=(const UniTensor& Tb) {
 
 // ---------------------------------------------------------------- contract
 // UniTensorTools.cpp:124-244
-UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast) {
+UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast) { return UniTensor::contract_impl(Ta, Tb, fast, true); }
+
+UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb) {
+  return UniTensor::contract_impl(const_cast<UniTensor&>(Ta), const_cast<UniTensor&>(Tb), true, false);
+}
+
+// mutate: permute the operands in place like the reference (restored unless
+// fast); otherwise the permuted operands are temporaries and Ta, Tb are
+// never written.
+UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool mutate) {
   if (!(Ta.status & Tb.status & UniTensor::HAVEELEM))
     throw std::runtime_error("Cannot perform contraction of two tensors before setting their elements.");
   if (&Ta == &Tb) {
     UniTensor tmp = Tb;
-    return contract(Ta, tmp, fast);
+    return contract_impl(Ta, tmp, fast, mutate);
   }
   if ((Ta.status & UniTensor::HAVEBOND) && (Tb.status & UniTensor::HAVEBOND)) {
     const int an = (int)Ta.bonds.size(), bn = (int)Tb.bonds.size();
@@ -535,17 +567,25 @@ UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast) {
         newLabelC.push_back(Tb.labels[b]);
       }
     const int conBond = (int)interLabel.size();
-    Ta.permute(newLabelA, an - conBond);
-    Tb.permute(newLabelB, conBond);
+    UniTensor pa, pb;
+    if (mutate) {
+      Ta.permute(newLabelA, an - conBond);
+      Tb.permute(newLabelB, conBond);
+    } else {
+      pa = permuted(Ta, newLabelA, an - conBond);
+      pb = permuted(Tb, newLabelB, conBond);
+    }
+    const UniTensor& A_ = mutate ? Ta : pa;
+    const UniTensor& B_ = mutate ? Tb : pb;
     std::vector<Bond> cBonds;
-    for (int i = 0; i < an - conBond; i++) cBonds.push_back(Ta.bonds[i]);
-    for (int i = conBond; i < bn; i++) cBonds.push_back(Tb.bonds[i]);
+    for (int i = 0; i < an - conBond; i++) cBonds.push_back(A_.bonds[i]);
+    for (int i = conBond; i < bn; i++) cBonds.push_back(B_.bonds[i]);
     UniTensor Tc(cBonds);
     if (!cBonds.empty()) Tc.setLabel(newLabelC);
     // every block of Ta with a block of the same charge in Tb is one sector GEMM
     std::vector<tn_sector_gemm> list;
-    const tn::SectorMap* ma = Ta.smap.get();
-    const tn::SectorMap* mb = Tb.smap.get();
+    const tn::SectorMap* ma = A_.smap.get();
+    const tn::SectorMap* mb = B_.smap.get();
     const tn::SectorMap* mc = Tc.smap.get();
     for (const auto& ba : ma->blocks) {
       int ib = mb->find_block(ba.q);
@@ -565,7 +605,7 @@ UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast) {
       g.c_off = mc ? mc->blocks[ic].off : 0;
       list.push_back(g);
     }
-    tn::run_sector_gemms(C(), g_mode, list, dptr(Ta.elem), dptr(Tb.elem), dptr(Tc.elem));
+    tn::run_sector_gemms(C(), g_mode, list, dptr(A_.elem), dptr(B_.elem), dptr(Tc.elem));
     Tc.status |= UniTensor::HAVEELEM;
     if (conBond == 0) {  // outer product (UniTensorTools.cpp:206-225)
       int idx = 0;
@@ -575,7 +615,7 @@ UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast) {
       for (int i = oldRnumB; i < bn; i++) newLabelC[idx++] = oldLabelB[i];
       Tc.permute(newLabelC, oldRnumA + oldRnumB);
     }
-    if (!fast) {
+    if (mutate && !fast) {
       Ta.permute(oldLabelA, oldRnumA);
       Tb.permute(oldLabelB, oldRnumB);
     }

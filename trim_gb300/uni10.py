@@ -221,6 +221,17 @@ class Network:
         call("tn_network_launch", self.h, _mode(mode), C.byref(h))
         return UniTensor(_h=h)
 
+    def capture(self, mode="fp64") -> None:
+        call("tn_network_capture", self.h, _mode(mode))
+
+    def replay(self) -> None:
+        call("tn_network_replay", self.h)
+
+    def output(self) -> UniTensor:
+        h = C.c_void_p()
+        call("tn_network_output", self.h, C.byref(h))
+        return UniTensor(_h=h)
+
     def tree(self) -> str:
         buf = C.create_string_buffer(4096)
         call("tn_network_tree", self.h, buf, 4096)
