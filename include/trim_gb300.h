@@ -55,8 +55,9 @@ enum {
   TN_MODE_FAST_BF16 = 2, /* one BF16 slice, FP32 accumulation */
   TN_MODE_FAST_TF32 = 3, /* TF32 operands, FP32 accumulation */
   /* flag: in the tensor-core modes, send every sector to the tensor cores
-   * (by default a contraction under 5e7 FLOP, or a sector with K < 16 or
-   * under 16K multiply-adds, runs on the exact FP64 kernel instead) */
+   * (by default a contraction under 5e7 FLOP, or a sector with K < 16,
+   * M < 32, N < 16 or under 16K multiply-adds, runs on the exact FP64
+   * kernel instead) */
   TN_MODE_TC_ONLY = 0x100
 };
 
@@ -168,6 +169,11 @@ int tn_tensor_combine_bond(tn_tensor_t t, int n, const int* labels);
 /* contract(Ta, Tb, fast) (UniTensor.h:605; UniTensorTools.cpp:124-244);
  * mutates a and b like the reference (restored unless fast). */
 int tn_contract(tn_tensor_t a, tn_tensor_t b, int fast, int mode, tn_tensor_t* out);
+/* n independent contractions a[i] . b[i] (operands untouched); all their
+ * sector GEMMs run in one grouped launch.  The reference contracts pair by
+ * pair (UniTensorTools.cpp:124-244, one matrixMul per sector); out[i] is
+ * what contract(a[i], b[i]) returns. */
+int tn_contract_batch(int n, const tn_tensor_t* a, const tn_tensor_t* b, int mode, tn_tensor_t* out);
 /* otimes(Ta, Tb) (UniTensorTools.cpp:246-273) */
 int tn_otimes(tn_tensor_t a, tn_tensor_t b, int mode, tn_tensor_t* out);
 /* multiply every element by a (operator*=(Real), UniTensor.h:262) */

@@ -86,6 +86,12 @@ class UniTensor {
   // contraction that leaves both operands untouched (permuted operands are
   // temporaries); Network::launch uses it so its leaves keep their buffers
   friend UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb);
+std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, const std::vector<const UniTensor*>& Bs);
+  // Many independent contractions (operands untouched): every pair's sector
+  // GEMMs run in one grouped launch.  No counterpart call in the reference,
+  // which contracts pair by pair.
+  friend std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As,
+                                               const std::vector<const UniTensor*>& Bs);
   friend UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
 
   UniTensor& operator*=(double a);
@@ -106,6 +112,9 @@ class UniTensor {
   UniTensor(const std::vector<Bond>& _bonds, const std::string& _name, NoFill);
   static UniTensor permuted(const UniTensor& src, const std::vector<int>& newLabels, int rowBondNum);
   static UniTensor contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool mutate);
+  struct ContractWork;
+  static void prepare_contract(const UniTensor& Ta, const UniTensor& Tb, ContractWork& w);
+  static void finish_contract(ContractWork& w);
   void initUniT(bool zero = true);
   std::string name;
   std::vector<Bond> bonds;
@@ -121,6 +130,7 @@ class UniTensor {
 
 UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast = false);
 UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb);
+std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, const std::vector<const UniTensor*>& Bs);
 UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
 UniTensor operator*(const UniTensor& Ta, double a);
 UniTensor operator*(double a, const UniTensor& Ta);

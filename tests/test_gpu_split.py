@@ -177,3 +177,26 @@ def test_network_graph_capture_replay(env):
         eager = net.launch(mode).get_elem()
         assert np.array_equal(out.get_elem(), eager)
         assert not np.array_equal(eager, eager0)
+
+
+def test_contract_batch_matches_pairwise(env):
+    """One grouped launch for many contractions equals the pairwise contract()
+    of each pair: golden fixtures (reference outputs) and 48 random pairs."""
+    torch, capi, tu = env
+    c = G.cases()["batched_small"]
+    spec = wl.batched(**c["params"])
+    A = [tu.UniTensor(t1.bonds, t1.labels, G.arr("batched_small", t1.name)) for t1, _ in spec["pairs"]]
+    B = [tu.UniTensor(t2.bonds, t2.labels, G.arr("batched_small", t2.name)) for _, t2 in spec["pairs"]]
+    for mode, tol in (("fp64", 1e-13), ("split_tc", SPLIT_TOL)):
+        outs = tu.contract_batch(A, B, mode)
+        for i, o in enumerate(outs):
+            assert rel(o.get_elem(), G.arr("batched_small", f"C{i}")) <= tol, (mode, i)
+    spec = wl.batched(n=48, lo=16, hi=96, seed=99)
+    rng = np.random.default_rng(1)
+    A = [tu.UniTensor(t1.bonds, t1.labels, wl.gen_elems(t1, rng)) for t1, _ in spec["pairs"]]
+    B = [tu.UniTensor(t2.bonds, t2.labels, wl.gen_elems(t2, rng)) for _, t2 in spec["pairs"]]
+    ref = [tu.contract(a, b, mode="fp64").get_elem() for a, b in zip(A, B)]
+    for mode, tol in (("fp64", 1e-13), ("split", SPLIT_TOL), ("split_tc", SPLIT_TOL)):
+        outs = tu.contract_batch(A, B, mode)
+        for o, r in zip(outs, ref):
+            assert rel(o.get_elem(), r) <= tol, mode

@@ -75,6 +75,7 @@ _PROTOS = {
     "tn_tensor_combine_bond": (_I, [_P, _I, _IP]),
     "tn_contract": (_I, [_P, _P, _I, _I, C.POINTER(_P)]),
     "tn_otimes": (_I, [_P, _P, _I, C.POINTER(_P)]),
+    "tn_contract_batch": (_I, [_I, C.POINTER(_P), C.POINTER(_P), _I, C.POINTER(_P)]),
     "tn_tensor_scale": (_I, [_P, C.c_double]),
     "tn_network_create": (_I, [_P, C.c_char_p, C.POINTER(_P)]),
     "tn_network_destroy": (_I, [_P]),

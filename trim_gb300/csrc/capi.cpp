@@ -416,6 +416,26 @@ int tn_contract(tn_tensor_t a, tn_tensor_t b, int fast, int mode, tn_tensor_t* o
   });
 }
 
+int tn_contract_batch(int n, const tn_tensor_t* a, const tn_tensor_t* b, int mode, tn_tensor_t* out) {
+  return guard([&] {
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative batch size");
+    if (n == 0) return;
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    std::vector<const uni10::UniTensor*> A(n), B(n);
+    for (int i = 0; i < n; i++) {
+      need(a[i], "a[i]");
+      need(b[i], "b[i]");
+      A[i] = &a[i]->t;
+      B[i] = &b[i]->t;
+    }
+    ModeScope ms(mode);
+    std::vector<uni10::UniTensor> r = uni10::contract_batch(A, B);
+    for (int i = 0; i < n; i++) out[i] = new tn_tensor_s{std::move(r[i])};
+  });
+}
+
 int tn_otimes(tn_tensor_t a, tn_tensor_t b, int mode, tn_tensor_t* out) {
   return guard([&] {
     need(a, "a");

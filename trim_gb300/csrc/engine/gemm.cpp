@@ -3,6 +3,7 @@
 // become one work list of output tiles, split along K until every SM has
 // work, and run in one launch (plus a deterministic split-K reduction).
 #include <algorithm>
+#include <cmath>
 #include <cstring>
 
 #include "engine.h"
@@ -14,23 +15,28 @@ constexpr int kTileM = 16, kTileN = 32;
 
 std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, int num_sms, bool allow_split,
                                       int64_t* ws_elems) {
-  int64_t tiles = 0, work = 0;
+  // K is split so that no work item (one 16x32 tile over a K range) carries
+  // much more than an even share of the total, with at least ~4 items per SM
+  int64_t tiles = 0;
+  double work = 0;
   for (const auto& g : list) {
     int64_t t = ((g.M + kTileM - 1) / kTileM) * ((g.N + kTileN - 1) / kTileN);
     tiles += t;
-    work += t * g.K;
+    work += (double)t * g.K;
   }
-  const int64_t target = (int64_t)num_sms * 4;
+  const int64_t target_items = (int64_t)num_sms * 8;
+  const double kmax = std::max(64.0, work / (double)target_items);  // K per item
   std::vector<GemmTile> out;
   int64_t ws = 0;
   for (const auto& g : list) {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX || g.N > INT32_MAX || g.K > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large");
     int nsplit = 1;
-    if (allow_split && tiles < target) {
-      // spread the K loop so the whole chip shares the FP64 work
-      nsplit = (int)std::min<int64_t>((target + tiles - 1) / tiles, (g.K + 15) / 16);
-      nsplit = std::max(1, std::min(nsplit, 64));
+    if (allow_split) {
+      nsplit = (int)std::ceil((double)g.K / kmax);
+      if (tiles < (int64_t)num_sms * 4)  // few tiles: spread the K loop over the chip
+        nsplit = std::max<int>(nsplit, (int)std::min<int64_t>((num_sms * 4 + tiles - 1) / tiles, (g.K + 15) / 16));
+      nsplit = std::max(1, std::min(nsplit, 256));
     }
     const int kchunk = (int)((g.K + nsplit - 1) / nsplit);
     nsplit = (int)((g.K + kchunk - 1) / kchunk);
@@ -61,7 +67,6 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
       }
   }
   *ws_elems = ws;
-  (void)work;
   return out;
 }
 }  // namespace
@@ -137,8 +142,9 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
 // Tensor-core modes route work where the tensor-core path cannot pay for its
 // fixed cost (operand slicing + a second launch, ~70 us measured on GB300) --
 // a whole contraction under 5e7 FLOP, or a sector with K < 16 or under 16K
-// multiply-adds -- to the FP64 kernel, which is exact and at that size no
-// slower; the rest goes to the tcgen05 kernel.
+// multiply-adds -- and sectors the 128 x 64 tensor tiles would pad four-fold
+// or more (M < 32 or N < 16) to the FP64 kernel, which is exact and for those
+// shapes no slower; the rest goes to the tcgen05 kernel.
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
                       double* C) {
   if (list.empty()) return;
@@ -154,7 +160,8 @@ void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& lis
   for (const auto& g : list) total += 2.0 * g.M * g.N * g.K;
   std::vector<tn_sector_gemm> tc, f64;
   for (const auto& g : list) {
-    const bool small = !tc_only && (total < 5.0e7 || g.K < 16 || (double)g.M * g.N * g.K < 16384.0);
+    const bool small = !tc_only && (total < 5.0e7 || g.K < 16 || g.M < 32 || g.N < 16 ||
+                                     (double)g.M * g.N * g.K < 16384.0);
     (small ? f64 : tc).push_back(g);
   }
   if (!f64.empty()) run_fp64(ctx, f64, A, B, C);

@@ -80,6 +80,8 @@ __global__ void __launch_bounds__(256) tc_maxima(const TcSector* __restrict__ se
                                                  const double* __restrict__ B, unsigned long long* __restrict__ amax,
                                                  unsigned long long* __restrict__ bmax) {
   __shared__ unsigned long long part[4][kTN];
+  if (threadIdx.x < kTN) part[0][threadIdx.x] = 0;
+  __syncthreads();
   for (int64_t t = blockIdx.x; t < a_tiles + b_tiles; t += gridDim.x) {
     if (t < a_tiles) {
       const int g = find_seg(a_ts, nsec, t);
@@ -113,23 +115,29 @@ __global__ void __launch_bounds__(256) tc_maxima(const TcSector* __restrict__ se
       const TcSector& S = secs[g];
       const int64_t local = u - b_ts[g];
       const int nt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
-      const int r = threadIdx.x % kTN, kq = threadIdx.x / kTN;  // lanes along the columns
-      const int64_t j = (int64_t)nt * kTN + r;
+      const int n0 = nt * kTN, k0 = kt * kTK;
+      const int w = min(kTN, S.N - n0), h = min(kTK, S.K - k0);
+      // flat walk of the h x w block: consecutive threads read consecutive
+      // addresses even when the sector is narrower than the tile
       unsigned long long m = 0;
-      if (j < S.N) {
-        const unsigned long long* src = (const unsigned long long*)(B + S.b_off + j);
-        for (int k = kt * kTK + kq; k < min(S.K, (kt + 1) * kTK); k += 4) {
-          const unsigned long long v = __ldg(src + (int64_t)k * S.N) & 0x7FFFFFFFFFFFFFFFull;
-          m = v > m ? v : m;
+      int col = -1;
+      for (int f = threadIdx.x; f < h * w; f += blockDim.x) {
+        const int k = f / w, n = f - k * w;
+        const unsigned long long v =
+            __ldg((const unsigned long long*)(B + S.b_off) + (int64_t)(k0 + k) * S.N + n0 + n) & 0x7FFFFFFFFFFFFFFFull;
+        if (n != col) {  // flush the running maximum of the previous column
+          if (col >= 0 && m) atomicMax((unsigned long long*)&part[0][col], m);
+          col = n;
+          m = 0;
         }
+        m = v > m ? v : m;
       }
-      part[kq][r] = m;
+      // part[0][n] doubles as the per-tile column maximum (zeroed below)
+      if (col >= 0 && m) atomicMax((unsigned long long*)&part[0][col], m);
       __syncthreads();
-      if (kq == 0 && j < S.N) {
-        unsigned long long v = part[0][r];
-        for (int q = 1; q < 4; q++) v = part[q][r] > v ? part[q][r] : v;
-        if (v) atomicMax(bmax + S.eb_off + j, v);
-      }
+      if (threadIdx.x < w && part[0][threadIdx.x]) atomicMax(bmax + S.eb_off + n0 + threadIdx.x, part[0][threadIdx.x]);
+      __syncthreads();
+      if (threadIdx.x < kTN) part[0][threadIdx.x] = 0;
       __syncthreads();
     }
   }
@@ -226,38 +234,44 @@ __device__ __forceinline__ void slice_a_tile(const TcSector* __restrict__ secs, 
   }
 }
 
-// B tile t: (sector, nt, kt) -> NS images of 64 columns (rows of the image) x 64 k
+// B tile t: (sector, nt, kt) -> NS images of 64 columns (rows of the image) x 64 k.
+// The FP64 block is first staged in shared memory with flat coalesced loads,
+// then each thread slices 8 consecutive k of one column.
 template <int NS>
 __device__ __forceinline__ void slice_b_tile(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
                                              int nsec, int64_t t, const double* __restrict__ B,
-                                             const unsigned long long* __restrict__ eb, uint8_t* __restrict__ ws) {
-  {
-    const int g = find_seg(tstart, nsec, t);
-    const TcSector& S = secs[g];
-    const int64_t local = t - tstart[g];
-    const int nt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
-    uint8_t* img = ws + S.b_img + (int64_t)local * NS * kBTile;
-    for (int u = threadIdx.x; u < kTN * 8; u += blockDim.x) {
-      const int r = u % kTN, c = u / kTN;  // lanes run along the columns: coalesced loads of B rows
-      const int64_t j = (int64_t)nt * kTN + r;
-      const int k0 = kt * kTK + c * 8;
-      double x[8];
-      int e = 0;
-      if (j < S.N) {
-        e = exp_of(eb[S.eb_off + j]);
-        const double* src = B + S.b_off + j;
+                                             const unsigned long long* __restrict__ eb, uint8_t* __restrict__ ws,
+                                             double (*stage)[kTN + 1]) {
+  const int g = find_seg(tstart, nsec, t);
+  const TcSector& S = secs[g];
+  const int64_t local = t - tstart[g];
+  const int nt = (int)(local / S.nkt), kt = (int)(local % S.nkt);
+  const int n0 = nt * kTN, k0 = kt * kTK;
+  const int w = min(kTN, S.N - n0), h = min(kTK, S.K - k0);
+  __syncthreads();  // the stage is reused tile after tile
+  for (int f = threadIdx.x; f < kTK * kTN; f += blockDim.x) {
+    const int k = f / kTN, n = f - k * kTN;
+    stage[k][n] = 0.0;
+  }
+  __syncthreads();
+  for (int f = threadIdx.x; f < h * w; f += blockDim.x) {
+    const int k = f / w, n = f - k * w;
+    stage[k][n] = __ldg(B + S.b_off + (int64_t)(k0 + k) * S.N + n0 + n);
+  }
+  __syncthreads();
+  uint8_t* img = ws + S.b_img + (int64_t)local * NS * kBTile;
+  for (int u = threadIdx.x; u < kTN * 8; u += blockDim.x) {
+    const int r = u % kTN, c = u / kTN;
+    int e = 0;
+    if (r < w) e = exp_of(eb[S.eb_off + n0 + r]);
+    double x[8];
 #pragma unroll
-        for (int q = 0; q < 8; q++) x[q] = (k0 + q < S.K) ? __ldg(src + (int64_t)(k0 + q) * S.N) : 0.0;
-      } else {
+    for (int q = 0; q < 8; q++) x[q] = stage[c * 8 + q][r];
+    uint4 o[NS];
+    make_slices<NS>(x, e, o);
+    const uint32_t off = swz_off(r, c);
 #pragma unroll
-        for (int q = 0; q < 8; q++) x[q] = 0.0;
-      }
-      uint4 o[NS];
-      make_slices<NS>(x, e, o);
-      const uint32_t off = swz_off(r, c);
-#pragma unroll
-      for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * kBTile + off) = o[s];
-    }
+    for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * kBTile + off) = o[s];
   }
 }
 
@@ -268,11 +282,12 @@ __global__ void __launch_bounds__(256) tc_slices(const TcSector* __restrict__ se
                                                  int64_t b_tiles, const double* __restrict__ A,
                                                  const double* __restrict__ B, const unsigned long long* __restrict__ ea,
                                                  const unsigned long long* __restrict__ eb, uint8_t* __restrict__ ws) {
+  __shared__ double stage[kTK][kTN + 1];
   for (int64_t t = blockIdx.x; t < a_tiles + b_tiles; t += gridDim.x) {
     if (t < a_tiles)
       slice_a_tile<NS>(secs, a_ts, nsec, t, A, ea, ws);
     else
-      slice_b_tile<NS>(secs, b_ts, nsec, t - a_tiles, B, eb, ws);
+      slice_b_tile<NS>(secs, b_ts, nsec, t - a_tiles, B, eb, ws, stage);
   }
 }
 

@@ -641,6 +641,115 @@ UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb) {
   return contract(T1, T2, true);
 }
 
+// ---------------------------------------------------------------- batches
+// One pair of a batch: permuted operands (aliases when already in contraction
+// order), the output and its sector GEMMs (offsets relative to the buffers).
+struct UniTensor::ContractWork {
+  UniTensor pa, pb, tc;
+  std::vector<tn_sector_gemm> sectors;
+  bool outer = false;
+  std::vector<int> outer_labels;
+  int outer_rn = 0;
+};
+
+// the label matching, permutes and output construction of contract
+// (UniTensorTools.cpp:138-200) without modifying Ta or Tb
+void UniTensor::prepare_contract(const UniTensor& Ta, const UniTensor& Tb, ContractWork& w) {
+  if (!(Ta.status & Tb.status & HAVEELEM))
+    throw std::runtime_error("Cannot perform contraction of two tensors before setting their elements.");
+  if (!((Ta.status & HAVEBOND) && (Tb.status & HAVEBOND)))
+    throw std::runtime_error("contract_batch: every operand needs bonds");
+  const int an = (int)Ta.bonds.size(), bn = (int)Tb.bonds.size();
+  std::vector<int> newLabelA, interLabel, newLabelB, newLabelC, markB(bn, 0);
+  for (int a = 0; a < an; a++) {
+    bool match = false;
+    for (int b = 0; b < bn; b++)
+      if (Ta.labels[a] == Tb.labels[b]) {
+        markB[b] = 1;
+        interLabel.push_back(Ta.labels[a]);
+        newLabelB.push_back(Tb.labels[b]);
+        if (!(Ta.bonds[a].dim() == Tb.bonds[b].dim()))
+          throw std::runtime_error("Cannot contract two bonds having different dimensions");
+        match = true;
+        break;
+      }
+    if (!match) {
+      newLabelA.push_back(Ta.labels[a]);
+      newLabelC.push_back(Ta.labels[a]);
+    }
+  }
+  for (int l : interLabel) newLabelA.push_back(l);
+  for (int b = 0; b < bn; b++)
+    if (markB[b] == 0) {
+      newLabelB.push_back(Tb.labels[b]);
+      newLabelC.push_back(Tb.labels[b]);
+    }
+  const int conBond = (int)interLabel.size();
+  w.pa = permuted(Ta, newLabelA, an - conBond);
+  w.pb = permuted(Tb, newLabelB, conBond);
+  std::vector<Bond> cBonds;
+  for (int i = 0; i < an - conBond; i++) cBonds.push_back(w.pa.bonds[i]);
+  for (int i = conBond; i < bn; i++) cBonds.push_back(w.pb.bonds[i]);
+  w.tc = UniTensor(cBonds);
+  if (!cBonds.empty()) w.tc.setLabel(newLabelC);
+  const tn::SectorMap* ma = w.pa.smap.get();
+  const tn::SectorMap* mb = w.pb.smap.get();
+  const tn::SectorMap* mc = w.tc.smap.get();
+  for (const auto& ba : ma->blocks) {
+    int ib = mb->find_block(ba.q);
+    if (ib < 0) continue;
+    const auto& bb = mb->blocks[ib];
+    int ic = mc ? mc->find_block(ba.q) : 0;
+    int64_t crow = mc ? (ic >= 0 ? mc->blocks[ic].rows : -1) : 1;
+    int64_t ccol = mc ? (ic >= 0 ? mc->blocks[ic].cols : -1) : 1;
+    if (!(ba.rows == crow && bb.cols == ccol && ba.cols == bb.rows))
+      throw std::runtime_error("The dimensions the bonds to be contracted out are different.");
+    w.sectors.push_back(tn_sector_gemm{ba.rows, bb.cols, ba.cols, ba.off, bb.off, mc ? mc->blocks[ic].off : 0});
+  }
+  w.outer = conBond == 0;
+  if (w.outer) {
+    const int ra = Ta.RBondNum, rb = Tb.RBondNum;
+    for (int i = 0; i < ra; i++) w.outer_labels.push_back(Ta.labels[i]);
+    for (int i = 0; i < rb; i++) w.outer_labels.push_back(Tb.labels[i]);
+    for (int i = ra; i < an; i++) w.outer_labels.push_back(Ta.labels[i]);
+    for (int i = rb; i < bn; i++) w.outer_labels.push_back(Tb.labels[i]);
+    w.outer_rn = ra + rb;
+  }
+}
+
+void UniTensor::finish_contract(ContractWork& w) {
+  w.tc.status |= HAVEELEM;
+  if (w.outer) w.tc.permute(w.outer_labels, w.outer_rn);
+}
+
+std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, const std::vector<const UniTensor*>& Bs) {
+  if (As.size() != Bs.size()) throw std::runtime_error("contract_batch: operand lists differ in length");
+  std::vector<UniTensor::ContractWork> work(As.size());
+  std::vector<tn_sector_gemm> all;
+  for (size_t i = 0; i < As.size(); i++) {
+    if (!As[i] || !Bs[i]) throw std::runtime_error("contract_batch: null operand");
+    UniTensor::prepare_contract(*As[i], *Bs[i], work[i]);
+    // absolute element addresses: the grouped launch gets null base pointers
+    const int64_t a0 = (int64_t)(uintptr_t)work[i].pa.getElem() / 8;
+    const int64_t b0 = (int64_t)(uintptr_t)work[i].pb.getElem() / 8;
+    const int64_t c0 = (int64_t)(uintptr_t)work[i].tc.getElem() / 8;
+    for (auto g : work[i].sectors) {
+      g.a_off += a0;
+      g.b_off += b0;
+      g.c_off += c0;
+      all.push_back(g);
+    }
+  }
+  tn::run_sector_gemms(C(), g_mode, all, nullptr, nullptr, nullptr);
+  std::vector<UniTensor> out;
+  out.reserve(work.size());
+  for (auto& w : work) {
+    UniTensor::finish_contract(w);
+    out.push_back(std::move(w.tc));
+  }
+  return out;
+}
+
 // ---------------------------------------------------------------- binary I/O
 // UniTensor::save layout (UniTensor.cpp:922-986)
 void UniTensor::save(const std::string& fname) const {

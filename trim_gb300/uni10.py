@@ -195,6 +195,15 @@ def contract(a: UniTensor, b: UniTensor, fast: bool = False, mode="fp64") -> Uni
     return UniTensor(_h=h)
 
 
+def contract_batch(As, Bs, mode="fp64") -> list:
+    n = len(As)
+    a = (C.c_void_p * max(1, n))(*[t.h.value for t in As])
+    b = (C.c_void_p * max(1, n))(*[t.h.value for t in Bs])
+    out = (C.c_void_p * max(1, n))()
+    call("tn_contract_batch", n, a, b, _mode(mode), out)
+    return [UniTensor(_h=C.c_void_p(out[i])) for i in range(n)]
+
+
 def otimes(a: UniTensor, b: UniTensor, mode="fp64") -> UniTensor:
     h = C.c_void_p()
     call("tn_otimes", a.h, b.h, _mode(mode), C.byref(h))
