@@ -447,6 +447,70 @@ def mera_main(args, rank, local, world):
                           "speedup_vs_fp64": {m: res["fp64"]["ms"] / res[m]["ms"] for m in modes}}))
 
 
+def ipeps_device(tu, spec, rng_seed=None):
+    """Device tensors of the Z2 iPEPS CTM quadrant: the double-layer site
+    a.a* over p with each (x, x') pair combined, then C, T1, T2."""
+    rng = np.random.default_rng(spec["seed"] if rng_seed is None else rng_seed)
+    site, C_, T1, T2 = spec["tensors"]
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    a = tu.UniTensor(site.bonds, site.labels, els["a"])
+    ac = a.copy()
+    ac.set_label([0, 11, 12, 13, 14])
+    aa = tu.contract(a, ac, mode="fp64")
+    for x in (1, 2, 3, 4):
+        aa.combine_bond([x, x + 10])
+    aa.permute(aa.labels(), 2)
+    aa.set_label([10, 20, 30, 40])
+    dev = {"A2": aa}
+    for s in (C_, T1, T2):
+        dev[s.name] = tu.UniTensor(s.bonds, s.labels, els[s.name])
+    return dev, els
+
+
+def ipeps_main(args, rank, local, world):
+    """Z2-symmetric iPEPS double-layer CTM quadrant, chi = 128, D = 8:
+    C.T1.T2.A2 through Network::launch (ORDER (((C T1) T2) A2)) in FP64, split
+    and fast BF16; time, FP64-equivalent TFLOP/s and error vs FP64."""
+    import torch
+
+    torch.cuda.set_device(local)
+    from trim_gb300 import uni10 as tu
+
+    stream = torch.cuda.Stream()
+    tu.set_stream(stream.cuda_stream)
+    spec = wl.ipeps_ctm(chi=args.chi_ctm, D=args.D)
+    dev, _ = ipeps_device(tu, spec)
+    net = tu.Network(spec["net"])
+    for n, t in dev.items():
+        net.put_tensor(n, t)
+    res, ref = {}, None
+    for mode in ["fp64"] + [m for m in args.modes.split(",") if m != "fp64"]:
+        net.launch(mode)
+        tu.sync()
+        tu.prof_enable(True)
+        s_, e_ = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s_.record(stream)
+        q = net.launch(mode)
+        e_.record(stream)
+        torch.cuda.synchronize()
+        prof = tu.prof_read()
+        tu.prof_enable(False)
+        ms = s_.elapsed_time(e_)
+        v = q.get_elem()
+        if mode == "fp64":
+            ref = v
+        flops = sum(x["flops"] for k, x in prof.items() if "gemm" in k)
+        res[mode] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12, "flops": flops,
+                     "err_vs_fp64": float(np.linalg.norm(v - ref) / np.linalg.norm(ref)),
+                     "kernels": {k: {"ms": x["ms"], "launches": x["launches"]} for k, x in prof.items()}}
+    if rank == 0:
+        best = [m for m in res if m != "fp64"][0] if len(res) > 1 else "fp64"
+        print(json.dumps({"metric": "contract() TFLOP/s (FP64-equivalent), Z2 iPEPS CTM quadrant",
+                          "value": res[best]["tflops"], "unit": "TFLOP/s", "n_gpus": world, "higher_is_better": True,
+                          "config": {"workload": f"ipeps_ctm_z2_chi{args.chi_ctm}_D{args.D}", "elements_out": int(ref.size)},
+                          "modes": res, "speedup_vs_fp64": {m: res["fp64"]["ms"] / r["ms"] for m, r in res.items()}}))
+
+
 def batched_main(args, rank, local, world):
     """1024 independent uneven U(1) contractions T1[x|y,z].T2[y,z|w]: one
     grouped launch (all 8k sector GEMMs) against a per-contraction loop and a
@@ -541,7 +605,9 @@ def main():
     ap.add_argument("--mode", default="split", choices=["fp64", "split", "bf16"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="itebd", choices=["itebd", "permute", "mera", "batched"])
+    ap.add_argument("--workload", default="itebd", choices=["itebd", "permute", "mera", "batched", "ipeps"])
+    ap.add_argument("--chi-ctm", type=int, default=128)
+    ap.add_argument("--D", type=int, default=8)
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--modes", default="split,bf16")
     ap.add_argument("--chi", type=int, default=24)
@@ -561,6 +627,8 @@ def main():
         mera_main(args, rank, local, world)
     elif args.workload == "batched":
         batched_main(args, rank, local, world)
+    elif args.workload == "ipeps":
+        ipeps_main(args, rank, local, world)
     else:
         gpu_main(args, rank, local, world)
     if world > 1:
