@@ -142,6 +142,42 @@ int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* lis
 int tn_contract_sectors_fp64_noalloc(void* cuda_stream, int n, const tn_sector_gemm* list, const double* A,
                                      const double* B, double* C);
 
+/* ---- per-sector SVD and truncation -------------------------------------
+ * One sector of a batched SVD: A[M x N] (row-major, ld N) at a_off equals
+ * U[M x k] . diag(S[k]) . VT[k x N], k = min(M, N), all row-major at the
+ * given element offsets, singular values in descending order.  Replaces
+ * Block::svd (data-structure/lib/BlockReal.cpp:226-250), i.e. LAPACK dgesvd
+ * 'S','S' (numeric/lapack/lib/uni10_lapack_cpu.cpp:289-313), called per block. */
+typedef struct {
+  int64_t M, N;
+  int64_t a_off, u_off, s_off, vt_off;
+} tn_svd_sector;
+
+/* All n sector SVDs in FP64 on the GPU, in one batch (one-sided Jacobi, each
+ * sector on a thread-block cluster; sectors too large for it use cuSOLVER's
+ * gesvdj).  list is a host array; A, U, S, VT are device buffers.  sweeps
+ * (host, n entries, may be NULL) receives the Jacobi sweeps per sector (0 for
+ * the cuSOLVER fallback, -1 if a sector did not converge in 40 sweeps); it
+ * makes the call synchronous.  Columns of U (or rows of VT) that belong to an
+ * exactly zero singular value are returned as zero vectors. */
+int tn_svd_sectors(tn_ctx_t ctx, int n, const tn_svd_sector* list, const double* A, double* U, double* S,
+                   double* VT, int* sweeps);
+
+/* Cluster shape the SVD of an M x N sector would use (no GPU needed):
+ * cluster size P (0: the sector goes to the cuSOLVER fallback), columns per
+ * block b, record length L and shared memory per CTA. */
+int tn_svd_plan(int64_t M, int64_t N, int max_cluster, int* P, int* b, int* L, int64_t* smem_bytes);
+
+/* Global truncation of an iTEBD step (examples/iTEBD.cpp:153-161 with
+ * Matrix::resize, tensor-network/lib/MatrixReal.cpp:289-360, applied over all
+ * U(1) sectors): S holds n sectors of singular values (device, each sorted
+ * descending, cnt[i] values at s_off[i]).  The chi largest over all sectors
+ * are kept (ties: lower sector index, then lower position first), their
+ * 2-norm is written to *norm and they are multiplied by 1/norm in place.
+ * kept (host, n entries) receives the number kept per sector.  Synchronous. */
+int tn_truncate_sectors(tn_ctx_t ctx, int n, const int64_t* s_off, const int64_t* cnt, double* S, int64_t chi,
+                        int64_t* kept, double* norm);
+
 /* ---- tensor level (UniTensor, tensor-network/UniTensor.h) -------------- */
 /* UniTensor(const std::vector<Bond>&, const std::string& name) (UniTensor.h:326) */
 int tn_tensor_create(tn_ctx_t ctx, int nbonds, const int* btype, const int* nq, const int* qnum,
@@ -178,6 +214,14 @@ int tn_contract_batch(int n, const tn_tensor_t* a, const tn_tensor_t* b, int mod
 int tn_otimes(tn_tensor_t a, tn_tensor_t b, int mode, tn_tensor_t* out);
 /* multiply every element by a (operator*=(Real), UniTensor.h:262) */
 int tn_tensor_scale(tn_tensor_t t, double a);
+/* SVD of every block of t (row bonds | column bonds), truncated to the chi
+ * largest singular values over all blocks and normalised: the U(1) form of
+ * the iTEBD update (examples/iTEBD.cpp:153-171).  With a new bond n carrying
+ * charge q at the multiplicity kept in block q: u = [t's row bonds | n OUT],
+ * s = [n IN | n OUT] with diagonal blocks, vt = [n IN | t's column bonds].
+ * norm (may be NULL) receives the norm the kept values were divided by. */
+int tn_tensor_svd_truncate(tn_tensor_t t, int64_t chi, tn_tensor_t* u, tn_tensor_t* s, tn_tensor_t* vt,
+                           double* norm);
 
 /* ---- network (Network.h:67-233, lib/Network.cpp) ------------------------ */
 /* Network(const std::string& fname) -- text is the content of a .net file */

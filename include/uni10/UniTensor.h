@@ -6,6 +6,7 @@
 // save() match the reference element for element.
 #ifndef TRIM_UNI10_UNITENSOR_H
 #define TRIM_UNI10_UNITENSOR_H
+#include <cstdint>
 #include <map>
 #include <memory>
 #include <string>
@@ -86,13 +87,19 @@ class UniTensor {
   // contraction that leaves both operands untouched (permuted operands are
   // temporaries); Network::launch uses it so its leaves keep their buffers
   friend UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb);
-std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, const std::vector<const UniTensor*>& Bs);
   // Many independent contractions (operands untouched): every pair's sector
   // GEMMs run in one grouped launch.  No counterpart call in the reference,
   // which contracts pair by pair.
   friend std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As,
                                                const std::vector<const UniTensor*>& Bs);
   friend UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
+  // SVD of every block, truncated to the chi largest singular values over
+  // all blocks and normalised (the U(1) iTEBD update, examples/iTEBD.cpp:153-171,
+  // as one batched call; the reference user code loops over blocks).  With a
+  // new bond n carrying charge q at the multiplicity kept in block q:
+  // U = [row bonds | n], S = [n | n] (diagonal blocks), VT = [n | column bonds],
+  // labelled so that U . S . VT contracts back to theta.  Returns the norm.
+  friend double svdTruncate(const UniTensor& theta, int64_t chi, UniTensor& U, UniTensor& S, UniTensor& VT);
 
   UniTensor& operator*=(double a);
   friend UniTensor operator*(const UniTensor& Ta, double a);
@@ -132,6 +139,7 @@ UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast = false);
 UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb);
 std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, const std::vector<const UniTensor*>& Bs);
 UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb);
+double svdTruncate(const UniTensor& theta, int64_t chi, UniTensor& U, UniTensor& S, UniTensor& VT);
 UniTensor operator*(const UniTensor& Ta, double a);
 UniTensor operator*(double a, const UniTensor& Ta);
 UniTensor operator*(const UniTensor& Ta, const UniTensor& Tb);

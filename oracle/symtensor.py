@@ -18,6 +18,9 @@ It restates, in numpy, the algorithms of the reference (Uni10 v1.0.0) for:
   * Network fromfile/construct/launch/merge and the greedy planner
                                     (tensor-network/lib/Network.cpp:63-135, 271-506, 602-739)
   * Block::svd via LAPACK dgesvd     (numeric/lapack/lib/uni10_lapack_cpu.cpp:289-313)
+  * the iTEBD truncation + normalisation over U(1) sectors
+                                    (examples/iTEBD.cpp:153-171, Matrix::resize
+                                     tensor-network/lib/MatrixReal.cpp:289-360)
 
 Per-sector GEMMs call numpy's BLAS (``@``), as the reference calls dgemm_
 (uni10_lapack_cpu.cpp:41-44).  The bit-exact parts (sector map, permute) are
@@ -760,3 +763,49 @@ def block_svd(mat: np.ndarray):
 
     u, s, vt = scipy.linalg.svd(mat, full_matrices=False, lapack_driver="gesvd")
     return u, s, vt
+
+
+# --------------------------------------------------------------------------- truncation
+def truncate_global(svals, chi: int):
+    """Keep the chi largest singular values over all sectors and normalise.
+
+    The reference example keeps the leading chi of its single sector
+    (examples/iTEBD.cpp:156-159: ``rets[1].resize(dim, dim).norm()`` then
+    ``rets[1] *= (1 / norm)``); over U(1) sectors the leading chi are taken
+    from the values of all sectors together, ordered by value descending,
+    ties by lower sector index, then lower position.  Returns (kept counts,
+    norm, normalised kept values per sector)."""
+    entries = sorted((-float(v), q, i) for q, sv in enumerate(svals) for i, v in enumerate(sv))[: max(0, chi)]
+    kept = [0] * len(svals)
+    for _, q, _ in entries:
+        kept[q] += 1
+    allkept = np.concatenate([np.asarray(sv[:k], dtype=np.float64) for sv, k in zip(svals, kept)] or [np.zeros(0)])
+    norm = float(np.linalg.norm(allkept))
+    inv = 1.0 / norm if norm > 0 else float("inf")
+    return kept, norm, [np.asarray(sv[:k], dtype=np.float64) * inv for sv, k in zip(svals, kept)]
+
+
+def svd_truncate(theta: "UniTensor", chi: int):
+    """Block SVD of theta (row bonds | column bonds), truncated to the chi
+    largest singular values over all blocks and normalised: the U(1) form of
+    the iTEBD update (examples/iTEBD.cpp:153-171).  Returns U [row bonds | n],
+    S [n | n] (diagonal blocks), VT [n | column bonds] and the norm, where the
+    new bond n carries charge q at the multiplicity kept in block q and the
+    labels chain U . S . VT back to theta's labels."""
+    qs = theta.block_qnums()
+    svds = [block_svd(theta.get_block(q)) for q in qs]
+    kept, norm, snorm = truncate_global([sv[1] for sv in svds], chi)
+    ql = [q for q, k in zip(qs, kept) for _ in range(k)]
+    nin, nout = Bond(BD_IN, ql), Bond(BD_OUT, ql)
+    rb = theta.in_bond_num()
+    nl = max(theta.labels) + 1 if theta.labels else 0
+    U = UniTensor(theta.bonds[:rb] + [nout], labels=theta.labels[:rb] + [nl])
+    S = UniTensor([nin, nout], labels=[nl, nl + 1])
+    VT = UniTensor([nin] + theta.bonds[rb:], labels=[nl + 1] + theta.labels[rb:])
+    for q, (u, _, vt), k, sn in zip(qs, svds, kept, snorm):
+        if k == 0:
+            continue
+        U.put_block(q, u[:, :k])
+        S.put_block(q, np.diag(sn))
+        VT.put_block(q, vt[:k, :])
+    return U, S, VT, norm

@@ -34,6 +34,11 @@ class SectorGemm(C.Structure):
                 ("a_off", C.c_int64), ("b_off", C.c_int64), ("c_off", C.c_int64)]
 
 
+class SvdSector(C.Structure):
+    _fields_ = [("M", C.c_int64), ("N", C.c_int64), ("a_off", C.c_int64), ("u_off", C.c_int64),
+                ("s_off", C.c_int64), ("vt_off", C.c_int64)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _I64 = C.c_int64
@@ -59,6 +64,10 @@ _PROTOS = {
     "tn_plan_check_permute": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
     "tn_contract_sectors": (_I, [_P, _I, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
     "tn_contract_sectors_fp64_noalloc": (_I, [_P, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
+    "tn_svd_sectors": (_I, [_P, _I, C.POINTER(SvdSector), _DP, _DP, _DP, _DP, _IP]),
+    "tn_svd_plan": (_I, [_I64, _I64, _I, _IP, _IP, _IP, _I64P]),
+    "tn_truncate_sectors": (_I, [_P, _I, _I64P, _I64P, _DP, _I64, _I64P, C.POINTER(C.c_double)]),
+    "tn_tensor_svd_truncate": (_I, [_P, _I64, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_double)]),
     "tn_tensor_create": (_I, [_P, _I, _IP, _IP, _IP, _IP, C.POINTER(_P)]),
     "tn_tensor_destroy": (_I, [_P]),
     "tn_tensor_copy": (_I, [_P, C.POINTER(_P)]),

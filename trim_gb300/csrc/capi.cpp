@@ -100,10 +100,7 @@ int tn_ctx_destroy(tn_ctx_t ctx) {
   return guard([&] {
     if (!ctx) return;
     tn::Ctx* c = tn::as_ctx(ctx);
-    cudaStreamSynchronize(c->stream);
-    c->perm_cache.clear();
-    c->workspace.reset();
-    if (c->own_stream) cudaStreamDestroy(c->stream);
+    tn::release_ctx(c);
     delete c;
   });
 }
@@ -269,6 +266,54 @@ int tn_contract_sectors_fp64_noalloc(void* stream, int n, const tn_sector_gemm* 
   });
 }
 
+// ---------------------------------------------------------------- SVD
+int tn_svd_sectors(tn_ctx_t ctx, int n, const tn_svd_sector* list, const double* A, double* U, double* S, double* VT,
+                   int* sweeps) {
+  return guard([&] {
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative sector count");
+    if (n == 0) return;
+    need(list, "list");
+    tn::Ctx& c = *tn::as_ctx(ctx);
+    std::vector<tn_svd_sector> l(list, list + n);
+    if (!sweeps) {
+      tn::run_svd_sectors(c, l, A, U, S, VT, nullptr);
+      return;
+    }
+    tn::DevBuf info((size_t)n * sizeof(int), c);
+    tn::run_svd_sectors(c, l, A, U, S, VT, (int*)info.ptr);
+    TN_CUDA(cudaMemcpyAsync(sweeps, info.ptr, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    TN_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
+int tn_svd_plan(int64_t M, int64_t N, int max_cluster, int* P, int* b, int* L, int64_t* smem_bytes) {
+  return guard([&] {
+    if (max_cluster < 1 || max_cluster > 16 || (max_cluster & (max_cluster - 1)))
+      tn::fail(TN_ERR_ARG, "max_cluster must be a power of two in 1..16");
+    const tn::SvdGeom g = tn::svd_geometry(M, N, max_cluster);
+    if (P) *P = g.P;
+    if (b) *b = g.b;
+    if (L) *L = g.L;
+    if (smem_bytes) *smem_bytes = (int64_t)g.smem;
+  });
+}
+
+int tn_truncate_sectors(tn_ctx_t ctx, int n, const int64_t* s_off, const int64_t* cnt, double* S, int64_t chi,
+                        int64_t* kept, double* norm) {
+  return guard([&] {
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative sector count");
+    need(kept, "kept");
+    if (n > 0) {
+      need(s_off, "s_off");
+      need(cnt, "cnt");
+    }
+    std::vector<int64_t> o(s_off, s_off + n), k(cnt, cnt + n), out;
+    const double nrm = tn::run_truncate(*tn::as_ctx(ctx), o, k, S, chi, out);
+    std::copy(out.begin(), out.end(), kept);
+    if (norm) *norm = nrm;
+  });
+}
+
 // ---------------------------------------------------------------- tensors
 int tn_tensor_create(tn_ctx_t, int nbonds, const int* btype, const int* nq, const int* qnum, const int* deg,
                      tn_tensor_t* out) {
@@ -403,6 +448,22 @@ int tn_tensor_scale(tn_tensor_t t, double a) {
   return guard([&] {
     need(t, "tensor");
     t->t *= a;
+  });
+}
+
+int tn_tensor_svd_truncate(tn_tensor_t t, int64_t chi, tn_tensor_t* u, tn_tensor_t* s, tn_tensor_t* vt,
+                           double* norm) {
+  return guard([&] {
+    need(t, "tensor");
+    need(u, "u");
+    need(s, "s");
+    need(vt, "vt");
+    uni10::UniTensor U, S, VT;
+    const double nrm = uni10::svdTruncate(t->t, chi, U, S, VT);
+    *u = new tn_tensor_s{std::move(U)};
+    *s = new tn_tensor_s{std::move(S)};
+    *vt = new tn_tensor_s{std::move(VT)};
+    if (norm) *norm = nrm;
   });
 }
 

@@ -250,6 +250,49 @@ void Ctx::check_device_error() {
   }
 }
 
+cudaStream_t Ctx::side_stream(int i) {
+  if (i == 0) return stream;
+  while ((int)side.size() < i) {
+    cudaStream_t s;
+    cudaEvent_t e;
+    TN_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    TN_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    side.push_back(s);
+    side_ev.push_back(e);
+  }
+  return side[i - 1];
+}
+
+void Ctx::fork(int n) {
+  if (n <= 1) return;
+  if (!fork_ev) TN_CUDA(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+  TN_CUDA(cudaEventRecord(fork_ev, stream));
+  for (int i = 1; i < n; i++) TN_CUDA(cudaStreamWaitEvent(side_stream(i), fork_ev, 0));
+}
+
+void Ctx::join(int n) {
+  for (int i = 1; i < n; i++) {
+    TN_CUDA(cudaEventRecord(side_ev[i - 1], side[i - 1]));
+    TN_CUDA(cudaStreamWaitEvent(stream, side_ev[i - 1], 0));
+  }
+}
+
+void release_ctx(Ctx* c) {
+  cudaStreamSynchronize(c->stream);
+  for (auto s : c->side) cudaStreamSynchronize(s);
+  c->perm_cache.clear();
+  c->gemm_cache.clear();
+  c->tc_cache.clear();
+  c->svd_cache.clear();
+  c->workspace.reset();
+  c->err_word.reset();
+  release_solver(c);
+  for (auto s : c->side) cudaStreamDestroy(s);
+  for (auto e : c->side_ev) cudaEventDestroy(e);
+  if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+}
+
 static std::mutex g_ctx_mu;
 static std::map<int, Ctx*> g_default;
 

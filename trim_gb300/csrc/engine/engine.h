@@ -156,6 +156,25 @@ struct TcSector {
   int32_t nmt, nnt, nkt;        // 128-row, 64-column and 64-k tile counts
 };
 
+// One sector of the cluster Jacobi SVD: A (M x N, row-major) at a_off,
+// U (M x k) at u_off, S (k) at s_off, VT (k x N) at vt_off, k = min(M, N);
+// b columns per block (2P blocks per sector), record length L (even).
+struct SvdJob {
+  int64_t a_off, u_off, s_off, vt_off;
+  int32_t M, N, b, L;
+  int32_t id;  // index of the sector in the caller's list (sweep counts)
+};
+constexpr int kSvdMaxSweeps = 40;
+constexpr int kSvdMaxSmem = 227 * 1024;
+
+// One sector of a truncation gather: the first `kept` singular triplets of a
+// sector's full factors (U M x k, S k, VT k x N) copied to compact blocks.
+struct TruncSector {
+  int64_t M, N, k, kept;
+  int64_t u_off, s_off, vt_off;     // full factors
+  int64_t uo_off, so_off, vo_off;   // compact outputs (S as a kept x kept block)
+};
+
 // ---------------------------------------------------------------- context
 // Per-kernel timing with CUDA events on the context's stream (enabled on
 // demand; used by bench.py for the roofline of the dominant kernel).
@@ -191,8 +210,20 @@ struct Ctx {
   int* device_error_word();
   void check_device_error();  // syncs the stream; throws TN_ERR_TIMEOUT if a wait gave up
   void launched(int n = 1) { launches += n; }
+  // side streams for launches that run next to each other (fork/join with
+  // events on `stream`, so the pattern is also legal under graph capture)
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> side_ev;
+  cudaEvent_t fork_ev = nullptr;
+  cudaStream_t side_stream(int i);  // i >= 1; index 0 is `stream` itself
+  void fork(int n);                 // side streams 1..n-1 wait for `stream`
+  void join(int n);                 // `stream` waits for side streams 1..n-1
+  void* solver = nullptr;           // cuSOLVER handle (lazily created)
+  std::unordered_map<uint64_t, std::shared_ptr<void>> svd_cache;  // SVD batch plans
 };
 Ctx* default_ctx();  // lazily created context on the current device
+void release_ctx(Ctx* c);     // syncs and frees everything a context holds (not the Ctx)
+void release_solver(Ctx* c);  // destroys the cuSOLVER handle, if any
 Ctx* as_ctx(tn_ctx_t c);
 
 // ---------------------------------------------------------------- operations
@@ -234,5 +265,30 @@ void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems,
                     const unsigned long long* ea, const unsigned long long* eb, double* C, int* err, int grid,
                     cudaStream_t s);
 void launch_scale(double* p, int64_t n, double a, cudaStream_t s);
+
+// SVD (Block::svd per sector) and truncation
+struct SvdGeom {
+  int P = 0, b = 0, L = 0;  // P == 0: too large for the cluster kernel
+  size_t smem = 0;
+};
+SvdGeom svd_geometry(int64_t M, int64_t N, int max_cluster);
+size_t svd_smem_bytes(int P, int b, int L);
+int svd_max_cluster();  // largest cluster size the device schedules (<= 16)
+void launch_svd_jacobi(const SvdJob* jobs, int njobs, int P, size_t smem, const double* A, double* U, double* S,
+                       double* VT, int* info, cudaStream_t s);
+void launch_truncate(const int64_t* s_off, const int64_t* s_cnt, int nsec, double* S, int64_t chi, int64_t* kept,
+                     double* norm, cudaStream_t s);
+void launch_gather_truncated(const TruncSector* secs, int nsec, const double* U, const double* S, const double* VT,
+                             double* Uo, double* So, double* VTo, cudaStream_t s);
+void launch_transpose(const double* src, double* dst, int rows, int cols, cudaStream_t s);
+// all sectors of `list` in one batch; info (device, optional) receives the
+// sweeps each sector took (-1: no convergence within kSvdMaxSweeps; 0 for a
+// sector solved by the cuSOLVER fallback)
+void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const double* A, double* U, double* S,
+                     double* VT, int* info);
+// global truncation to chi over sectors with sorted singular values; fills
+// kept (host, one count per sector) and returns the norm of the kept values
+double run_truncate(Ctx& ctx, const std::vector<int64_t>& s_off, const std::vector<int64_t>& s_cnt, double* S,
+                    int64_t chi, std::vector<int64_t>& kept);
 
 }  // namespace tn

@@ -1,8 +1,6 @@
 // uni10::Block / uni10::Matrix on device memory: the views contract() and the
 // SVD truncation of an iTEBD step use (data-structure/lib/Block.cpp,
 // BlockReal.cpp:226-250; tensor-network/lib/MatrixReal.cpp:289-360).
-#include <cusolverDn.h>
-
 #include <cmath>
 #include <sstream>
 #include <stdexcept>
@@ -144,71 +142,19 @@ Matrix operator*(const Block& a, const Block& b) {
 }
 
 // ---------------------------------------------------------------- SVD
-namespace {
-struct Solver {
-  cusolverDnHandle_t h = nullptr;
-  gesvdjInfo_t info = nullptr;
-  Solver() {
-    if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS) tn::fail(TN_ERR_CUDA, "cusolverDnCreate failed");
-    if (cusolverDnCreateGesvdjInfo(&info) != CUSOLVER_STATUS_SUCCESS) tn::fail(TN_ERR_CUDA, "gesvdj info failed");
-  }
-};
-Solver& solver() {
-  static thread_local Solver s;
-  cusolverDnSetStream(s.h, C().stream);
-  return s;
-}
-
-__global__ void transpose_kernel(const double* __restrict__ src, double* __restrict__ dst, int rows, int cols) {
-  // src row-major rows x cols -> dst row-major cols x rows
-  __shared__ double t[32][33];
-  int bx = blockIdx.x * 32, by = blockIdx.y * 32;
-  for (int j = threadIdx.y; j < 32; j += 8) {
-    int r = by + j, c = bx + threadIdx.x;
-    if (r < rows && c < cols) t[j][threadIdx.x] = src[(int64_t)r * cols + c];
-  }
-  __syncthreads();
-  for (int j = threadIdx.y; j < 32; j += 8) {
-    int c = bx + j, r = by + threadIdx.x;
-    if (r < rows && c < cols) dst[(int64_t)c * rows + r] = t[threadIdx.x][j];
-  }
-}
-
-void transpose(const double* src, double* dst, int rows, int cols) {
-  dim3 grid((cols + 31) / 32, (rows + 31) / 32), block(32, 8);
-  transpose_kernel<<<grid, block, 0, C().stream>>>(src, dst, rows, cols);
-  TN_CUDA(cudaGetLastError());
-  C().launched();
-}
-}  // namespace
-
 // Block::svd: A (M x N, row-major) = U (M x k) . S (k, diagonal) . VT (k x N),
-// k = min(M, N), singular values descending.  The row-major A is the
-// column-major A^T (N x M); its Jacobi SVD A^T = U' S V'^T gives VT = U'^T
-// (already row-major in U''s column-major buffer) and U = V' (transposed).
+// k = min(M, N), singular values descending (one-sided Jacobi on a cluster of
+// CTAs; cuSOLVER gesvdj for blocks too large for shared memory).
 std::vector<Matrix> Block::svd() const {
   if (diag) throw std::runtime_error("svd of a diagonal matrix is not supported");
-  const int M = (int)Rnum, N = (int)Cnum, k = std::min(M, N);
-  Matrix work(Rnum, Cnum, m_elem, false, true);
-  Matrix U(Rnum, k), S(k, k, true), VT(k, Cnum), V(Rnum, k);
-  Solver& s = solver();
-  int lwork = 0;
-  if (cusolverDnDgesvdj_bufferSize(s.h, CUSOLVER_EIG_MODE_VECTOR, 1, N, M, work.getElem(), N, S.getElem(),
-                                   VT.getElem(), N, V.getElem(), M, &lwork, s.info) != CUSOLVER_STATUS_SUCCESS)
-    tn::fail(TN_ERR_CUDA, "gesvdj buffer size failed");
-  tn::Ctx& c = C();
-  tn::DevBuf wk((size_t)lwork * sizeof(double) + sizeof(int), c);
-  int* dinfo = (int*)((double*)wk.ptr + lwork);
-  if (cusolverDnDgesvdj(s.h, CUSOLVER_EIG_MODE_VECTOR, 1, N, M, work.getElem(), N, S.getElem(), VT.getElem(), N,
-                        V.getElem(), M, (double*)wk.ptr, lwork, dinfo, s.info) != CUSOLVER_STATUS_SUCCESS)
-    tn::fail(TN_ERR_CUDA, "gesvdj failed");
-  c.launched();
-  // V' is column-major M x k == row-major k x M; U = its transpose (M x k)
-  transpose(V.getElem(), U.getElem(), k, M);
-  int hinfo = 0;
-  TN_CUDA(cudaMemcpyAsync(&hinfo, dinfo, sizeof(int), cudaMemcpyDeviceToHost, c.stream));
-  TN_CUDA(cudaStreamSynchronize(c.stream));
-  if (hinfo < 0) tn::fail(TN_ERR_CUDA, "gesvdj: invalid parameter");
+  const size_t k = std::min(Rnum, Cnum);
+  Matrix U(Rnum, k), S(k, k, true), VT(k, Cnum);
+  if (k) {
+    // the three factors are separate allocations: offsets relative to each base
+    std::vector<tn_svd_sector> list(1);
+    list[0] = tn_svd_sector{(int64_t)Rnum, (int64_t)Cnum, 0, 0, 0, 0};
+    tn::run_svd_sectors(C(), list, m_elem, U.getElem(), S.getElem(), VT.getElem(), nullptr);
+  }
   std::vector<Matrix> out;
   out.push_back(U);
   out.push_back(S);

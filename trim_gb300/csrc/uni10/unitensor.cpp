@@ -750,6 +750,92 @@ std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, c
   return out;
 }
 
+// ---------------------------------------------------------------- SVD + truncation
+// The U(1) form of the iTEBD update (examples/iTEBD.cpp:153-171): Block::svd of
+// every block (BlockReal.cpp:226-250), the chi largest singular values over
+// all blocks kept (Matrix::resize, MatrixReal.cpp:289-360) and divided by
+// their norm (iTEBD.cpp:158-159).  All blocks go through one batched SVD
+// launch, one truncation kernel and one gather kernel; the only host round
+// trip is the kept count per block, which fixes the new bond.
+double svdTruncate(const UniTensor& theta, int64_t chi, UniTensor& U, UniTensor& S, UniTensor& VT) {
+  if (!(theta.status & UniTensor::HAVEBOND)) throw std::runtime_error("svdTruncate: the tensor has no bonds");
+  if (!(theta.status & UniTensor::HAVEELEM)) throw std::runtime_error("svdTruncate: the tensor has no elements");
+  if (chi <= 0) throw std::runtime_error("svdTruncate: chi must be positive");
+  const tn::SectorMap& m = *theta.smap;
+  tn::Ctx& c = C();
+  std::vector<tn_svd_sector> list;
+  std::vector<int64_t> s_off, s_cnt;
+  int64_t nu = 0, ns = 0, nv = 0;
+  for (const auto& b : m.blocks) {
+    const int64_t k = std::min(b.rows, b.cols);
+    list.push_back(tn_svd_sector{b.rows, b.cols, b.off, nu, ns, nv});
+    s_off.push_back(ns);
+    s_cnt.push_back(k);
+    nu += b.rows * k;
+    ns += k;
+    nv += k * b.cols;
+  }
+  DevBuf uf((size_t)nu * sizeof(double), c), sf((size_t)ns * sizeof(double), c), vf((size_t)nv * sizeof(double), c);
+  tn::run_svd_sectors(c, list, dptr(theta.elem), (double*)uf.ptr, (double*)sf.ptr, (double*)vf.ptr, nullptr);
+  std::vector<int64_t> kept;
+  const double norm = tn::run_truncate(c, s_off, s_cnt, (double*)sf.ptr, chi, kept);
+  std::vector<Qnum> qs;
+  for (size_t i = 0; i < m.blocks.size(); i++)
+    for (int64_t j = 0; j < kept[i]; j++) qs.push_back(to_qnum(m.blocks[i].q));
+  if (qs.empty()) throw std::runtime_error("svdTruncate: no singular value kept");
+  const Bond nin(BD_IN, qs), nout(BD_OUT, qs);
+  const int rb = theta.RBondNum;
+  std::vector<Bond> ub(theta.bonds.begin(), theta.bonds.begin() + rb), vb{nin};
+  ub.push_back(nout);
+  vb.insert(vb.end(), theta.bonds.begin() + rb, theta.bonds.end());
+  U = UniTensor(ub, "U", UniTensor::NoFill{});
+  S = UniTensor(std::vector<Bond>{nin, nout}, "S", UniTensor::NoFill{});
+  VT = UniTensor(vb, "VT", UniTensor::NoFill{});
+  // labels: U = (theta's row labels, n), S = (n, n+1), VT = (n+1, theta's column labels)
+  int nl = 0;
+  for (int l : theta.labels) nl = std::max(nl, l + 1);
+  std::vector<int> ul(theta.labels.begin(), theta.labels.begin() + rb), vl{nl + 1};
+  ul.push_back(nl);
+  vl.insert(vl.end(), theta.labels.begin() + rb, theta.labels.end());
+  U.setLabel(ul);
+  S.setLabel(std::vector<int>{nl, nl + 1});
+  VT.setLabel(vl);
+  std::vector<tn::TruncSector> g;
+  for (size_t i = 0; i < m.blocks.size(); i++) {
+    if (!kept[i]) continue;
+    const auto& b = m.blocks[i];
+    const int iu = U.smap->find_block(b.q), is = S.smap->find_block(b.q), iv = VT.smap->find_block(b.q);
+    if (iu < 0 || is < 0 || iv < 0) throw std::runtime_error("svdTruncate: block layout mismatch");
+    tn::TruncSector t;
+    t.M = b.rows;
+    t.N = b.cols;
+    t.k = std::min(b.rows, b.cols);
+    t.kept = kept[i];
+    t.u_off = list[i].u_off;
+    t.s_off = list[i].s_off;
+    t.vt_off = list[i].vt_off;
+    t.uo_off = U.smap->blocks[iu].off;
+    t.so_off = S.smap->blocks[is].off;
+    t.vo_off = VT.smap->blocks[iv].off;
+    g.push_back(t);
+  }
+  DevBuf gd(g.size() * sizeof(tn::TruncSector), c);
+  TN_CUDA(cudaMemcpyAsync(gd.ptr, g.data(), g.size() * sizeof(tn::TruncSector), cudaMemcpyHostToDevice, c.stream));
+  {
+    tn::ProfScope ps(c, "gather_truncated");
+    tn::launch_gather_truncated((const tn::TruncSector*)gd.ptr, (int)g.size(), (const double*)uf.ptr,
+                                (const double*)sf.ptr, (const double*)vf.ptr, dptr(U.elem), dptr(S.elem),
+                                dptr(VT.elem), c.stream);
+    c.launched();
+  }
+  U.status |= UniTensor::HAVEELEM;
+  S.status |= UniTensor::HAVEELEM;
+  VT.status |= UniTensor::HAVEELEM;
+  // the host list must outlive the copy above
+  TN_CUDA(cudaStreamSynchronize(c.stream));
+  return norm;
+}
+
 // ---------------------------------------------------------------- binary I/O
 // UniTensor::save layout (UniTensor.cpp:922-986)
 void UniTensor::save(const std::string& fname) const {

@@ -60,6 +60,35 @@ def contract_sectors(mode, gemms, a_ptr: int, b_ptr: int, c_ptr: int) -> None:
     call("tn_contract_sectors", None, _mode(mode), len(gemms), arr, a_ptr, b_ptr, c_ptr)
 
 
+def svd_sectors(sectors, a_ptr: int, u_ptr: int, s_ptr: int, vt_ptr: int, sweeps: bool = False):
+    """Batched per-sector SVD; sectors are (M, N, a_off, u_off, s_off, vt_off)
+    tuples, the pointers device addresses.  With sweeps=True returns the
+    Jacobi sweep count of every sector (synchronous)."""
+    n = len(sectors)
+    arr = (capi.SvdSector * max(1, n))(*[capi.SvdSector(*t) for t in sectors])
+    sw = (C.c_int * max(1, n))() if sweeps else None
+    call("tn_svd_sectors", None, n, arr, a_ptr, u_ptr, s_ptr, vt_ptr, sw)
+    return list(sw)[:n] if sweeps else None
+
+
+def svd_plan(M: int, N: int, max_cluster: int = 16) -> dict:
+    P, b, L, sm = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
+    call("tn_svd_plan", int(M), int(N), int(max_cluster), C.byref(P), C.byref(b), C.byref(L), C.byref(sm))
+    return {"P": P.value, "b": b.value, "L": L.value, "smem": sm.value}
+
+
+def truncate_sectors(s_off, counts, s_ptr: int, chi: int):
+    """Global truncation of sorted per-sector singular values (device, in
+    place); returns (kept per sector, norm)."""
+    n = len(s_off)
+    o = (C.c_int64 * max(1, n))(*s_off)
+    k = (C.c_int64 * max(1, n))(*counts)
+    kept = (C.c_int64 * max(1, n))()
+    norm = C.c_double()
+    call("tn_truncate_sectors", None, n, o, k, s_ptr, int(chi), kept, C.byref(norm))
+    return list(kept)[:n], norm.value
+
+
 def sync() -> None:
     call("tn_ctx_sync", None)
 
@@ -187,6 +216,14 @@ class UniTensor:
     def scale(self, a: float) -> "UniTensor":
         call("tn_tensor_scale", self.h, C.c_double(a))
         return self
+
+    def svd_truncate(self, chi: int):
+        """Block SVDs truncated to the chi largest singular values over all
+        blocks and normalised; returns (U, S, VT, norm) (the U(1) iTEBD update)."""
+        u, sv, vt = C.c_void_p(), C.c_void_p(), C.c_void_p()
+        norm = C.c_double()
+        call("tn_tensor_svd_truncate", self.h, int(chi), C.byref(u), C.byref(sv), C.byref(vt), C.byref(norm))
+        return UniTensor(_h=u), UniTensor(_h=sv), UniTensor(_h=vt), norm.value
 
 
 def contract(a: UniTensor, b: UniTensor, fast: bool = False, mode="fp64") -> UniTensor:
