@@ -96,7 +96,7 @@ def _tournament(P, b, nx):
 
 
 @pytest.mark.parametrize("P,b", [(1, 1), (1, 2), (1, 3), (1, 8), (2, 5), (2, 6), (4, 5), (4, 8), (8, 7),
-                                 (8, 8), (16, 5), (16, 9)])
+                                 (8, 8), (16, 5), (16, 9), (4, 17), (8, 19), (2, 24), (1, 23)])
 def test_tournament_visits_every_pair_once(P, b):
     nx = 2 * P * b
     seen = {}

@@ -156,16 +156,44 @@ struct TcSector {
   int32_t nmt, nnt, nkt;        // 128-row, 64-column and 64-k tile counts
 };
 
-// One sector of the cluster Jacobi SVD: A (M x N, row-major) at a_off,
-// U (M x k) at u_off, S (k) at s_off, VT (k x N) at vt_off, k = min(M, N);
-// b columns per block (2P blocks per sector), record length L (even).
+// One sector of the cluster Jacobi SVD (M x N, row-major).  Stage 1 (FP32):
+// the sector at a_off of the input, rotation product V (nx x nx) and V^T out
+// at v_off.  Stage 2 (FP64): X1 (M x N) at a_off, Q^T at v_off in; U (M x k)
+// at u_off, S (k) at s_off, VT (k x N) at vt_off out, k = min(M, N).  b
+// columns per block (2P blocks per sector), record length L (multiple of 4).
 struct SvdJob {
-  int64_t a_off, u_off, s_off, vt_off;
+  int64_t a_off, v_off, u_off, s_off, vt_off;
   int32_t M, N, b, L;
   int32_t id;  // index of the sector in the caller's list (sweep counts)
 };
-constexpr int kSvdMaxSweeps = 40;
+constexpr int kSvdMaxSweeps = 40;    // FP64 stage
+constexpr int kSvdMaxSweeps32 = 20;  // FP32 stage
+constexpr int kSvdMaxPairs = 40;     // pairs of one sub-round (b + 1 at most)
 constexpr int kSvdMaxSmem = 227 * 1024;
+
+// Shared-memory layout of one CTA of the Jacobi kernel (byte offsets);
+// es = 4 (FP32 stage) or 8 (FP64 stage).
+struct SvdSmem {
+  size_t sig, all, red, rec, nrm, pd, ph, ps, pf, cnt, misc, total;
+};
+__host__ __device__ inline SvdSmem svd_smem(int P, int b, int L, int es) {
+  SvdSmem m;
+  const size_t nbuf = P > 1 ? 2 : 1;
+  const size_t nsig = (size_t)2 * P * b;
+  m.sig = 0;
+  m.all = m.sig + 8 * nsig;
+  m.red = m.all + 8 * nsig;
+  m.rec = (m.red + 8 * 32 + 15) & ~(size_t)15;
+  m.nrm = m.rec + (size_t)es * nbuf * 2 * b * L;
+  m.pd = m.nrm + (size_t)es * nbuf * 2 * b;
+  m.ph = m.pd + (size_t)es * kSvdMaxPairs;
+  m.ps = m.ph + (size_t)es * kSvdMaxPairs;
+  m.pf = (m.ps + (size_t)es * kSvdMaxPairs + 7) & ~(size_t)7;
+  m.cnt = m.pf + 4 * kSvdMaxPairs;
+  m.misc = m.cnt + 4 * 32;
+  m.total = m.misc + 4 * 4;
+  return m;
+}
 
 // One sector of a truncation gather: the first `kept` singular triplets of a
 // sector's full factors (U M x k, S k, VT k x N) copied to compact blocks.
@@ -269,13 +297,20 @@ void launch_scale(double* p, int64_t n, double a, cudaStream_t s);
 // SVD (Block::svd per sector) and truncation
 struct SvdGeom {
   int P = 0, b = 0, L = 0;  // P == 0: too large for the cluster kernel
+  int threads = 0;          // one warp per column pair of a sub-round, 8..24 warps
   size_t smem = 0;
 };
+// cluster size P, columns per block b, record length L, threads per CTA and
+// shared memory of the FP64 stage (svd_geometry) and the FP32 stage
 SvdGeom svd_geometry(int64_t M, int64_t N, int max_cluster);
-size_t svd_smem_bytes(int P, int b, int L);
+SvdGeom svd_geometry32(int64_t M, int64_t N, int max_cluster);
 int svd_max_cluster();  // largest cluster size the device schedules (<= 16)
-void launch_svd_jacobi(const SvdJob* jobs, int njobs, int P, size_t smem, const double* A, double* U, double* S,
-                       double* VT, int* info, cudaStream_t s);
+// stage 1: FP32 sweeps from the identity, V and V^T out to Vout; stage 2:
+// FP64 sweeps from X1 and Q^T (in X and Vin), U, S, VT out
+void launch_svd_jacobi(int stage, const SvdJob* jobs, int njobs, int P, int threads, size_t smem, const double* X,
+                       const double* Vin, double* Vout, double* U, double* S, double* VT, int* info, cudaStream_t s);
+// T = 3/2 I - (G + G^T)/4 for every (n, g_off, t_off) triple of tab (device)
+void launch_ns_factor(const int64_t* tab, int njobs, double* ws, cudaStream_t s);
 void launch_truncate(const int64_t* s_off, const int64_t* s_cnt, int nsec, double* S, int64_t chi, int64_t* kept,
                      double* norm, cudaStream_t s);
 void launch_gather_truncated(const TruncSector* secs, int nsec, const double* U, const double* S, const double* VT,

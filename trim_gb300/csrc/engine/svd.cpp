@@ -13,26 +13,64 @@
 
 namespace tn {
 
-// Smallest power-of-two cluster whose blocks hold at most one column pair per
-// warp (b <= 8) within shared memory; larger sectors take P = max_cluster with
-// wider blocks while they fit.  P = 0: the sector does not fit at all.
+// Threads of a CTA: one warp per column pair of a sub-round (b + 1 pairs at
+// most), between 8 and 24 warps; the FP64 stage runs 8 warps.
+static int svd_threads(int b, bool fp64) {
+  if (fp64) return 256;
+  return 32 * std::max(8, std::min(24, b + (b & 1)));
+}
+
+// FP64 stage: the smallest power-of-two cluster whose blocks hold at most
+// bmax columns (8, or 4 from nx = 96 on, where the stage is bound by the FP64
+// rate of the cluster's SMs) within shared memory; larger sectors take
+// P = max_cluster with wider blocks while they fit.  P = 0: the sector does
+// not fit at all (cuSOLVER fallback).
 SvdGeom svd_geometry(int64_t M, int64_t N, int max_cluster) {
   SvdGeom g;
   const int64_t mx = std::max(M, N), nx = std::min(M, N);
   if (nx <= 0 || mx > INT_MAX / 4) return g;
-  const int L = (int)((mx + nx + 1) & ~int64_t(1));
+  const int L = (int)((mx + nx + 3) & ~int64_t(3));
+  const int64_t bmax = nx >= 96 ? 4 : 8;
   for (int P = 1; P <= max_cluster; P *= 2) {
     const int64_t b = (nx + 2 * P - 1) / (2 * P);
     const bool last = 2 * P > max_cluster;
-    if (b > 8 && !last) continue;
-    const size_t smem = svd_smem_bytes(P, (int)b, L);
-    if (smem > (size_t)kSvdMaxSmem) {
+    if (b > bmax && !last) continue;
+    const size_t smem = svd_smem(P, (int)std::min<int64_t>(b, INT_MAX), L, 8).total;
+    if (b + 1 > kSvdMaxPairs || smem > (size_t)kSvdMaxSmem) {
       if (last) return g;
       continue;
     }
     g.P = P;
     g.b = (int)b;
     g.L = L;
+    g.threads = svd_threads(g.b, true);
+    g.smem = smem;
+    return g;
+  }
+  return g;
+}
+
+// FP32 stage: the smallest power-of-two cluster with b <= 24 (one warp per
+// pair, 24 warps at most), which keeps the block exchanges (2P - 1 per
+// sweep) few; wider blocks when the cluster size is capped.
+SvdGeom svd_geometry32(int64_t M, int64_t N, int max_cluster) {
+  SvdGeom g;
+  const int64_t mx = std::max(M, N), nx = std::min(M, N);
+  if (nx <= 0 || mx > INT_MAX / 4) return g;
+  const int L = (int)((mx + nx + 3) & ~int64_t(3));
+  for (int P = 1; P <= max_cluster; P *= 2) {
+    const int64_t b = (nx + 2 * P - 1) / (2 * P);
+    const bool last = 2 * P > max_cluster;
+    if (b > 23 && !last) continue;
+    const size_t smem = svd_smem(P, (int)std::min<int64_t>(b, INT_MAX), L, 4).total;
+    if (b + 1 > kSvdMaxPairs || smem > (size_t)kSvdMaxSmem) {
+      if (last) return g;
+      continue;
+    }
+    g.P = P;
+    g.b = (int)b;
+    g.L = L;
+    g.threads = svd_threads(g.b, false);
     g.smem = smem;
     return g;
   }
@@ -44,16 +82,31 @@ namespace {
 struct SvdClass {
   int P = 0;
   int njobs = 0;
-  int64_t first = 0;  // index of the first job of this class in the job buffer
+  int64_t first = 0;  // index of the first job of this class in its job buffer
+  int threads = 256;
   size_t smem = 0;
+};
+
+// Workspace of one Jacobi sector (doubles): V | V^T, Q | Q^T (Newton-Schulz
+// ping-pong), G, T, X1.
+struct SvdWs {
+  int64_t v, q, g, t, x1;
 };
 
 struct SvdPlan {
   std::vector<tn_svd_sector> list;
-  DevBufP jobs;
-  std::vector<SvdClass> classes;  // largest cluster first
-  std::vector<int> fallback;      // sectors for cuSOLVER
-  std::vector<int> empty;         // sectors with M or N == 0
+  DevBufP jobs1, jobs2;  // stage 1 / stage 2 job lists, grouped by class
+  DevBufP ns_tab;        // (n, g_off, t_off) per Jacobi sector
+  std::vector<SvdClass> classes1, classes2;  // per stage, largest cluster first
+  std::vector<tn_svd_sector> jac;  // the Jacobi sectors
+  std::vector<SvdWs> ws;
+  int64_t ws_elems = 0;
+  // grouped FP64 GEMMs of the orthogonalisation, all in workspace offsets
+  std::vector<tn_sector_gemm> gram1, prod1, gram2, prod2;
+  std::vector<tn_sector_gemm> x1_direct;  // X1 = A Q   (A operand in the input)
+  std::vector<tn_sector_gemm> x1_trans;   // X1^T = Q^T A (B operand in the input)
+  std::vector<int> fallback;  // sectors for cuSOLVER
+  std::vector<int> empty;     // sectors with M or N == 0
 };
 
 uint64_t hash_svd(const std::vector<tn_svd_sector>& list, int maxp) {
@@ -61,6 +114,12 @@ uint64_t hash_svd(const std::vector<tn_svd_sector>& list, int maxp) {
   const unsigned char* p = reinterpret_cast<const unsigned char*>(list.data());
   for (size_t i = 0; i < list.size() * sizeof(tn_svd_sector); i++) h = (h ^ p[i]) * 1099511628211ull;
   return h;
+}
+
+DevBufP upload(Ctx& ctx, const void* p, size_t bytes) {
+  auto b = std::make_shared<DevBuf>(bytes, ctx);
+  if (bytes) TN_CUDA(cudaMemcpyAsync(b->ptr, p, bytes, cudaMemcpyHostToDevice, ctx.stream));
+  return b;
 }
 
 std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>& list) {
@@ -75,8 +134,10 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
   }
   auto plan = std::make_shared<SvdPlan>();
   plan->list = list;
-  std::vector<SvdJob> byP[5];
-  size_t smemP[5] = {0, 0, 0, 0, 0};
+  std::vector<SvdJob> byP1[5], byP2[5];
+  size_t smem1[5] = {0, 0, 0, 0, 0}, smem2[5] = {0, 0, 0, 0, 0};
+  int thr1[5] = {256, 256, 256, 256, 256}, thr2[5] = {256, 256, 256, 256, 256};
+  std::vector<int64_t> tab;
   for (size_t i = 0; i < list.size(); i++) {
     const tn_svd_sector& s = list[i];
     if (s.M < 0 || s.N < 0) fail(TN_ERR_ARG, "svd: negative sector dimension");
@@ -86,40 +147,83 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     }
     if (s.M > INT_MAX || s.N > INT_MAX) fail(TN_ERR_ARG, "svd: sector dimension too large");
     const SvdGeom g = svd_geometry(s.M, s.N, maxp);
-    if (!g.P) {
+    const SvdGeom g1 = svd_geometry32(s.M, s.N, maxp);
+    if (!g.P || !g1.P) {
       plan->fallback.push_back((int)i);
       continue;
     }
-    int c = 0;
-    while ((1 << c) < g.P) c++;
-    SvdJob j;
-    j.a_off = s.a_off;
-    j.u_off = s.u_off;
-    j.s_off = s.s_off;
-    j.vt_off = s.vt_off;
-    j.M = (int)s.M;
-    j.N = (int)s.N;
-    j.b = g.b;
-    j.L = g.L;
-    j.id = (int)i;
-    byP[c].push_back(j);
-    smemP[c] = std::max(smemP[c], g.smem);
+    const int64_t n = std::min(s.M, s.N);
+    SvdWs w;
+    w.v = plan->ws_elems;
+    w.q = w.v + 2 * n * n;
+    w.g = w.q + 2 * n * n;
+    w.t = w.g + n * n;
+    w.x1 = w.t + n * n;
+    plan->ws_elems = w.x1 + s.M * s.N;
+    plan->ws.push_back(w);
+    plan->jac.push_back(s);
+    // Newton-Schulz: G = V^T V, T = 3/2 I - (G + G^T)/4, Q = V T, Q^T = T V^T;
+    // then the same from Q back into V
+    plan->gram1.push_back(tn_sector_gemm{n, n, n, w.v + n * n, w.v, w.g});
+    plan->prod1.push_back(tn_sector_gemm{n, n, n, w.v, w.t, w.q});
+    plan->prod1.push_back(tn_sector_gemm{n, n, n, w.t, w.v + n * n, w.q + n * n});
+    plan->gram2.push_back(tn_sector_gemm{n, n, n, w.q + n * n, w.q, w.g});
+    plan->prod2.push_back(tn_sector_gemm{n, n, n, w.q, w.t, w.v});
+    plan->prod2.push_back(tn_sector_gemm{n, n, n, w.t, w.q + n * n, w.v + n * n});
+    if (s.M >= s.N)
+      plan->x1_direct.push_back(tn_sector_gemm{s.M, s.N, s.N, s.a_off, w.v, w.x1});
+    else
+      plan->x1_trans.push_back(tn_sector_gemm{s.M, s.N, s.M, w.v + n * n, s.a_off, w.x1});
+    tab.push_back(n);
+    tab.push_back(w.g);
+    tab.push_back(w.t);
+    SvdJob j1;
+    j1.a_off = s.a_off;
+    j1.v_off = w.v;
+    j1.u_off = s.u_off;
+    j1.s_off = s.s_off;
+    j1.vt_off = s.vt_off;
+    j1.M = (int)s.M;
+    j1.N = (int)s.N;
+    j1.b = g1.b;
+    j1.L = g1.L;
+    j1.id = (int)i;
+    SvdJob j2 = j1;
+    j2.a_off = w.x1;
+    j2.v_off = w.v + n * n;  // Q^T after the second Newton-Schulz step
+    j2.b = g.b;
+    j2.L = g.L;
+    int c1 = 0, c2 = 0;
+    while ((1 << c1) < g1.P) c1++;
+    while ((1 << c2) < g.P) c2++;
+    byP1[c1].push_back(j1);
+    byP2[c2].push_back(j2);
+    smem1[c1] = std::max(smem1[c1], g1.smem);
+    smem2[c2] = std::max(smem2[c2], g.smem);
+    thr1[c1] = std::max(thr1[c1], g1.threads);
+    thr2[c2] = std::max(thr2[c2], g.threads);
   }
-  std::vector<SvdJob> all;
-  for (int c = 4; c >= 0; c--) {
-    if (byP[c].empty()) continue;
-    SvdClass k;
-    k.P = 1 << c;
-    k.njobs = (int)byP[c].size();
-    k.first = (int64_t)all.size();
-    k.smem = smemP[c];
-    plan->classes.push_back(k);
-    all.insert(all.end(), byP[c].begin(), byP[c].end());
-  }
-  if (!all.empty()) {
-    plan->jobs = std::make_shared<DevBuf>(all.size() * sizeof(SvdJob), ctx);
-    TN_CUDA(cudaMemcpyAsync(plan->jobs->ptr, all.data(), all.size() * sizeof(SvdJob), cudaMemcpyHostToDevice,
-                            ctx.stream));
+  auto group = [&](std::vector<SvdJob>* by, size_t* smem, int* thr, std::vector<SvdClass>& classes) {
+    std::vector<SvdJob> all;
+    for (int c = 4; c >= 0; c--) {
+      if (by[c].empty()) continue;
+      SvdClass k;
+      k.P = 1 << c;
+      k.njobs = (int)by[c].size();
+      k.first = (int64_t)all.size();
+      k.smem = smem[c];
+      k.threads = thr[c];
+      classes.push_back(k);
+      all.insert(all.end(), by[c].begin(), by[c].end());
+    }
+    return all;
+  };
+  std::vector<SvdJob> all1 = group(byP1, smem1, thr1, plan->classes1);
+  std::vector<SvdJob> all2 = group(byP2, smem2, thr2, plan->classes2);
+  if (!all1.empty()) {
+    plan->jobs1 = upload(ctx, all1.data(), all1.size() * sizeof(SvdJob));
+    plan->jobs2 = upload(ctx, all2.data(), all2.size() * sizeof(SvdJob));
+    plan->ns_tab = upload(ctx, tab.data(), tab.size() * sizeof(int64_t));
     TN_CUDA(cudaStreamSynchronize(ctx.stream));
   }
   ctx.svd_cache[key] = plan;
@@ -179,17 +283,37 @@ void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const dou
                      double* VT, int* info) {
   if (list.empty()) return;
   auto plan = get_svd_plan(ctx, list);
-  {
-    ProfScope ps(ctx, "svd_jacobi");
-    const int nc = (int)plan->classes.size();
-    ctx.fork(nc);
-    for (int c = 0; c < nc; c++) {
-      const SvdClass& k = plan->classes[c];
-      launch_svd_jacobi((const SvdJob*)plan->jobs->ptr + k.first, k.njobs, k.P, k.smem, A, U, S, VT, info,
-                        ctx.side_stream(c));
-      ctx.launched();
-    }
-    ctx.join(nc);
+  if (!plan->jac.empty()) {
+    ProfScope ps(ctx, "svd");
+    DevBuf wsb((size_t)plan->ws_elems * sizeof(double), ctx);
+    double* ws = (double*)wsb.ptr;
+    auto stage = [&](int st) {
+      ProfScope pst(ctx, st == 1 ? "svd_stage1_fp32" : "svd_stage2_fp64");
+      const std::vector<SvdClass>& cls = st == 1 ? plan->classes1 : plan->classes2;
+      const int nc = (int)cls.size();
+      ctx.fork(nc);
+      for (int c = 0; c < nc; c++) {
+        const SvdClass& k = cls[c];
+        const SvdJob* jobs = (const SvdJob*)(st == 1 ? plan->jobs1 : plan->jobs2)->ptr + k.first;
+        launch_svd_jacobi(st, jobs, k.njobs, k.P, k.threads, k.smem, st == 1 ? A : ws, ws,
+                          ws, U, S, VT, info, ctx.side_stream(c));
+        ctx.launched();
+      }
+      ctx.join(nc);
+    };
+    const int nj = (int)plan->jac.size();
+    stage(1);  // FP32 sweeps: V, V^T
+    run_sector_gemms(ctx, TN_MODE_FP64, plan->gram1, ws, ws, ws);
+    launch_ns_factor((const int64_t*)plan->ns_tab->ptr, nj, ws, ctx.stream);
+    ctx.launched();
+    run_sector_gemms(ctx, TN_MODE_FP64, plan->prod1, ws, ws, ws);
+    run_sector_gemms(ctx, TN_MODE_FP64, plan->gram2, ws, ws, ws);
+    launch_ns_factor((const int64_t*)plan->ns_tab->ptr, nj, ws, ctx.stream);
+    ctx.launched();
+    run_sector_gemms(ctx, TN_MODE_FP64, plan->prod2, ws, ws, ws);
+    if (!plan->x1_direct.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_direct, A, ws, ws);
+    if (!plan->x1_trans.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_trans, ws, A, ws);
+    stage(2);  // FP64 sweeps on [X1 | Q]: U, S, VT
   }
   for (int i : plan->fallback) {
     svd_fallback(ctx, list[i], A, U, S, VT);
