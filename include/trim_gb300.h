@@ -124,6 +124,17 @@ int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const do
 int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A,
                         const double* B, double* C);
 
+/* Autotuner of the FP64 grouped GEMM (no counterpart in the reference): when
+ * on, the first contraction with a new sector-size histogram (the number of
+ * sectors per (log2 M, log2 N, log2 K) bucket) times each candidate plan --
+ * tile width rule (narrowest of 4/8/16/32 columns that covers N, or always
+ * 32) x K-split target (4, 8, 16 work items per SM) -- once with CUDA events
+ * and keeps the fastest for that histogram; that call is synchronous.  Later
+ * contractions with the same histogram use the kept choice, so they stay
+ * deterministic.  Off by default (the narrowest-width rule, 8 items per SM).
+ * entries (may be NULL) receives the number of histograms tuned so far. */
+int tn_autotune(tn_ctx_t ctx, int on, int64_t* entries);
+
 /* Fixed-scratch variant of tn_contract_sectors in TN_MODE_FP64, for callers
  * that cannot allocate device memory (a host framework that has reserved the
  * GPU for its own allocator under a hard cap, a latency-critical loop that

@@ -63,6 +63,7 @@ _PROTOS = {
     "tn_permute": (_I, [_P, _P, _P, _IP, _DP, _DP]),
     "tn_plan_check_permute": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
     "tn_contract_sectors": (_I, [_P, _I, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
+    "tn_autotune": (_I, [_P, _I, _I64P]),
     "tn_contract_sectors_fp64_noalloc": (_I, [_P, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
     "tn_svd_sectors": (_I, [_P, _I, C.POINTER(SvdSector), _DP, _DP, _DP, _DP, _IP]),
     "tn_svd_plan": (_I, [_I64, _I64, _I, _IP, _IP, _IP, _I64P]),

@@ -255,6 +255,14 @@ int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* lis
   });
 }
 
+int tn_autotune(tn_ctx_t ctx, int on, int64_t* entries) {
+  return guard([&] {
+    tn::Ctx* c = tn::as_ctx(ctx);
+    c->autotune = on != 0;
+    if (entries) *entries = (int64_t)c->tuned.size();
+  });
+}
+
 int tn_contract_sectors_fp64_noalloc(void* stream, int n, const tn_sector_gemm* list, const double* A,
                                      const double* B, double* C) {
   return guard([&] {

@@ -143,7 +143,17 @@ struct GemmTile {
   int32_t k0, k1;               // K range of this item
   int32_t split;                // index of this K split (0..nsplit-1)
   int32_t nsplit;
+  int32_t tn;                   // tile columns: 32, 16, 8 or 4 (512/tn rows)
   int64_t ws_off;               // partial-tile slot in the workspace (elements), -1 if nsplit==1
+};
+
+// Planning choices of the FP64 grouped GEMM (the autotuner's search space):
+// tile width rule (0: the narrowest of 4/8/16/32 that covers N; 1: always 32)
+// and the K-split target (work items per SM).
+struct Fp64Policy {
+  int tn_rule = 0;
+  int items_per_sm = 8;
+  bool operator==(const Fp64Policy& o) const { return tn_rule == o.tn_rule && items_per_sm == o.items_per_sm; }
 };
 
 // Tensor-core sector GEMM (split precision / fast BF16): one contraction's
@@ -247,6 +257,8 @@ struct Ctx {
   void fork(int n);                 // side streams 1..n-1 wait for `stream`
   void join(int n);                 // `stream` waits for side streams 1..n-1
   void* solver = nullptr;           // cuSOLVER handle (lazily created)
+  bool autotune = false;            // FP64 GEMM policies timed per sector histogram
+  std::unordered_map<uint64_t, Fp64Policy> tuned;
   std::unordered_map<uint64_t, std::shared_ptr<void>> svd_cache;  // SVD batch plans
 };
 Ctx* default_ctx();  // lazily created context on the current device
@@ -271,11 +283,12 @@ uint64_t hash_list(const std::vector<tn_sector_gemm>& list, int tag);
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A,
                       const double* B, double* C);
 
-// FP64 tile plan: 16x32 output tiles, K split until ~4 items per SM; with
-// ws_cap_elems >= 0 the split is dropped when its partial tiles would need
-// more workspace than that (ws_elems receives the workspace needed).
+// FP64 tile plan: 512-entry output tiles shaped to each sector's width, K
+// split to the policy's items per SM; with ws_cap_elems >= 0 the split is
+// dropped when its partial tiles would need more workspace than that
+// (ws_elems receives the workspace needed).
 std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num_sms, int64_t ws_cap_elems,
-                                int64_t* ws_elems);
+                                int64_t* ws_elems, const Fp64Policy& pol = Fp64Policy());
 
 // kernel launchers (defined in the .cu files)
 void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles,

@@ -5,32 +5,44 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <map>
 
 #include "engine.h"
 
 namespace tn {
 
 namespace {
-constexpr int kTileM = 16, kTileN = 32;
+constexpr int kTileElems = 512;
+
+// tile width for a sector of N columns under a policy
+int tile_width(int64_t N, const Fp64Policy& pol) {
+  if (pol.tn_rule == 1) return 32;
+  int tn = 4;
+  while (tn < 32 && tn < N) tn *= 2;
+  return tn;
+}
 
 std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, int num_sms, bool allow_split,
-                                      int64_t* ws_elems) {
-  // K is split so that no work item (one 16x32 tile over a K range) carries
-  // much more than an even share of the total, with at least ~4 items per SM
+                                      int64_t* ws_elems, const Fp64Policy& pol) {
+  // K is split so that no work item (one tile over a K range) carries much
+  // more than total / (SMs x items_per_sm), with at least ~4 items per SM
   int64_t tiles = 0;
   double work = 0;
   for (const auto& g : list) {
-    int64_t t = ((g.M + kTileM - 1) / kTileM) * ((g.N + kTileN - 1) / kTileN);
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
+    const int tn = tile_width(g.N, pol), tm = kTileElems / tn;
+    int64_t t = ((g.M + tm - 1) / tm) * ((g.N + tn - 1) / tn);
     tiles += t;
     work += (double)t * g.K;
   }
-  const int64_t target_items = (int64_t)num_sms * 8;
+  const int64_t target_items = (int64_t)num_sms * std::max(1, pol.items_per_sm);
   const double kmax = std::max(64.0, work / (double)target_items);  // K per item
   std::vector<GemmTile> out;
   int64_t ws = 0;
   for (const auto& g : list) {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX || g.N > INT32_MAX || g.K > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large");
+    const int tn = tile_width(g.N, pol), tm = kTileElems / tn;
     int nsplit = 1;
     if (allow_split) {
       nsplit = (int)std::ceil((double)g.K / kmax);
@@ -40,12 +52,12 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
     }
     const int kchunk = (int)((g.K + nsplit - 1) / nsplit);
     nsplit = (int)((g.K + kchunk - 1) / kchunk);
-    for (int64_t m0 = 0; m0 < g.M; m0 += kTileM)
-      for (int64_t n0 = 0; n0 < g.N; n0 += kTileN) {
+    for (int64_t m0 = 0; m0 < g.M; m0 += tm)
+      for (int64_t n0 = 0; n0 < g.N; n0 += tn) {
         int64_t slot = -1;
         if (nsplit > 1) {
           slot = ws;
-          ws += (int64_t)nsplit * kTileM * kTileN;
+          ws += (int64_t)nsplit * kTileElems;
         }
         for (int s = 0; s < nsplit; s++) {
           GemmTile t;
@@ -61,6 +73,7 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
           t.k1 = (int32_t)std::min<int64_t>(g.K, (int64_t)(s + 1) * kchunk);
           t.split = s;
           t.nsplit = nsplit;
+          t.tn = tn;
           t.ws_off = slot;
           out.push_back(t);
         }
@@ -72,35 +85,38 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
 }  // namespace
 
 std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num_sms, int64_t ws_cap_elems,
-                                int64_t* ws_elems) {
-  std::vector<GemmTile> t = plan_fp64_split(list, num_sms, true, ws_elems);
-  if (ws_cap_elems >= 0 && *ws_elems > ws_cap_elems) t = plan_fp64_split(list, num_sms, false, ws_elems);
+                                int64_t* ws_elems, const Fp64Policy& pol) {
+  std::vector<GemmTile> t = plan_fp64_split(list, num_sms, true, ws_elems, pol);
+  if (ws_cap_elems >= 0 && *ws_elems > ws_cap_elems) t = plan_fp64_split(list, num_sms, false, ws_elems, pol);
   return t;
 }
 
 struct Fp64Plan {
   std::vector<tn_sector_gemm> list;
+  Fp64Policy pol;
   DevBufP tiles;
   int ntiles = 0;
   int64_t ws_elems = 0;
   double flops = 0, bytes = 0;
 };
 
-static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list) {
-  const uint64_t key = hash_list(list, 64);
+static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list,
+                                               const Fp64Policy& pol) {
+  const uint64_t key = hash_list(list, 64 + 16 * pol.tn_rule + pol.items_per_sm);
   {
     std::lock_guard<std::mutex> lk(ctx.mu);
     auto it = ctx.gemm_cache.find(key);
     if (it != ctx.gemm_cache.end()) {
       auto P = std::static_pointer_cast<Fp64Plan>(it->second);
-      if (P->list.size() == list.size() &&
+      if (P->pol == pol && P->list.size() == list.size() &&
           std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0)
         return P;
     }
   }
   auto P = std::make_shared<Fp64Plan>();
   P->list = list;
-  std::vector<GemmTile> tiles = plan_fp64(list, ctx.num_sms, -1, &P->ws_elems);
+  P->pol = pol;
+  std::vector<GemmTile> tiles = plan_fp64(list, ctx.num_sms, -1, &P->ws_elems, pol);
   P->ntiles = (int)tiles.size();
   for (const auto& g : list) {
     P->flops += 2.0 * g.M * g.N * g.K;
@@ -118,22 +134,107 @@ static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_se
   return P;
 }
 
-static void run_fp64(Ctx& ctx, const std::vector<tn_sector_gemm>& list, const double* A, const double* B, double* C) {
-  auto P = get_fp64_plan(ctx, list);
-  if (!P->ntiles) return;
+static void launch_fp64_plan(Ctx& ctx, const Fp64Plan& P, const double* A, const double* B, double* C) {
   double* ws = nullptr;
-  if (P->ws_elems > 0) ws = (double*)ctx.ensure_workspace(P->ws_elems * sizeof(double))->ptr;
-  int grid = (int)std::min<int64_t>((int64_t)P->ntiles, (int64_t)ctx.num_sms * 16);
+  if (P.ws_elems > 0) ws = (double*)ctx.ensure_workspace(P.ws_elems * sizeof(double))->ptr;
+  int grid = (int)std::min<int64_t>((int64_t)P.ntiles, (int64_t)ctx.num_sms * 16);
   {
-    ProfScope ps(ctx, "gemm_fp64", P->bytes, P->flops);
-    launch_gemm_fp64((const GemmTile*)P->tiles->ptr, P->ntiles, A, B, C, ws, grid, ctx.stream);
+    ProfScope ps(ctx, "gemm_fp64", P.bytes, P.flops);
+    launch_gemm_fp64((const GemmTile*)P.tiles->ptr, P.ntiles, A, B, C, ws, grid, ctx.stream);
     ctx.launched();
   }
-  if (P->ws_elems > 0) {
+  if (P.ws_elems > 0) {
     ProfScope ps(ctx, "splitk_reduce", 0, 0);
-    launch_splitk_reduce((const GemmTile*)P->tiles->ptr, P->ntiles, ws, C, grid, ctx.stream);
+    launch_splitk_reduce((const GemmTile*)P.tiles->ptr, P.ntiles, ws, C, grid, ctx.stream);
     ctx.launched();
   }
+}
+
+// The key of a contraction for the autotuner: its sector-size histogram
+// (number of sectors per (log2 M, log2 N, log2 K) bucket), FNV-hashed.
+uint64_t sector_histogram_key(const std::vector<tn_sector_gemm>& list) {
+  std::map<uint32_t, int64_t> h;
+  auto lg = [](int64_t v) {
+    uint32_t r = 0;
+    while ((int64_t(1) << (r + 1)) <= v) r++;
+    return r;
+  };
+  for (const auto& g : list)
+    if (g.M > 0 && g.N > 0 && g.K > 0) h[(lg(g.M) << 16) | (lg(g.N) << 8) | lg(g.K)]++;
+  uint64_t x = 1469598103934665603ull;
+  for (const auto& kv : h) {
+    x = (x ^ kv.first) * 1099511628211ull;
+    x = (x ^ (uint64_t)kv.second) * 1099511628211ull;
+  }
+  return x;
+}
+
+const std::vector<Fp64Policy>& fp64_candidates() {
+  static const std::vector<Fp64Policy> c = [] {
+    std::vector<Fp64Policy> v;
+    for (int rule : {0, 1})
+      for (int items : {4, 8, 16}) {
+        Fp64Policy p;
+        p.tn_rule = rule;
+        p.items_per_sm = items;
+        v.push_back(p);
+      }
+    return v;
+  }();
+  return c;
+}
+
+// Times every candidate once on this call's operands (CUDA events on the
+// context's stream, outside any graph capture) and keeps the fastest for the
+// histogram key; the winner's result is the one left in C.
+static Fp64Policy tune_fp64(Ctx& ctx, uint64_t key, const std::vector<tn_sector_gemm>& list, const double* A,
+                            const double* B, double* C) {
+  cudaEvent_t e0, e1;
+  TN_CUDA(cudaEventCreate(&e0));
+  TN_CUDA(cudaEventCreate(&e1));
+  Fp64Policy best;
+  float best_ms = -1.0f;
+  for (const auto& pol : fp64_candidates()) {
+    auto P = get_fp64_plan(ctx, list, pol);
+    if (!P->ntiles) continue;
+    launch_fp64_plan(ctx, *P, A, B, C);  // warm the plan and the caches
+    TN_CUDA(cudaEventRecord(e0, ctx.stream));
+    launch_fp64_plan(ctx, *P, A, B, C);
+    TN_CUDA(cudaEventRecord(e1, ctx.stream));
+    TN_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    TN_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    if (best_ms < 0 || ms < best_ms) {
+      best_ms = ms;
+      best = pol;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  ctx.tuned[key] = best;
+  return best;
+}
+
+static bool capturing(Ctx& ctx) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  TN_CUDA(cudaStreamIsCapturing(ctx.stream, &st));
+  return st != cudaStreamCaptureStatusNone;
+}
+
+static void run_fp64(Ctx& ctx, const std::vector<tn_sector_gemm>& list, const double* A, const double* B, double* C) {
+  Fp64Policy pol;
+  if (ctx.autotune) {
+    const uint64_t key = sector_histogram_key(list);
+    auto it = ctx.tuned.find(key);
+    if (it != ctx.tuned.end()) {
+      pol = it->second;
+    } else if (!capturing(ctx)) {
+      pol = tune_fp64(ctx, key, list, A, B, C);
+    }
+  }
+  auto P = get_fp64_plan(ctx, list, pol);
+  if (!P->ntiles) return;
+  launch_fp64_plan(ctx, *P, A, B, C);
 }
 
 void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,

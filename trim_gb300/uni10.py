@@ -89,6 +89,14 @@ def truncate_sectors(s_off, counts, s_ptr: int, chi: int):
     return list(kept)[:n], norm.value
 
 
+def autotune(on: bool) -> int:
+    """Switch the FP64 GEMM autotuner of the default context; returns the
+    number of sector-size histograms tuned so far."""
+    n = C.c_int64()
+    call("tn_autotune", None, int(bool(on)), C.byref(n))
+    return n.value
+
+
 def sync() -> None:
     call("tn_ctx_sync", None)
 
