@@ -162,8 +162,11 @@ struct TcSector {
   int64_t a_off, b_off, c_off;  // operand / output element offsets
   int64_t a_img, b_img;         // byte offsets of the slice images in the workspace
   int64_t ea_off, eb_off;       // offsets of the row / column maxima (IEEE bits, uint64)
+  int64_t p_off;                // FP64 partial tiles of a K-split sector (elements), -1 if not split
   int32_t M, N, K;
   int32_t nmt, nnt, nkt;        // 128-row, 64-column and 64-k tile counts
+  int32_t nsplit;               // K ranges per output tile (chunk aligned)
+  int32_t kts;                  // 64-k tiles per K range (a multiple of the 512-k chunk)
 };
 
 // One sector of the cluster Jacobi SVD (M x N, row-major).  Stage 1 (FP32):
@@ -303,8 +306,11 @@ void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts,
                     unsigned long long* bmax, int64_t nmax, uint8_t* images, int num_sms, cudaStream_t s);
 size_t tc_gemm_smem(int ns);
 void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems, const uint8_t* ws,
-                    const unsigned long long* ea, const unsigned long long* eb, double* C, int* err, int grid,
-                    cudaStream_t s);
+                    const unsigned long long* ea, const unsigned long long* eb, double* C, double* part, int* err,
+                    int grid, cudaStream_t s);
+// C tile = sum over the K ranges of its FP64 partial tiles, in range order
+void launch_tc_reduce(const TcSector* secs, const int4* ritems, int nred, const double* part, double* C, int grid,
+                      cudaStream_t s);
 void launch_scale(double* p, int64_t n, double a, cudaStream_t s);
 
 // SVD (Block::svd per sector) and truncation

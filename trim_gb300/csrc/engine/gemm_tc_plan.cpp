@@ -13,6 +13,7 @@ namespace tn {
 
 namespace {
 constexpr int kTM = 128, kTN = 64, kTK = 64;
+constexpr int kChunkTiles = 9;  // 64-k tiles per exact-accumulation chunk of the split kernel
 int64_t cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
 }  // namespace
 
@@ -20,8 +21,9 @@ struct TcPlan {
   std::vector<tn_sector_gemm> list;
   int ns = 7;
   DevBufP meta;
-  size_t off_secs = 0, off_rb = 0, off_cb = 0, off_at = 0, off_bt = 0, off_it = 0;
-  int nsec = 0, nitems = 0;
+  size_t off_secs = 0, off_rb = 0, off_cb = 0, off_at = 0, off_bt = 0, off_it = 0, off_rit = 0;
+  int nsec = 0, nitems = 0, nred = 0;
+  int64_t part_elems = 0;  // FP64 partial tiles of the K-split sectors
   int64_t rows = 0, cols = 0, nrb = 0, ncb = 0, a_tiles = 0, b_tiles = 0, img = 0;
   double flops = 0, in_bytes = 0;
 };
@@ -70,9 +72,9 @@ static std::shared_ptr<TcPlan> build_tc_plan(Ctx& ctx, const std::vector<tn_sect
     P->ncb += s.nnt;
     P->a_tiles += (int64_t)s.nmt * s.nkt;
     P->b_tiles += (int64_t)s.nnt * s.nkt;
-    const int idx = (int)secs.size();
-    for (int mt = 0; mt < s.nmt; mt++)
-      for (int nt = 0; nt < s.nnt; nt++) items.push_back(make_int4(idx, mt, nt, 0));
+    s.nsplit = 1;
+    s.kts = s.nkt;
+    s.p_off = -1;
     secs.push_back(s);
     rb.push_back(P->nrb);
     cb.push_back(P->ncb);
@@ -81,8 +83,38 @@ static std::shared_ptr<TcPlan> build_tc_plan(Ctx& ctx, const std::vector<tn_sect
     P->flops += 2.0 * g.M * g.N * g.K;
     P->in_bytes += 8.0 * ((double)g.M * g.K + (double)g.K * g.N);
   }
+  // K split: with fewer than two output tiles per SM, long-K sectors are cut
+  // into K ranges of whole 576-k chunks (the exact-accumulation unit); each
+  // range writes an FP64 partial tile and a reduction sums them in order.
+  int64_t tiles = 0;
+  for (const auto& s : secs) tiles += (int64_t)s.nmt * s.nnt;
+  const int64_t want = 2 * (int64_t)ctx.num_sms;
+  const int64_t factor = tiles > 0 ? std::max<int64_t>(1, (want + tiles - 1) / tiles) : 1;
+  std::vector<int4> ritems;
+  for (int idx = 0; idx < (int)secs.size(); idx++) {
+    TcSector& s = secs[idx];
+    const int64_t chunks = cdiv(s.nkt, kChunkTiles);
+    if (factor > 1 && chunks > 1) {
+      const int64_t nsplit = std::min<int64_t>({factor, chunks, 64});
+      const int64_t cps = cdiv(chunks, nsplit);
+      s.kts = (int32_t)(cps * kChunkTiles);
+      s.nsplit = (int32_t)cdiv(s.nkt, s.kts);
+      if (s.nsplit > 1) {
+        s.p_off = P->part_elems;
+        P->part_elems += (int64_t)s.nmt * s.nnt * s.nsplit * kTM * kTN;
+      } else {
+        s.kts = s.nkt;
+      }
+    }
+    for (int mt = 0; mt < s.nmt; mt++)
+      for (int nt = 0; nt < s.nnt; nt++) {
+        for (int q = 0; q < s.nsplit; q++) items.push_back(make_int4(idx, mt, nt, q));
+        if (s.nsplit > 1) ritems.push_back(make_int4(idx, mt, nt, 0));
+      }
+  }
   P->nsec = (int)secs.size();
   P->nitems = (int)items.size();
+  P->nred = (int)ritems.size();
   if (!P->nsec) return P;
   const int n1 = P->nsec + 1;
   P->off_secs = 0;
@@ -91,7 +123,8 @@ static std::shared_ptr<TcPlan> build_tc_plan(Ctx& ctx, const std::vector<tn_sect
   P->off_at = P->off_cb + n1 * sizeof(int64_t);
   P->off_bt = P->off_at + n1 * sizeof(int64_t);
   P->off_it = (P->off_bt + n1 * sizeof(int64_t) + 15) & ~(size_t)15;
-  size_t bytes = P->off_it + items.size() * sizeof(int4);
+  P->off_rit = P->off_it + items.size() * sizeof(int4);
+  size_t bytes = P->off_rit + ritems.size() * sizeof(int4);
   std::vector<uint8_t> meta(bytes);
   std::memcpy(meta.data() + P->off_secs, secs.data(), P->nsec * sizeof(TcSector));
   std::memcpy(meta.data() + P->off_rb, rb.data(), n1 * sizeof(int64_t));
@@ -99,6 +132,7 @@ static std::shared_ptr<TcPlan> build_tc_plan(Ctx& ctx, const std::vector<tn_sect
   std::memcpy(meta.data() + P->off_at, ats.data(), n1 * sizeof(int64_t));
   std::memcpy(meta.data() + P->off_bt, bts.data(), n1 * sizeof(int64_t));
   std::memcpy(meta.data() + P->off_it, items.data(), items.size() * sizeof(int4));
+  if (!ritems.empty()) std::memcpy(meta.data() + P->off_rit, ritems.data(), ritems.size() * sizeof(int4));
   P->meta = std::make_shared<DevBuf>(bytes, ctx);
   TN_CUDA(cudaMemcpyAsync(P->meta->ptr, meta.data(), bytes, cudaMemcpyHostToDevice, ctx.stream));
   TN_CUDA(cudaStreamSynchronize(ctx.stream));  // the host copy dies here
@@ -130,12 +164,15 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
   if (!P->nsec) return;
   const uint8_t* mb = (const uint8_t*)P->meta->ptr;
   const TcSector* dsecs = (const TcSector*)(mb + P->off_secs);
-  // workspace: row / column maxima (uint64) then the slice images
+  // workspace: row / column maxima (uint64), the slice images, then the
+  // FP64 partial tiles of K-split sectors
   size_t max_bytes = (((size_t)(P->rows + P->cols)) * sizeof(unsigned long long) + 1023) & ~(size_t)1023;
-  uint8_t* ws = (uint8_t*)ctx.ensure_workspace(max_bytes + (size_t)P->img)->ptr;
+  const size_t img_bytes = ((size_t)P->img + 1023) & ~(size_t)1023;
+  uint8_t* ws = (uint8_t*)ctx.ensure_workspace(max_bytes + img_bytes + (size_t)P->part_elems * sizeof(double))->ptr;
   unsigned long long* ea = (unsigned long long*)ws;
   unsigned long long* eb = ea + P->rows;
   uint8_t* images = ws + max_bytes;
+  double* part = (double*)(images + img_bytes);
   int* err = ctx.device_error_word();
   {
     ProfScope ps(ctx, "tc_slice", 2 * P->in_bytes + (double)P->img, 0);
@@ -146,7 +183,14 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
   {
     ProfScope ps(ctx, ns == 7 ? "tc_gemm_split" : "tc_gemm_bf16", 0, P->flops);
     int grid = (int)std::min<int64_t>((int64_t)P->nitems, (int64_t)ctx.num_sms);
-    launch_tc_gemm(ns, dsecs, (const int4*)(mb + P->off_it), P->nitems, images, ea, eb, C, err, grid, ctx.stream);
+    launch_tc_gemm(ns, dsecs, (const int4*)(mb + P->off_it), P->nitems, images, ea, eb, C, part, err, grid,
+                   ctx.stream);
+    ctx.launched();
+  }
+  if (P->nred > 0) {
+    ProfScope ps(ctx, "tc_reduce", 0, 0);
+    const int grid = (int)std::min<int64_t>((int64_t)P->nred, (int64_t)ctx.num_sms * 4);
+    launch_tc_reduce(dsecs, (const int4*)(mb + P->off_rit), P->nred, part, C, grid, ctx.stream);
     ctx.launched();
   }
 }

@@ -6,8 +6,9 @@
 // (d_0 in [-129, 129], d_1..d_6 in [-64, 63]); digit s is stored as the BF16
 // value d * 2^-7s, exact.  C = 2^(ea+eb-14) * sum_{s+t<=7} A_s B_t (34 of the
 // 49 digit products).  The products of one level l = s+t are integers times
-// 2^-7l and stay below 2^15 per k for l <= 4, so levels 0..4 accumulate
-// exactly in FP32 over a chunk of 512 k; they get their own TMEM
+// 2^-7l; per k their magnitudes sum to at most 2*129*64 + 3*64*64 = 28800
+// (level 4, the largest), so levels 0..4 accumulate exactly in FP32 over a
+// chunk of 576 k (576 * 28800 < 2^24); they get their own TMEM
 // accumulators and are drained into a double-float (hi, lo) FP32 sum per
 // chunk.  Levels 5..7 share one accumulator (their FP32 rounding is far
 // below 2^-53 of the result).  The dropped levels 8..12 and the operand
@@ -37,8 +38,8 @@ using namespace ptx;
 constexpr int kTM = 128, kTN = 64, kTK = 64;
 constexpr int kATile = kTM * kTK * 2;  // bytes of one A slice tile
 constexpr int kBTile = kTN * kTK * 2;  // bytes of one B slice tile
-constexpr int kARing = 4, kBRing = 2;
-constexpr int kChunkTiles = 8;  // 512 k per exact-accumulation chunk
+constexpr int kARing = 6, kBRing = 2;
+constexpr int kChunkTiles = 9;  // 576 k per exact-accumulation chunk
 constexpr int kLevels = 6;      // exact levels 0..4 + one shared accumulator for 5..7
 constexpr int kMaxLevel = 7;    // digit products with s + t <= 7 are kept
 constexpr int kThreadsTc = 192;
@@ -317,7 +318,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
                                                          const uint8_t* __restrict__ ws,
                                                          const unsigned long long* __restrict__ ea,
                                                          const unsigned long long* __restrict__ eb,
-                                                         double* __restrict__ C,
+                                                         double* __restrict__ C, double* __restrict__ part,
                                                          int* __restrict__ err) {
   constexpr int LV = (NS == 1) ? 1 : kLevels;
   constexpr int kChunk = (NS == 1) ? 1 << 20 : kChunkTiles;  // fast mode: one chunk over all of K
@@ -363,7 +364,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
         const TcSector& S = secs[w.x];
         const uint8_t* a_src = ws + S.a_img + (int64_t)w.y * S.nkt * NS * kATile;
         const uint8_t* b_src = ws + S.b_img + (int64_t)w.z * S.nkt * NS * kBTile;
-        for (int kt = 0; kt < S.nkt && ok; kt++) {
+        const int kb = w.w * S.kts, ke = min(S.nkt, kb + S.kts);  // this item's K range
+        for (int kt = kb; kt < ke && ok; kt++) {
           const int sb = nb % kBRing;
           if (!mbar_wait(&sh.emptyB[sb], ((nb / kBRing) & 1) ^ 1, &sh.abort)) { ok = false; break; }
           mbar_arrive_expect_tx(&sh.fullB[sb], NS * kBTile);
@@ -398,8 +400,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
       for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
         const int4 w = items[it];
         const TcSector& S = secs[w.x];
-        for (int k0 = 0; k0 < S.nkt && ok; k0 += kChunk) {
-          const int k1 = min(S.nkt, k0 + kChunk);
+        const int kb = w.w * S.kts, ke = min(S.nkt, kb + S.kts);
+        for (int k0 = kb; k0 < ke && ok; k0 += kChunk) {
+          const int k1 = min(ke, k0 + kChunk);
           if (!mbar_wait(&sh.acc_empty, (nchunk & 1) ^ 1, &sh.abort)) { ok = false; break; }
           tc_fence_after();
           uint32_t touched = 0;
@@ -451,7 +454,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
       float hi[kTN], lo[kTN];
 #pragma unroll
       for (int j = 0; j < kTN; j++) hi[j] = lo[j] = 0.f;
-      for (int k0 = 0; k0 < S.nkt; k0 += kChunk) {
+      const int kb = w.w * S.kts, ke = min(S.nkt, kb + S.kts);
+      for (int k0 = kb; k0 < ke; k0 += kChunk) {
         if (!mbar_wait(&sh.acc_full, nchunk & 1, &sh.abort)) { ok = false; break; }
         tc_fence_after();
 #pragma unroll
@@ -473,7 +477,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
       const int64_t i = (int64_t)w.y * kTM + quad * 32 + lane;
       if (i < S.M) {
         const int e_i = exp_of(ea[S.ea_off + i]);
-        double* crow = C + S.c_off + i * S.N;
+        // one K range of a split sector: its FP64 partial tile, [128][64]
+        double* crow = S.nsplit > 1
+                           ? part + S.p_off + (((int64_t)w.y * S.nnt + w.z) * S.nsplit + w.w) * (kTM * kTN) +
+                                 (quad * 32 + lane) * kTN - (int64_t)w.z * kTN
+                           : C + S.c_off + i * S.N;
 #pragma unroll
         for (int j = 0; j < kTN; j++) {
           const int64_t jj = (int64_t)w.z * kTN + j;
@@ -487,6 +495,23 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
   __syncthreads();
   tc_fence_after();
   if (warp == 1) tmem_dealloc(tmem, 512);
+}
+
+// one CTA per split output tile: C = sum of its partial tiles in K-range order
+__global__ void __launch_bounds__(256) tc_reduce(const TcSector* __restrict__ secs, const int4* __restrict__ ritems,
+                                                 int nred, const double* __restrict__ part, double* __restrict__ C) {
+  for (int it = blockIdx.x; it < nred; it += gridDim.x) {
+    const int4 w = ritems[it];
+    const TcSector& S = secs[w.x];
+    const double* p = part + S.p_off + ((int64_t)w.y * S.nnt + w.z) * S.nsplit * (kTM * kTN);
+    for (int e = threadIdx.x; e < kTM * kTN; e += blockDim.x) {
+      const int64_t i = (int64_t)w.y * kTM + e / kTN, j = (int64_t)w.z * kTN + e % kTN;
+      if (i >= S.M || j >= S.N) continue;
+      double s = 0.0;
+      for (int q = 0; q < S.nsplit; q++) s += p[(int64_t)q * (kTM * kTN) + e];
+      C[S.c_off + i * S.N + j] = s;
+    }
+  }
 }
 
 }  // namespace
@@ -510,8 +535,8 @@ void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts,
 size_t tc_gemm_smem(int ns) { return (size_t)kARing * kATile + (size_t)kBRing * ns * kBTile + 1024; }
 
 void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems, const uint8_t* ws,
-                    const unsigned long long* ea, const unsigned long long* eb, double* C, int* err, int grid,
-                    cudaStream_t s) {
+                    const unsigned long long* ea, const unsigned long long* eb, double* C, double* part, int* err,
+                    int grid, cudaStream_t s) {
   const size_t smem = tc_gemm_smem(ns);
   if (ns == 7) {
     static bool attr = false;
@@ -519,15 +544,22 @@ void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems,
       TN_CUDA(cudaFuncSetAttribute(tc_gemm<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr = true;
     }
-    tc_gemm<7><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, err);
+    tc_gemm<7><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, part, err);
   } else {
     static bool attr = false;
     if (!attr) {
       TN_CUDA(cudaFuncSetAttribute(tc_gemm<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr = true;
     }
-    tc_gemm<1><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, err);
+    tc_gemm<1><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, part, err);
   }
+  TN_CUDA(cudaGetLastError());
+}
+
+void launch_tc_reduce(const TcSector* secs, const int4* ritems, int nred, const double* part, double* C, int grid,
+                      cudaStream_t s) {
+  if (nred <= 0) return;
+  tc_reduce<<<grid, 256, 0, s>>>(secs, ritems, nred, part, C);
   TN_CUDA(cudaGetLastError());
 }
 
