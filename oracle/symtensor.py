@@ -26,8 +26,9 @@ Per-sector GEMMs call numpy's BLAS (``@``), as the reference calls dgemm_
 (uni10_lapack_cpu.cpp:41-44).  The bit-exact parts (sector map, permute) are
 pinned against the compiled reference (oracle/_ref) and against the
 reference's own fixtures (Swig/examples/egU3_W, egU3_WT); see tests/golden.
-Fermionic signs (UniTensorReal.cpp:654-681) are restated for bosonic tensors
-only: every configuration of this path is bosonic.
+Fermionic signs of permute (UniTensorReal.cpp:654-681, 733-738) are restated
+and pinned by fermionic fixtures of the compiled reference; transpose carries
+no sign (UniTensorReal.cpp:448-506), as in the reference.
 """
 from __future__ import annotations
 
@@ -394,13 +395,38 @@ def _subblock_dims(t: UniTensor, qidx: int):
     return idxs
 
 
+def fermion_swaps(n: int, rbn_in: int, rbn_out: int, rsp):
+    """Bond swaps that carry fermionic signs (UniTensorReal.cpp:656-681;
+    recSwap, tools/lib/uni10_tools.cpp:48-67): in- and output bonds are put in
+    the order row bonds, then column bonds reversed; the adjacent exchanges
+    of a bubble sort of the output order (by input position) are the swaps,
+    each named by its two input bonds."""
+    ordf = [b if b < rbn_in else n - b + rbn_in - 1 for b in range(n)]  # bond -> position (an involution)
+    ord_ = [0] * n
+    for j in range(n):
+        pj = j if j < rbn_out else n - j + rbn_out - 1
+        ord_[pj] = ordf[rsp[j]]
+    swaps = []
+    for i in range(n - 1):
+        for j in range(n - i - 1):
+            if ord_[j] > ord_[j + 1]:
+                swaps.append((ordf[ord_[j + 1]], ordf[ord_[j]]))
+                ord_[j], ord_[j + 1] = ord_[j + 1], ord_[j]
+    return swaps
+
+
 def permute_elems(src: UniTensor, dst: UniTensor, rsp) -> None:
     """The data movement of permute: for every sub-block (Qidx in QidxEnc
     order) copy the input sub-block, viewed as a dense tensor over its bonds'
     degeneracies, into the output sub-block with bonds reordered by rsp
-    (UniTensorReal.cpp:685-757).  Exact: pure data movement."""
+    (UniTensorReal.cpp:685-757).  Exact: pure data movement, times the
+    sub-block's fermionic sign on the symmetric path (:653-681, 733-738)."""
     n = len(src.bonds)
     sm, dm = src.smap, dst.smap
+    # the symmetric path: some input bond has more than one charge
+    # (UniTensorReal.cpp:567-571); bosonic charges give +1 everywhere
+    symmetric = any(len(b.qnums) != 1 for b in src.bonds)
+    swaps = fermion_swaps(n, sm.rbond_num, dm.rbond_num, rsp) if symmetric else []
     qot_acc = [1] * n
     for b in range(n - 1, 0, -1):
         qot_acc[b - 1] = qot_acc[b] * len(dst.bonds[b].qnums)
@@ -420,8 +446,11 @@ def permute_elems(src: UniTensor, dst: UniTensor, rsp) -> None:
             src.elem[s0:], shape=(srd, scd), strides=(bin_c * 8, 8)
         )
         sub = sub.reshape(degs).transpose(rsp).reshape(ord_, ocd)
+        parity = 0
+        for b1, b2 in swaps:
+            parity ^= src.bonds[b1].qnums[qi[b1]].prtf & src.bonds[b2].qnums[qi[b2]].prtf
         dview = np.lib.stride_tricks.as_strided(dst.elem[d0:], shape=(ord_, ocd), strides=(bot_c * 8, 8))
-        dview[...] = sub
+        dview[...] = -sub if parity else sub
 
 
 # --------------------------------------------------------------------------- contract

@@ -71,6 +71,11 @@ def rand_bond(rng, btype, sym):
         for p in rng.permutation(2)[: int(rng.integers(1, 3))]:
             runs.append((0, int(p), 0, int(rng.integers(1, 4))))
         return (btype, runs)
+    if sym == "fermion":  # U(1) charges with fermionic parity (PRTF_ODD sets the reference's Fermionic flag)
+        pool = [(-1, 0), (-1, 1), (0, 0), (0, 1), (1, 0), (1, 1)]
+        nq = int(rng.integers(1, 4))
+        pick = sorted(rng.choice(len(pool), size=nq, replace=False))
+        return (btype, [(pool[k][0], 0, pool[k][1], int(rng.integers(1, 4))) for k in pick])
     return (btype, [(0, 0, 0, int(rng.integers(1, 5)))])
 
 
@@ -141,6 +146,68 @@ def contract_cases(w: Writer, rng, n: int):
         if "C" not in o:
             continue
         case = {"id": f"con{made}", "kind": "contract", "A": tensor_meta(o["A1"]["bonds"], o["A1"]["labels"]),
+                "B": tensor_meta(o["B1"]["bonds"], o["B1"]["labels"]), "out": out_meta(o["C"])}
+        w.add(case, {"A": o["A1"]["elem"], "B": o["B1"]["elem"], "C": o["C"]["elem"]})
+        made += 1
+
+
+def fermion_cases(w: Writer, rng, nperm: int, ncon: int):
+    """Permutes and contractions of tensors with fermionic charges: the
+    reference multiplies each moved sub-block by its swap sign."""
+    made = 0
+    while made < nperm:
+        rank = int(rng.integers(2, 7))
+        bonds = rand_tensor(rng, rank, "fermion")
+        if all(len(runs) == 1 for _, runs in bonds):
+            continue  # a single charge per bond takes the reference's dense path
+        labels = [int(x) for x in rng.permutation(np.arange(10, 10 + rank))]
+        perm = [labels[j] for j in rng.permutation(rank)]
+        rn = int(rng.integers(0, rank + 1))
+        el = rng.uniform(-1, 1, wl.elem_count(bonds))
+        S = refrun.RefSession()
+        S.tensor("T", bonds, labels, el)
+        S.cmd(f"permute T {rn} " + " ".join(map(str, perm)))
+        S.save("T", "P")
+        S.cmd("transpose T")
+        S.save("T", "PT")
+        o = S.run()
+        case = {"id": f"fperm{made}", "kind": "permute", "T": tensor_meta(bonds, labels), "new_labels": perm,
+                "rownum": rn, "out": out_meta(o["P"]), "out_transpose": out_meta(o["PT"])}
+        w.add(case, {"T": el, "P": o["P"]["elem"], "PT": o["PT"]["elem"]})
+        made += 1
+    made = 0
+    while made < ncon:
+        nfa, nfb, nsh = int(rng.integers(1, 3)), int(rng.integers(1, 3)), int(rng.integers(1, 3))
+        shared = [rand_bond(rng, -1, "fermion") for _ in range(nsh)]
+        fa = [rand_bond(rng, 1, "fermion") for _ in range(nfa)]
+        fb = [rand_bond(rng, -1, "fermion") for _ in range(nfb)]
+        a_bonds = fa + shared
+        b_bonds = [wl.change(x, 1) for x in shared] + fb
+        if wl.elem_count(a_bonds) == 0 or wl.elem_count(b_bonds) == 0:
+            continue
+        la = list(range(100, 100 + nfa)) + list(range(200, 200 + nsh))
+        lb = list(range(200, 200 + nsh)) + list(range(300, 300 + nfb))
+        ea = rng.uniform(-1, 1, wl.elem_count(a_bonds))
+        eb = rng.uniform(-1, 1, wl.elem_count(b_bonds))
+        pa = [la[j] for j in rng.permutation(len(la))]
+        pb = [lb[j] for j in rng.permutation(len(lb))]
+        ra, rb = int(rng.integers(0, len(la) + 1)), int(rng.integers(0, len(lb) + 1))
+        S = refrun.RefSession()
+        S.tensor("A", a_bonds, la, ea)
+        S.tensor("B", b_bonds, lb, eb)
+        S.cmd(f"permute A {ra} " + " ".join(map(str, pa)))
+        S.cmd(f"permute B {rb} " + " ".join(map(str, pb)))
+        S.save("A", "A1")
+        S.save("B", "B1")
+        S.cmd("contract C A B 0")
+        S.save("C")
+        try:
+            o = S.run()
+        except RuntimeError:
+            continue
+        if "C" not in o:
+            continue
+        case = {"id": f"fcon{made}", "kind": "contract", "A": tensor_meta(o["A1"]["bonds"], o["A1"]["labels"]),
                 "B": tensor_meta(o["B1"]["bonds"], o["B1"]["labels"]), "out": out_meta(o["C"])}
         w.add(case, {"A": o["A1"]["elem"], "B": o["B1"]["elem"], "C": o["C"]["elem"]})
         made += 1
@@ -323,6 +390,8 @@ def main():
     greedy_network(w, rng)
     permute_cases(w, rng, 40)
     contract_cases(w, rng, 30)
+    # fermionic signs of permute / contract, with a stream of their own
+    fermion_cases(w, np.random.default_rng(777), 16, 8)
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(w.cases, f, indent=0)
     np.savez_compressed(os.path.join(HERE, "arrays.npz"), **w.arrays)

@@ -78,6 +78,28 @@ PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, co
   return finish_plan(ctx, key, subs, src.elem_num);
 }
 
+// The bond swaps that carry fermionic signs (UniTensorReal.cpp:656-681 with
+// recSwap, tools/lib/uni10_tools.cpp:48-67): bonds are ordered row bonds
+// first, column bonds in reverse (before and after the permute); the
+// adjacent exchanges of a bubble sort that takes the new order back to the
+// old one are the swaps, each named by its two source bonds.
+static std::vector<std::pair<int, int>> fermion_swaps(int n, int rbn_in, int rbn_out, const std::vector<int>& rsp) {
+  auto fpos_in = [&](int b) { return b < rbn_in ? b : n - 1 - (b - rbn_in); };  // an involution
+  std::vector<int> ord(n);
+  for (int j = 0; j < n; j++) {
+    const int pj = j < rbn_out ? j : n - 1 - (j - rbn_out);
+    ord[pj] = fpos_in(rsp[j]);
+  }
+  std::vector<std::pair<int, int>> swaps;
+  for (int i = 0; i < n - 1; i++)
+    for (int j = 0; j < n - i - 1; j++)
+      if (ord[j] > ord[j + 1]) {
+        swaps.emplace_back(fpos_in(ord[j + 1]), fpos_in(ord[j]));
+        std::swap(ord[j], ord[j + 1]);
+      }
+  return swaps;
+}
+
 std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp) {
   const int n = (int)src.bonds.size();
   if ((int)dst.bonds.size() != n || (int)rsp.size() != n) fail(TN_ERR_ARG, "permute: bond counts differ");
@@ -93,6 +115,17 @@ std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst,
   std::vector<int64_t> qot_acc(n, 1);
   for (int b = n - 1; b > 0; b--) qot_acc[b - 1] = qot_acc[b] * (int64_t)dst.bonds[b].q.size();
   const int rbn_in = src.rbond_num, rbn_out = dst.rbond_num;
+
+  // fermionic signs apply on the symmetric path only: some source bond has
+  // more than one charge (UniTensorReal.cpp:567-571, 653-681); bosonic
+  // charges (prtF = 0) make every sign +1
+  bool symmetric = false, odd = false;
+  for (const auto& b : src.bonds) {
+    if (b.q.size() != 1) symmetric = true;
+    for (const auto& q : b.q) odd |= q.prtf != 0;
+  }
+  std::vector<std::pair<int, int>> swaps;
+  if (symmetric && odd) swaps = fermion_swaps(n, rbn_in, rbn_out, rsp);
 
   std::vector<PermSub> subs;
   subs.reserve(src.qidx_enc.size());
@@ -129,7 +162,10 @@ std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst,
     std::memset(&ps, 0, sizeof(ps));
     ps.src_base = Bi.off + src.rq2off[rin] * Bi.cols + src.cq2off[cin];
     ps.dst_base = Bo.off + dst.rq2off[rot] * Bo.cols + dst.cq2off[cot];
-    ps.sign = 1.0;
+    int parity = 0;  // UniTensorReal.cpp:733-738
+    for (const auto& sw : swaps)
+      parity ^= src.bonds[sw.first].q[qin[sw.first]].prtf & src.bonds[sw.second].q[qin[sw.second]].prtf;
+    ps.sign = parity ? -1.0 : 1.0;
     // canonical dims in destination order: drop extent 1, merge contiguous
     std::vector<Dim> dims;
     for (int j = 0; j < n; j++) {
