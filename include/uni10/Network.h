@@ -82,6 +82,9 @@ class Network {
   UniTensor graph_out;
   std::vector<std::string> graph_sigs;
   int64_t graph_kernels = 0;
+  // device work lists and workspace the graph's kernels read, kept alive
+  // while the graph exists (the context may replace or evict its own copies)
+  std::vector<std::shared_ptr<void>> graph_keep;
   void drop_graph();
 };
 

@@ -179,6 +179,29 @@ def test_network_graph_capture_replay(env):
         assert not np.array_equal(eager, eager0)
 
 
+def test_graph_replay_survives_workspace_growth(env):
+    """A captured graph keeps the plans and workspace its kernels read: after
+    other work grows the context's workspace (large split-K partials), the
+    replay still gives the eager result bit for bit."""
+    torch, capi, tu = env
+    spec = wl.itebd()
+    rng = np.random.default_rng(spec["seed"])
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    net = tu.Network(spec["net"])
+    ts = {s.name: tu.UniTensor(s.bonds, s.labels, els[s.name]) for s in spec["tensors"]}
+    for n, t in ts.items():
+        net.put_tensor(n, t)
+    net.capture("fp64")
+    out = net.output()
+    eager0 = net.launch("fp64").get_elem()
+    # the operand slice images of a large split-precision product need far
+    # more workspace than the network did
+    errs = _grouped(env, "split_tc", [(2048, 2048, 2048)], 9)
+    assert max(errs) <= SPLIT_TOL
+    net.replay()
+    assert np.array_equal(out.get_elem(), eager0)
+
+
 def test_contract_batch_matches_pairwise(env):
     """One grouped launch for many contractions equals the pairwise contract()
     of each pair: golden fixtures (reference outputs) and 48 random pairs."""

@@ -212,6 +212,7 @@ DevBufP Ctx::ensure_workspace(size_t bytes) {
     size_t want = std::max(bytes, workspace ? workspace->bytes * 2 : (size_t)(16 << 20));
     workspace = std::make_shared<DevBuf>(want, *this);
   }
+  keep_alive(workspace);
   return workspace;
 }
 

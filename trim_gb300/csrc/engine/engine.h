@@ -144,6 +144,7 @@ struct GemmTile {
   int32_t split;                // index of this K split (0..nsplit-1)
   int32_t nsplit;
   int32_t tn;                   // tile columns: 32, 16, 8 or 4 (512/tn rows)
+  int32_t grp;                  // split group (one per split output tile), -1 if nsplit==1
   int64_t ws_off;               // partial-tile slot in the workspace (elements), -1 if nsplit==1
 };
 
@@ -260,6 +261,12 @@ struct Ctx {
   void fork(int n);                 // side streams 1..n-1 wait for `stream`
   void join(int n);                 // `stream` waits for side streams 1..n-1
   void* solver = nullptr;           // cuSOLVER handle (lazily created)
+  // while a stream capture records work: every device plan and workspace the
+  // recorded kernels use is appended here (the graph owner keeps them alive)
+  std::vector<std::shared_ptr<void>>* keep = nullptr;
+  void keep_alive(const std::shared_ptr<void>& p) {
+    if (keep && p) keep->push_back(p);
+  }
   bool autotune = false;            // FP64 GEMM policies timed per sector histogram
   std::unordered_map<uint64_t, Fp64Policy> tuned;
   std::unordered_map<uint64_t, std::shared_ptr<void>> svd_cache;  // SVD batch plans
@@ -296,8 +303,11 @@ std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num
 // kernel launchers (defined in the .cu files)
 void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles,
                            const double* src, double* dst, int grid, cudaStream_t s);
+// counters (one int per split group, zero between launches) may be null: then
+// split tiles need launch_splitk_reduce afterwards; otherwise the last CTA of
+// each split group sums its partial tiles in split order and resets the counter
 void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const double* B, double* C,
-                      double* ws, int grid, cudaStream_t s);
+                      double* ws, int* counters, int grid, cudaStream_t s);
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
                           cudaStream_t s);
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s);

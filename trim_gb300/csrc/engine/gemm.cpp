@@ -38,7 +38,7 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
   const int64_t target_items = (int64_t)num_sms * std::max(1, pol.items_per_sm);
   const double kmax = std::max(64.0, work / (double)target_items);  // K per item
   std::vector<GemmTile> out;
-  int64_t ws = 0;
+  int64_t ws = 0, ngrp = 0;
   for (const auto& g : list) {
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX || g.N > INT32_MAX || g.K > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large");
@@ -59,6 +59,7 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
           slot = ws;
           ws += (int64_t)nsplit * kTileElems;
         }
+        if (nsplit > 1 && ngrp >= INT32_MAX) fail(TN_ERR_UNSUPPORTED, "too many split tiles");
         for (int s = 0; s < nsplit; s++) {
           GemmTile t;
           t.a_off = g.a_off;
@@ -74,9 +75,11 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
           t.split = s;
           t.nsplit = nsplit;
           t.tn = tn;
+          t.grp = nsplit > 1 ? (int32_t)ngrp : -1;
           t.ws_off = slot;
           out.push_back(t);
         }
+        if (nsplit > 1) ngrp++;
       }
   }
   *ws_elems = ws;
@@ -95,6 +98,7 @@ struct Fp64Plan {
   std::vector<tn_sector_gemm> list;
   Fp64Policy pol;
   DevBufP tiles;
+  DevBufP counters;  // one per split group, zero between launches
   int ntiles = 0;
   int64_t ws_elems = 0;
   double flops = 0, bytes = 0;
@@ -109,8 +113,10 @@ static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_se
     if (it != ctx.gemm_cache.end()) {
       auto P = std::static_pointer_cast<Fp64Plan>(it->second);
       if (P->pol == pol && P->list.size() == list.size() &&
-          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0)
+          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0) {
+        ctx.keep_alive(P);
         return P;
+      }
     }
   }
   auto P = std::make_shared<Fp64Plan>();
@@ -122,6 +128,12 @@ static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_se
     P->flops += 2.0 * g.M * g.N * g.K;
     P->bytes += 8.0 * (g.M * g.K + g.K * g.N + g.M * g.N);
   }
+  int64_t ngrp = 0;
+  for (const auto& t : tiles) ngrp = std::max<int64_t>(ngrp, (int64_t)t.grp + 1);
+  if (ngrp > 0) {
+    P->counters = std::make_shared<DevBuf>((size_t)ngrp * sizeof(int), ctx);
+    TN_CUDA(cudaMemsetAsync(P->counters->ptr, 0, (size_t)ngrp * sizeof(int), ctx.stream));
+  }
   if (!tiles.empty()) {
     P->tiles = std::make_shared<DevBuf>(tiles.size() * sizeof(GemmTile), ctx);
     TN_CUDA(cudaMemcpyAsync(P->tiles->ptr, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice,
@@ -131,6 +143,7 @@ static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_se
   std::lock_guard<std::mutex> lk(ctx.mu);
   if (ctx.gemm_cache.size() > 4096) ctx.gemm_cache.clear();
   ctx.gemm_cache[key] = P;
+  ctx.keep_alive(P);
   return P;
 }
 
@@ -139,13 +152,10 @@ static void launch_fp64_plan(Ctx& ctx, const Fp64Plan& P, const double* A, const
   if (P.ws_elems > 0) ws = (double*)ctx.ensure_workspace(P.ws_elems * sizeof(double))->ptr;
   int grid = (int)std::min<int64_t>((int64_t)P.ntiles, (int64_t)ctx.num_sms * 16);
   {
+    // split tiles are summed by the last CTA of each group (no second launch)
     ProfScope ps(ctx, "gemm_fp64", P.bytes, P.flops);
-    launch_gemm_fp64((const GemmTile*)P.tiles->ptr, P.ntiles, A, B, C, ws, grid, ctx.stream);
-    ctx.launched();
-  }
-  if (P.ws_elems > 0) {
-    ProfScope ps(ctx, "splitk_reduce", 0, 0);
-    launch_splitk_reduce((const GemmTile*)P.tiles->ptr, P.ntiles, ws, C, grid, ctx.stream);
+    launch_gemm_fp64((const GemmTile*)P.tiles->ptr, P.ntiles, A, B, C, ws,
+                     P.counters ? (int*)P.counters->ptr : nullptr, grid, ctx.stream);
     ctx.launched();
   }
 }

@@ -147,14 +147,17 @@ static std::shared_ptr<TcPlan> get_tc_plan(Ctx& ctx, const std::vector<tn_sector
     if (it != ctx.tc_cache.end()) {
       auto P = std::static_pointer_cast<TcPlan>(it->second);
       if (P->ns == ns && P->list.size() == list.size() &&
-          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0)
+          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0) {
+        ctx.keep_alive(P);
         return P;
+      }
     }
   }
   auto P = build_tc_plan(ctx, list, ns);
   std::lock_guard<std::mutex> lk(ctx.mu);
   if (ctx.tc_cache.size() > 1024) ctx.tc_cache.clear();
   ctx.tc_cache[key] = P;
+  ctx.keep_alive(P);
   return P;
 }
 

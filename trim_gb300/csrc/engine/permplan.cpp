@@ -72,7 +72,10 @@ PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, co
   {
     std::lock_guard<std::mutex> lk(ctx.mu);
     auto it = ctx.perm_cache.find(key);
-    if (it != ctx.perm_cache.end()) return it->second;
+    if (it != ctx.perm_cache.end()) {
+      ctx.keep_alive(it->second);
+      return it->second;
+    }
   }
   std::vector<PermSub> subs = build_perm_subs(src, dst, rsp);
   return finish_plan(ctx, key, subs, src.elem_num);
@@ -205,7 +208,10 @@ PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& ds
   {
     std::lock_guard<std::mutex> lk(ctx.mu);
     auto it = ctx.perm_cache.find(key);
-    if (it != ctx.perm_cache.end()) return it->second;
+    if (it != ctx.perm_cache.end()) {
+      ctx.keep_alive(it->second);
+      return it->second;
+    }
   }
   std::vector<PermSub> subs;
   for (const auto& bi : src.blocks) {
@@ -276,6 +282,7 @@ static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermS
   std::lock_guard<std::mutex> lk(ctx.mu);
   if (ctx.perm_cache.size() > 4096) ctx.perm_cache.clear();
   ctx.perm_cache[key] = plan;
+  ctx.keep_alive(plan);
   return plan;
 }
 

@@ -68,10 +68,35 @@ __device__ __forceinline__ void fp64_tile(const GemmTile& t, const double* __res
   }
 }
 
+// The last CTA to finish a split tile sums the group's partial tiles in split
+// order (deterministic) and resets the group's counter for the next launch.
+__device__ __forceinline__ void finish_split(const GemmTile& t, const double* __restrict__ ws, double* __restrict__ C,
+                                             int* __restrict__ counters) {
+  __shared__ int last;
+  __threadfence();  // this thread's partial entries are visible device-wide
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&counters[t.grp], 1) == t.nsplit - 1;
+  __syncthreads();
+  if (last) {
+    __threadfence();
+    const double* p = ws + t.ws_off;
+    for (int e = threadIdx.x; e < kTileElems; e += blockDim.x) {
+      const int r = e / t.tn, c = e % t.tn;
+      const int m = t.m0 + r, n = t.n0 + c;
+      if (m >= t.M || n >= t.N) continue;
+      double s = 0.0;
+      for (int k = 0; k < t.nsplit; k++) s += __ldcg(p + (int64_t)k * kTileElems + e);
+      C[t.c_off + (int64_t)m * t.N + n] = s;
+    }
+    if (threadIdx.x == 0) counters[t.grp] = 0;
+  }
+  __syncthreads();  // `last` is rewritten by the next item
+}
+
 __global__ void __launch_bounds__(128) gemm_fp64_kernel(const GemmTile* __restrict__ tiles, int ntiles,
                                                         const double* __restrict__ A,
                                                         const double* __restrict__ B, double* __restrict__ C,
-                                                        double* __restrict__ ws) {
+                                                        double* __restrict__ ws, int* __restrict__ counters) {
   for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
     const GemmTile t = tiles[it];
     switch (t.tn) {
@@ -80,6 +105,7 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(const GemmTile* __restri
       case 16: fp64_tile<16>(t, A, B, C, ws); break;
       default: fp64_tile<32>(t, A, B, C, ws); break;
     }
+    if (counters && t.nsplit > 1) finish_split(t, ws, C, counters);
   }
 }
 
@@ -104,9 +130,9 @@ __global__ void __launch_bounds__(kTileElems) splitk_reduce_kernel(const GemmTil
 }  // namespace
 
 void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const double* B, double* C, double* ws,
-                      int grid, cudaStream_t s) {
+                      int* counters, int grid, cudaStream_t s) {
   if (ntiles <= 0) return;
-  gemm_fp64_kernel<<<grid, 128, 0, s>>>(tiles, ntiles, A, B, C, ws);
+  gemm_fp64_kernel<<<grid, 128, 0, s>>>(tiles, ntiles, A, B, C, ws, counters);
   TN_CUDA(cudaGetLastError());
 }
 

@@ -468,6 +468,7 @@ void Network::drop_graph() {
   if (graph) cudaGraphDestroy((cudaGraph_t)graph);
   graph_exec = nullptr;
   graph = nullptr;
+  graph_keep.clear();
 }
 
 void Network::capture() {
@@ -492,11 +493,14 @@ void Network::capture() {
     cudaStreamDestroy(cap);
     TN_CUDA(began);
   }
+  c.keep = &graph_keep;  // plans and workspace the recorded kernels read
   try {
     UniTensor r = launch();
     TN_CUDA(cudaMemcpyAsync(graph_out.getElem(), r.getElem(), r.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
                             cap));
   } catch (...) {
+    c.keep = nullptr;
+    graph_keep.clear();
     cudaStreamEndCapture(cap, &g);
     if (g) cudaGraphDestroy(g);
     c.stream = orig;
@@ -504,6 +508,7 @@ void Network::capture() {
     cudaGetLastError();
     throw;
   }
+  c.keep = nullptr;
   cudaError_t ended = cudaStreamEndCapture(cap, &g);
   c.stream = orig;
   cudaStreamDestroy(cap);
