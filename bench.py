@@ -187,9 +187,9 @@ def _time_steps(torch, stream, flush, steps, fn):
 
 def _timed_with_clocks(torch, stream, flush, steps, fn, gpu, min_seconds=1.0, max_reps=400):
     """Repeats the timed region (exactly `steps` steps, CUDA events) until the
-    clock sampler has seen at least 3 samples and min_seconds have passed;
-    returns the median ms per step over the repetitions, their count and the
-    clocks sampled while they ran."""
+    clock sampler has seen at least 3 samples and min_seconds have passed
+    (min_seconds 0: one repetition); returns the median ms per step over the
+    repetitions, their count and the clocks sampled while they ran."""
     reps = []
     with ClockSampler(gpu) as clk:
         clk.wait_samples(1, 10.0)
@@ -197,7 +197,7 @@ def _timed_with_clocks(torch, stream, flush, steps, fn, gpu, min_seconds=1.0, ma
         t0 = time.time()
         while len(reps) < max_reps:
             reps.append(_time_steps(torch, stream, flush, steps, fn))
-            if time.time() - t0 >= min_seconds and len(clk.lines) - n0 >= 3:
+            if min_seconds <= 0 or (time.time() - t0 >= min_seconds and len(clk.lines) - n0 >= 3):
                 break
         clk.lines = clk.lines[n0:]
     return statistics.median(reps), len(reps), clk.summary()
@@ -234,7 +234,8 @@ def gpu_main(args, rank, local, world):
             torch.distributed.barrier()
         torch.cuda.synchronize()
         l0 = tu.launch_count()
-        ms_graph, reps, clocks = _timed_with_clocks(torch, stream, flush, args.steps, net.replay, local)
+        ms_graph, reps, clocks = _timed_with_clocks(torch, stream, flush, args.steps, net.replay, local,
+                                                    min_seconds=args.clock_seconds)
         launches = (tu.launch_count() - l0) // (args.steps * reps)
         ms_eager = _time_steps(torch, stream, flush, args.steps, lambda: net.launch(mode))
         # per-kernel times: eager pass with events around every launch
@@ -697,6 +698,8 @@ def main():
     ap.add_argument("--mode", default="split", choices=["fp64", "split", "bf16"])
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--clock-seconds", type=float, default=1.0,
+                    help="repeat the timed region for at least this long while SM clocks are sampled (0: once)")
     ap.add_argument("--workload", default="itebd", choices=["itebd", "permute", "mera", "batched", "ipeps"])
     ap.add_argument("--chi-ctm", type=int, default=128)
     ap.add_argument("--D", type=int, default=8)
