@@ -119,6 +119,14 @@ int tn_permute(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, const int* rsp, const
 int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host, double* dst_host,
                           int64_t* written);
 
+/* Host-side check of the operand views a contraction uses instead of this
+ * permute when the FP64 kernel can read the source in place (every
+ * sub-block of the result a row-major view of the source): builds the
+ * permuted elements on the CPU through the views alone.  *applies is 0 (and
+ * nothing is written) when the permute has no such views. */
+int tn_plan_check_views(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host, double* dst_host,
+                        int* applies);
+
 /* ---- grouped sector GEMMs (contract's per-sector matrixMul) ------------
  * All n sector GEMMs in one launch; list is a host array.  A, B, C device. */
 int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A,

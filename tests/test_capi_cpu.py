@@ -54,6 +54,39 @@ def test_sectormap_and_permute_plan_match_reference(case):
     assert np.array_equal(got, G.arr(case["id"], "P"))
 
 
+@pytest.mark.parametrize("case", PERM, ids=[c["id"] for c in PERM])
+def test_operand_views_match_reference_permute(case):
+    """Where a permute's result is a set of row-major views of its source
+    (what the FP64 GEMM reads in place of the permuted copy), the views
+    rebuild the reference's permuted elements exactly."""
+    bonds = G.bonds_of(case["T"])
+    src = tu.SectorMap(bonds)
+    labels, new = case["T"]["labels"], case["new_labels"]
+    rsp = [labels.index(l) for l in new]
+    out = [wl.change(bonds[rsp[b]], 1 if b < case["rownum"] else -1) for b in range(len(bonds))]
+    dst = tu.SectorMap(out)
+    got = tu.plan_check_views(src, dst, rsp, G.arr(case["id"], "T"))
+    if got is not None:
+        assert np.array_equal(got, G.arr(case["id"], "P"))
+
+
+def test_operand_views_cover_the_itebd_regroups():
+    """The iTEBD network's regroups (one physical state per charge) are views."""
+    spec = wl.itebd()
+    A = next(s for s in spec["tensors"] if s.name == "A")
+    x = np.arange(wl.elem_count(A.bonds), dtype=np.float64)
+    src = tu.SectorMap(A.bonds)
+    for rn, rsp in [(1, [0, 1, 2]), (2, [0, 1, 2])]:
+        out = [wl.change(A.bonds[rsp[b]], 1 if b < rn else -1) for b in range(3)]
+        dst = tu.SectorMap(out)
+        want, _ = tu.plan_check_permute(src, dst, rsp, x)
+        got = tu.plan_check_views(src, dst, rsp, x)
+        if rn == 2:
+            assert got is not None and np.array_equal(got, x)  # no move at all
+        else:
+            assert got is not None and np.array_equal(got, want)
+
+
 def test_permute_plans_of_workloads_bit_exact():
     rng = np.random.default_rng(7)
     # workload 1's permute, the iTEBD tensors' contract permutes, MERA chi=6

@@ -62,6 +62,7 @@ _PROTOS = {
     "tn_sectormap_destroy": (_I, [_P]),
     "tn_permute": (_I, [_P, _P, _P, _IP, _DP, _DP]),
     "tn_plan_check_permute": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
+    "tn_plan_check_views": (_I, [_P, _P, _IP, _DP, _DP, _IP]),
     "tn_contract_sectors": (_I, [_P, _I, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
     "tn_autotune": (_I, [_P, _I, _I64P]),
     "tn_contract_sectors_fp64_noalloc": (_I, [_P, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),

@@ -244,6 +244,45 @@ int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const do
   });
 }
 
+int tn_plan_check_views(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host, double* dst_host,
+                        int* applies) {
+  return guard([&] {
+    need(src, "src");
+    need(dst, "dst");
+    need(rsp, "rsp");
+    need(applies, "applies");
+    std::vector<int> r(rsp, rsp + src->m->bonds.size());
+    tn::OpViewsP v = tn::build_op_views(*src->m, *dst->m, r);
+    *applies = v->ok ? 1 : 0;
+    if (!v->ok) return;
+    const tn::SectorMap& D = *dst->m;
+    const int64_t n = D.elem_num;
+    std::vector<unsigned char> hit(n, 0);
+    for (size_t bo = 0; bo < D.blocks.size(); bo++) {
+      const auto& B = D.blocks[bo];
+      const tn::ViewHdr& h = v->hdrs[v->hdr_of_block[bo]];
+      const int64_t* rs = v->pool.data() + h.rs;
+      const int64_t* cs = v->pool.data() + h.cs;
+      for (int i = 0; i < h.nr; i++)
+        for (int j = 0; j < h.nc; j++) {
+          const int64_t base = v->pool[h.tab + 2 * ((int64_t)i * h.nc + j)];
+          const int64_t ld = v->pool[h.tab + 2 * ((int64_t)i * h.nc + j) + 1];
+          for (int64_t r0 = rs[i]; r0 < rs[i + 1]; r0++)
+            for (int64_t c0 = cs[j]; c0 < cs[j + 1]; c0++) {
+              const int64_t so = base + (r0 - rs[i]) * ld + (c0 - cs[j]);
+              const int64_t d = B.off + r0 * B.cols + c0;
+              if (so < 0 || so >= src->m->elem_num || d < 0 || d >= n)
+                tn::fail(TN_ERR_ARG, "view check: offset out of range");
+              if (hit[d]++) tn::fail(TN_ERR_ARG, "view check: destination covered twice");
+              dst_host[d] = src_host[so];
+            }
+        }
+    }
+    for (int64_t d = 0; d < n; d++)
+      if (!hit[d]) tn::fail(TN_ERR_ARG, "view check: destination element not covered");
+  });
+}
+
 int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A, const double* B,
                         double* C) {
   return guard([&] {

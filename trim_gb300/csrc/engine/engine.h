@@ -145,6 +145,7 @@ struct GemmTile {
   int32_t nsplit;
   int32_t tn;                   // tile columns: 32, 16, 8 or 4 (512/tn rows)
   int32_t grp;                  // split group (one per split output tile), -1 if nsplit==1
+  int32_t a_vw, b_vw;           // operand views (ViewHdr index), -1: contiguous row-major
   int64_t ws_off;               // partial-tile slot in the workspace (elements), -1 if nsplit==1
 };
 
@@ -156,6 +157,22 @@ struct Fp64Policy {
   int items_per_sm = 8;
   bool operator==(const Fp64Policy& o) const { return tn_rule == o.tn_rule && items_per_sm == o.items_per_sm; }
 };
+
+// A permuted operand read in place by the FP64 GEMM (the permute fused into
+// the operand load).  Every sub-block (row tuple i, column tuple j) of a
+// destination block must be a plain row-major view of the source: element
+// (r, c) of the sub-block at source offset base + r * ld + c.
+struct ViewHdr {
+  int32_t nr, nc;       // row and column tuples of the block
+  int64_t rs, cs, tab;  // pool offsets: row starts [nr+1], column starts [nc+1], (base, ld) pairs [nr*nc]
+};
+struct OpViews {
+  bool ok = false;                // false: some sub-block is not a view (or carries a sign)
+  std::vector<int> hdr_of_block;  // destination block -> header
+  std::vector<ViewHdr> hdrs;
+  std::vector<int64_t> pool;
+};
+using OpViewsP = std::shared_ptr<const OpViews>;
 
 // Tensor-core sector GEMM (split precision / fast BF16): one contraction's
 // sectors, their slice images in the workspace and their scale exponents.
@@ -270,6 +287,7 @@ struct Ctx {
   bool autotune = false;            // FP64 GEMM policies timed per sector histogram
   std::unordered_map<uint64_t, Fp64Policy> tuned;
   std::unordered_map<uint64_t, std::shared_ptr<void>> svd_cache;  // SVD batch plans
+  std::unordered_map<std::string, OpViewsP> view_cache;           // operand views per permute
 };
 Ctx* default_ctx();  // lazily created context on the current device
 void release_ctx(Ctx* c);     // syncs and frees everything a context holds (not the Ctx)
@@ -292,6 +310,17 @@ uint64_t hash_list(const std::vector<tn_sector_gemm>& list, int tag);
 // sector GEMMs: C_i = A_i . B_i for every item, all in one grouped launch
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A,
                       const double* B, double* C);
+// operand views of a permute (cached; ->ok false when it cannot be fused)
+OpViewsP get_op_views(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
+std::shared_ptr<OpViews> build_op_views(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
+// true when these sectors run on the FP64 kernel in this mode (views apply)
+bool sectors_on_fp64(int mode, const std::vector<tn_sector_gemm>& list);
+// the FP64 grouped GEMM with operands read through views: va / vb may be
+// null (contiguous operand); a_blk[i] / b_blk[i] name the view block of
+// sector i; A / B are then the unpermuted source buffers
+void run_sector_gemms_views(Ctx& ctx, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
+                            double* C, const OpViewsP& va, const std::vector<int>& a_blk, const OpViewsP& vb,
+                            const std::vector<int>& b_blk);
 
 // FP64 tile plan: 512-entry output tiles shaped to each sector's width, K
 // split to the policy's items per SM; with ws_cap_elems >= 0 the split is
@@ -307,7 +336,8 @@ void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int n
 // split tiles need launch_splitk_reduce afterwards; otherwise the last CTA of
 // each split group sums its partial tiles in split order and resets the counter
 void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const double* B, double* C,
-                      double* ws, int* counters, int grid, cudaStream_t s);
+                      double* ws, int* counters, const ViewHdr* views, const int64_t* pool, int grid,
+                      cudaStream_t s);
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
                           cudaStream_t s);
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s);

@@ -23,7 +23,8 @@ int tile_width(int64_t N, const Fp64Policy& pol) {
 }
 
 std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, int num_sms, bool allow_split,
-                                      int64_t* ws_elems, const Fp64Policy& pol) {
+                                      int64_t* ws_elems, const Fp64Policy& pol,
+                                      const std::vector<std::pair<int, int>>* vw = nullptr) {
   // K is split so that no work item (one tile over a K range) carries much
   // more than total / (SMs x items_per_sm), with at least ~4 items per SM
   int64_t tiles = 0;
@@ -39,7 +40,8 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
   const double kmax = std::max(64.0, work / (double)target_items);  // K per item
   std::vector<GemmTile> out;
   int64_t ws = 0, ngrp = 0;
-  for (const auto& g : list) {
+  for (size_t gi = 0; gi < list.size(); gi++) {
+    const auto& g = list[gi];
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX || g.N > INT32_MAX || g.K > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large");
     const int tn = tile_width(g.N, pol), tm = kTileElems / tn;
@@ -76,6 +78,8 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
           t.nsplit = nsplit;
           t.tn = tn;
           t.grp = nsplit > 1 ? (int32_t)ngrp : -1;
+          t.a_vw = vw ? (*vw)[gi].first : -1;
+          t.b_vw = vw ? (*vw)[gi].second : -1;
           t.ws_off = slot;
           out.push_back(t);
         }
@@ -96,6 +100,8 @@ std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num
 
 struct Fp64Plan {
   std::vector<tn_sector_gemm> list;
+  std::vector<std::pair<int, int>> vw;  // operand view ids per sector (empty: contiguous operands)
+  const void* table = nullptr;          // the view table the ids index
   Fp64Policy pol;
   DevBufP tiles;
   DevBufP counters;  // one per split group, zero between launches
@@ -105,14 +111,21 @@ struct Fp64Plan {
 };
 
 static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list,
-                                               const Fp64Policy& pol) {
-  const uint64_t key = hash_list(list, 64 + 16 * pol.tn_rule + pol.items_per_sm);
+                                               const Fp64Policy& pol,
+                                               const std::vector<std::pair<int, int>>* vw = nullptr,
+                                               const void* table = nullptr) {
+  uint64_t key = hash_list(list, 64 + 16 * pol.tn_rule + pol.items_per_sm);
+  if (vw) {
+    for (const auto& v : *vw) key = (key ^ (uint64_t)(uint32_t)v.first ^ ((uint64_t)(uint32_t)v.second << 32)) * 1099511628211ull;
+    key ^= (uint64_t)(uintptr_t)table;
+  }
   {
     std::lock_guard<std::mutex> lk(ctx.mu);
     auto it = ctx.gemm_cache.find(key);
     if (it != ctx.gemm_cache.end()) {
       auto P = std::static_pointer_cast<Fp64Plan>(it->second);
-      if (P->pol == pol && P->list.size() == list.size() &&
+      const bool same_vw = vw ? (P->vw == *vw && P->table == table) : P->vw.empty();
+      if (same_vw && P->pol == pol && P->list.size() == list.size() &&
           std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0) {
         ctx.keep_alive(P);
         return P;
@@ -122,7 +135,11 @@ static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_se
   auto P = std::make_shared<Fp64Plan>();
   P->list = list;
   P->pol = pol;
-  std::vector<GemmTile> tiles = plan_fp64(list, ctx.num_sms, -1, &P->ws_elems, pol);
+  if (vw) {
+    P->vw = *vw;
+    P->table = table;
+  }
+  std::vector<GemmTile> tiles = plan_fp64_split(list, ctx.num_sms, true, &P->ws_elems, pol, vw);
   P->ntiles = (int)tiles.size();
   for (const auto& g : list) {
     P->flops += 2.0 * g.M * g.N * g.K;
@@ -147,7 +164,8 @@ static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_se
   return P;
 }
 
-static void launch_fp64_plan(Ctx& ctx, const Fp64Plan& P, const double* A, const double* B, double* C) {
+static void launch_fp64_plan(Ctx& ctx, const Fp64Plan& P, const double* A, const double* B, double* C,
+                             const ViewHdr* views = nullptr, const int64_t* pool = nullptr) {
   double* ws = nullptr;
   if (P.ws_elems > 0) ws = (double*)ctx.ensure_workspace(P.ws_elems * sizeof(double))->ptr;
   int grid = (int)std::min<int64_t>((int64_t)P.ntiles, (int64_t)ctx.num_sms * 16);
@@ -155,7 +173,7 @@ static void launch_fp64_plan(Ctx& ctx, const Fp64Plan& P, const double* A, const
     // split tiles are summed by the last CTA of each group (no second launch)
     ProfScope ps(ctx, "gemm_fp64", P.bytes, P.flops);
     launch_gemm_fp64((const GemmTile*)P.tiles->ptr, P.ntiles, A, B, C, ws,
-                     P.counters ? (int*)P.counters->ptr : nullptr, grid, ctx.stream);
+                     P.counters ? (int*)P.counters->ptr : nullptr, views, pool, grid, ctx.stream);
     ctx.launched();
   }
 }
@@ -256,6 +274,92 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
 // multiply-adds -- and sectors the 128 x 64 tensor tiles would pad four-fold
 // or more (M < 32 or N < 16) to the FP64 kernel, which is exact and for those
 // shapes no slower; the rest goes to the tcgen05 kernel.
+// the tensor-core modes' routing rule (see run_sector_gemms): true for a
+// sector the FP64 kernel takes
+static bool small_sector(const tn_sector_gemm& g, double total) {
+  return total < 5.0e7 || g.K < 16 || g.M < 32 || g.N < 16 || (double)g.M * g.N * g.K < 16384.0;
+}
+
+bool sectors_on_fp64(int mode, const std::vector<tn_sector_gemm>& list) {
+  const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0;
+  mode &= ~TN_MODE_TC_ONLY;
+  if (mode == TN_MODE_FP64) return true;
+  if (tc_only) return false;
+  double total = 0;
+  for (const auto& g : list) total += 2.0 * g.M * g.N * g.K;
+  for (const auto& g : list)
+    if (!small_sector(g, total)) return false;
+  return true;
+}
+
+// The views of one contraction's two operands as one device table.
+struct ViewTable {
+  DevBufP hdrs, pool;
+  int na = 0;  // headers of the A operand come first
+};
+
+static std::shared_ptr<ViewTable> get_view_table(Ctx& ctx, const OpViewsP& va, const OpViewsP& vb) {
+  const std::string key = "VT#" + std::to_string((uintptr_t)va.get()) + "#" + std::to_string((uintptr_t)vb.get());
+  const uint64_t hk = std::hash<std::string>()(key);
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.gemm_cache.find(hk);
+    if (it != ctx.gemm_cache.end()) {
+      auto T = std::static_pointer_cast<ViewTable>(it->second);
+      ctx.keep_alive(T);
+      return T;
+    }
+  }
+  auto T = std::make_shared<ViewTable>();
+  std::vector<ViewHdr> hdrs;
+  std::vector<int64_t> pool;
+  if (va) {
+    hdrs = va->hdrs;
+    pool = va->pool;
+  }
+  T->na = (int)hdrs.size();
+  if (vb) {
+    const int64_t shift = (int64_t)pool.size();
+    for (ViewHdr h : vb->hdrs) {
+      h.rs += shift;
+      h.cs += shift;
+      h.tab += shift;
+      hdrs.push_back(h);
+    }
+    pool.insert(pool.end(), vb->pool.begin(), vb->pool.end());
+  }
+  T->hdrs = std::make_shared<DevBuf>(hdrs.size() * sizeof(ViewHdr), ctx);
+  T->pool = std::make_shared<DevBuf>(pool.size() * sizeof(int64_t), ctx);
+  TN_CUDA(cudaMemcpyAsync(T->hdrs->ptr, hdrs.data(), hdrs.size() * sizeof(ViewHdr), cudaMemcpyHostToDevice,
+                          ctx.stream));
+  TN_CUDA(cudaMemcpyAsync(T->pool->ptr, pool.data(), pool.size() * sizeof(int64_t), cudaMemcpyHostToDevice,
+                          ctx.stream));
+  TN_CUDA(cudaStreamSynchronize(ctx.stream));  // the host copies die here
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  ctx.gemm_cache[hk] = T;  // the OpViews behind the two keys are cached for good
+  ctx.keep_alive(T);
+  return T;
+}
+
+void run_sector_gemms_views(Ctx& ctx, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
+                            double* C, const OpViewsP& va, const std::vector<int>& a_blk, const OpViewsP& vb,
+                            const std::vector<int>& b_blk) {
+  if (list.empty()) return;
+  if (!va && !vb) {
+    run_fp64(ctx, list, A, B, C);
+    return;
+  }
+  auto T = get_view_table(ctx, va, vb);
+  std::vector<std::pair<int, int>> vw(list.size(), {-1, -1});
+  for (size_t i = 0; i < list.size(); i++) {
+    if (va) vw[i].first = va->hdr_of_block.at(a_blk.at(i));
+    if (vb) vw[i].second = T->na + vb->hdr_of_block.at(b_blk.at(i));
+  }
+  auto P = get_fp64_plan(ctx, list, Fp64Policy(), &vw, T.get());
+  if (!P->ntiles) return;
+  launch_fp64_plan(ctx, *P, A, B, C, (const ViewHdr*)T->hdrs->ptr, (const int64_t*)T->pool->ptr);
+}
+
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
                       double* C) {
   if (list.empty()) return;
@@ -271,8 +375,7 @@ void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& lis
   for (const auto& g : list) total += 2.0 * g.M * g.N * g.K;
   std::vector<tn_sector_gemm> tc, f64;
   for (const auto& g : list) {
-    const bool small = !tc_only && (total < 5.0e7 || g.K < 16 || g.M < 32 || g.N < 16 ||
-                                     (double)g.M * g.N * g.K < 16384.0);
+    const bool small = !tc_only && small_sector(g, total);
     (small ? f64 : tc).push_back(g);
   }
   if (!f64.empty()) run_fp64(ctx, f64, A, B, C);

@@ -200,6 +200,132 @@ std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst,
   return subs;
 }
 
+// Operand views of a permute (the permute fused into the FP64 GEMM's operand
+// load): for every source sub-block, the destination column digits must be
+// unit-stride contiguous in the source and the destination row digits must
+// form one row stride, so the destination sub-block is the row-major view
+// (base, ld) of the source; no sub-block may carry a fermionic sign.  The
+// views are grouped per destination block by row and column tuple.
+std::shared_ptr<OpViews> build_op_views(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp) {
+  auto V = std::make_shared<OpViews>();
+  const int n = (int)src.bonds.size();
+  if ((int)dst.bonds.size() != n || (int)rsp.size() != n || src.elem_num != dst.elem_num) return V;
+  std::vector<int64_t> qot_acc(n, 1);
+  for (int b = n - 1; b > 0; b--) qot_acc[b - 1] = qot_acc[b] * (int64_t)dst.bonds[b].q.size();
+  const int rbn_in = src.rbond_num, rbn_out = dst.rbond_num;
+  bool symmetric = false, odd = false;
+  for (const auto& b : src.bonds) {
+    if (b.q.size() != 1) symmetric = true;
+    for (const auto& q : b.q) odd |= q.prtf != 0;
+  }
+  std::vector<std::pair<int, int>> swaps;
+  if (symmetric && odd) swaps = fermion_swaps(n, rbn_in, rbn_out, rsp);
+  struct SB {
+    int64_t rot, cot, base, ld;
+  };
+  std::vector<std::vector<SB>> per_block(dst.blocks.size());
+  std::vector<int> qin(n), deg(n);
+  std::vector<int64_t> ss(n);
+  for (int64_t qidx : src.qidx_enc) {
+    int64_t tmp = qidx;
+    for (int b = n - 1; b >= 0; b--) {
+      const int64_t qd = (int64_t)src.bonds[b].q.size();
+      qin[b] = (int)(tmp % qd);
+      deg[b] = src.bonds[b].deg[qin[b]];
+      tmp /= qd;
+    }
+    int64_t qot = 0;
+    for (int b = 0; b < n; b++) qot += (int64_t)qin[rsp[b]] * qot_acc[b];
+    const int64_t rin = qidx / src.cqdim, cin = qidx % src.cqdim;
+    const int64_t rot = qot / dst.cqdim, cot = qot % dst.cqdim;
+    const int bi = src.rq2blk[rin], bo = dst.rq2blk[rot];
+    if (bi < 0 || bo < 0 || dst.cq2off[cot] < 0) return V;
+    int parity = 0;
+    for (const auto& sw : swaps)
+      parity ^= src.bonds[sw.first].q[qin[sw.first]].prtf & src.bonds[sw.second].q[qin[sw.second]].prtf;
+    if (parity) return V;
+    const auto& Bi = src.blocks[bi];
+    int64_t acc = 1;
+    for (int b = rbn_in - 1; b >= 0; b--) { ss[b] = acc * Bi.cols; acc *= deg[b]; }
+    acc = 1;
+    for (int b = n - 1; b >= rbn_in; b--) { ss[b] = acc; acc *= deg[b]; }
+    int64_t expect = 1;
+    for (int j = n - 1; j >= rbn_out; j--) {  // columns: unit stride, contiguous
+      const int b = rsp[j];
+      if (deg[b] == 1) continue;
+      if (ss[b] != expect) return V;
+      expect *= deg[b];
+    }
+    int64_t ld = -1;
+    for (int j = rbn_out - 1; j >= 0; j--) {  // rows: one stride
+      const int b = rsp[j];
+      if (deg[b] == 1) continue;
+      if (ld < 0) {
+        ld = ss[b];
+      } else if (ss[b] != expect) {
+        return V;
+      }
+      expect = ss[b] * deg[b];
+    }
+    per_block[bo].push_back(SB{rot, cot, Bi.off + src.rq2off[rin] * Bi.cols + src.cq2off[cin], ld < 0 ? 0 : ld});
+  }
+  V->hdr_of_block.assign(dst.blocks.size(), -1);
+  for (size_t bo = 0; bo < dst.blocks.size(); bo++) {
+    auto& v = per_block[bo];
+    std::vector<int64_t> rots, cots;
+    for (const auto& x : v) {
+      rots.push_back(x.rot);
+      cots.push_back(x.cot);
+    }
+    std::sort(rots.begin(), rots.end(), [&](int64_t a, int64_t b) { return dst.rq2off[a] < dst.rq2off[b]; });
+    rots.erase(std::unique(rots.begin(), rots.end()), rots.end());
+    std::sort(cots.begin(), cots.end(), [&](int64_t a, int64_t b) { return dst.cq2off[a] < dst.cq2off[b]; });
+    cots.erase(std::unique(cots.begin(), cots.end()), cots.end());
+    const int nr = (int)rots.size(), nc = (int)cots.size();
+    if ((size_t)nr * nc != v.size() || nr == 0) return V;  // every tuple pair of the block is a sub-block
+    ViewHdr h;
+    h.nr = nr;
+    h.nc = nc;
+    h.rs = (int64_t)V->pool.size();
+    for (int64_t r : rots) V->pool.push_back(dst.rq2off[r]);
+    V->pool.push_back(dst.blocks[bo].rows);
+    h.cs = (int64_t)V->pool.size();
+    for (int64_t c : cots) V->pool.push_back(dst.cq2off[c]);
+    V->pool.push_back(dst.blocks[bo].cols);
+    h.tab = (int64_t)V->pool.size();
+    V->pool.resize(V->pool.size() + 2 * (size_t)nr * nc, -1);
+    for (const auto& x : v) {
+      const int i = (int)(std::lower_bound(rots.begin(), rots.end(), x.rot,
+                                           [&](int64_t a, int64_t b) { return dst.rq2off[a] < dst.rq2off[b]; }) -
+                          rots.begin());
+      const int j = (int)(std::lower_bound(cots.begin(), cots.end(), x.cot,
+                                           [&](int64_t a, int64_t b) { return dst.cq2off[a] < dst.cq2off[b]; }) -
+                          cots.begin());
+      V->pool[h.tab + 2 * ((int64_t)i * nc + j)] = x.base;
+      V->pool[h.tab + 2 * ((int64_t)i * nc + j) + 1] = x.ld;
+    }
+    V->hdr_of_block[bo] = (int)V->hdrs.size();
+    V->hdrs.push_back(h);
+  }
+  V->ok = true;
+  return V;
+}
+
+OpViewsP get_op_views(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp) {
+  std::string key = src.key + "#" + dst.key + "#";
+  for (int r : rsp) key += std::to_string(r) + ",";
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.view_cache.find(key);
+    if (it != ctx.view_cache.end()) return it->second;
+  }
+  OpViewsP v = build_op_views(src, dst, rsp);
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  if (ctx.view_cache.size() > 4096) ctx.view_cache.clear();
+  ctx.view_cache[key] = v;
+  return v;
+}
+
 // Block-wise transpose of UniTensor::transpose (UniTensorReal.cpp:448-506):
 // block q of the source (R x C, row-major) becomes block q of the destination
 // (C x R).  One 2-D copy per block.

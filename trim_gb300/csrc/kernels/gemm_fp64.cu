@@ -3,6 +3,10 @@
 // row-major dgemm, numeric/lapack/lib/uni10_lapack_cpu.cpp:41-44) in one
 // launch over a device work list of output tiles.
 //
+// An operand may be read through views of its unpermuted source (the permute
+// fused into the operand load, see ViewHdr): K is then walked in segments
+// (the contracted bonds' charge tuples), each a plain row-major view.
+//
 // On GB300 the FP64 pipe (~1.2 TFLOP/s for the whole chip) is the bound, not
 // memory, so no FMA lane may be spent on padding: an output tile has 512
 // entries laid out to the sector's width, tn = 32, 16, 8 or 4 columns by
@@ -18,10 +22,23 @@ namespace {
 
 constexpr int kTileElems = 512, kRowsPerLane = 4;
 
+__device__ __forceinline__ int find_start(const int64_t* __restrict__ st, int n, int64_t v) {
+  int lo = 0, hi = n - 1;  // largest i with st[i] <= v
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (st[mid] <= v)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
 template <int TN>
 __device__ __forceinline__ void fp64_tile(const GemmTile& t, const double* __restrict__ A,
                                           const double* __restrict__ B, double* __restrict__ C,
-                                          double* __restrict__ ws) {
+                                          double* __restrict__ ws, const ViewHdr* __restrict__ views,
+                                          const int64_t* __restrict__ pool) {
   constexpr int LR = 32 / TN;               // lane rows of a warp
   constexpr int WM = LR * kRowsPerLane;     // rows of a warp
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -34,24 +51,57 @@ __device__ __forceinline__ void fp64_tile(const GemmTile& t, const double* __res
   const int slots = rem <= 0 ? 0 : min(kRowsPerLane, (rem + LR - 1) / LR);
   double acc[kRowsPerLane] = {0.0, 0.0, 0.0, 0.0};
   if (slots > 0) {
-    const double* a[kRowsPerLane];
+    int mrow[kRowsPerLane];
 #pragma unroll
-    for (int i = 0; i < kRowsPerLane; i++) {
-      const int m = min(wm0 + rl + i * LR, t.M - 1);  // rows past M read row M-1, results dropped
-      a[i] = A + t.a_off + (int64_t)m * t.K;
-    }
-    const double* b = B + t.b_off + (nvalid ? n : 0);
-    if (slots == kRowsPerLane) {
-      for (int k = t.k0; k < t.k1; k++) {
-        const double bv = nvalid ? __ldg(b + (int64_t)k * t.N) : 0.0;
+    for (int i = 0; i < kRowsPerLane; i++) mrow[i] = min(wm0 + rl + i * LR, t.M - 1);  // rows past M: dropped
+    const ViewHdr* av = t.a_vw >= 0 ? views + t.a_vw : nullptr;
+    const ViewHdr* bv = t.b_vw >= 0 ? views + t.b_vw : nullptr;
+    // K is walked in segments: the column tuples of a viewed A (the row
+    // tuples of a viewed B are the same), else one segment
+    const int64_t* seg = av ? pool + av->cs : (bv ? pool + bv->rs : nullptr);
+    const int nseg = av ? av->nc : (bv ? bv->nr : 1);
+    int ri[kRowsPerLane];
 #pragma unroll
-        for (int i = 0; i < kRowsPerLane; i++) acc[i] = fma(__ldg(a[i] + k), bv, acc[i]);
+    for (int i = 0; i < kRowsPerLane; i++) ri[i] = av ? find_start(pool + av->rs, av->nr, mrow[i]) : 0;
+    const int ncol = nvalid ? n : 0;
+    const int cj = bv ? find_start(pool + bv->cs, bv->nc, ncol) : 0;
+    int sidx = seg ? find_start(seg, nseg, t.k0) : 0;
+    for (int k0 = t.k0; k0 < t.k1; sidx++) {
+      const int k1 = seg ? (int)min((int64_t)t.k1, seg[sidx + 1]) : t.k1;
+      const int64_t s0 = seg ? seg[sidx] : 0;
+      // element k of row i is A[ao[i] + k]; element k of this lane's column is B[bo + k * ldb]
+      int64_t ao[kRowsPerLane];
+#pragma unroll
+      for (int i = 0; i < kRowsPerLane; i++) {
+        if (av) {
+          const int64_t* pr = pool + av->tab + 2 * ((int64_t)ri[i] * av->nc + sidx);
+          ao[i] = pr[0] + (mrow[i] - pool[av->rs + ri[i]]) * pr[1] - s0;
+        } else {
+          ao[i] = t.a_off + (int64_t)mrow[i] * t.K;
+        }
       }
-    } else {
-      for (int k = t.k0; k < t.k1; k++) {
-        const double bv = nvalid ? __ldg(b + (int64_t)k * t.N) : 0.0;
-        for (int i = 0; i < slots; i++) acc[i] = fma(__ldg(a[i] + k), bv, acc[i]);
+      int64_t bo, ldb;
+      if (bv) {
+        const int64_t* pr = pool + bv->tab + 2 * ((int64_t)sidx * bv->nc + cj);
+        ldb = pr[1];
+        bo = pr[0] + (ncol - pool[bv->cs + cj]) - s0 * ldb;
+      } else {
+        ldb = t.N;
+        bo = t.b_off + ncol;
       }
+      if (slots == kRowsPerLane) {
+        for (int k = k0; k < k1; k++) {
+          const double bval = nvalid ? __ldg(B + bo + (int64_t)k * ldb) : 0.0;
+#pragma unroll
+          for (int i = 0; i < kRowsPerLane; i++) acc[i] = fma(__ldg(A + ao[i] + k), bval, acc[i]);
+        }
+      } else {
+        for (int k = k0; k < k1; k++) {
+          const double bval = nvalid ? __ldg(B + bo + (int64_t)k * ldb) : 0.0;
+          for (int i = 0; i < slots; i++) acc[i] = fma(__ldg(A + ao[i] + k), bval, acc[i]);
+        }
+      }
+      k0 = k1;
     }
   }
   if (t.nsplit == 1) {
@@ -96,14 +146,16 @@ __device__ __forceinline__ void finish_split(const GemmTile& t, const double* __
 __global__ void __launch_bounds__(128) gemm_fp64_kernel(const GemmTile* __restrict__ tiles, int ntiles,
                                                         const double* __restrict__ A,
                                                         const double* __restrict__ B, double* __restrict__ C,
-                                                        double* __restrict__ ws, int* __restrict__ counters) {
+                                                        double* __restrict__ ws, int* __restrict__ counters,
+                                                        const ViewHdr* __restrict__ views,
+                                                        const int64_t* __restrict__ pool) {
   for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
     const GemmTile t = tiles[it];
     switch (t.tn) {
-      case 4: fp64_tile<4>(t, A, B, C, ws); break;
-      case 8: fp64_tile<8>(t, A, B, C, ws); break;
-      case 16: fp64_tile<16>(t, A, B, C, ws); break;
-      default: fp64_tile<32>(t, A, B, C, ws); break;
+      case 4: fp64_tile<4>(t, A, B, C, ws, views, pool); break;
+      case 8: fp64_tile<8>(t, A, B, C, ws, views, pool); break;
+      case 16: fp64_tile<16>(t, A, B, C, ws, views, pool); break;
+      default: fp64_tile<32>(t, A, B, C, ws, views, pool); break;
     }
     if (counters && t.nsplit > 1) finish_split(t, ws, C, counters);
   }
@@ -130,9 +182,9 @@ __global__ void __launch_bounds__(kTileElems) splitk_reduce_kernel(const GemmTil
 }  // namespace
 
 void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const double* B, double* C, double* ws,
-                      int* counters, int grid, cudaStream_t s) {
+                      int* counters, const ViewHdr* views, const int64_t* pool, int grid, cudaStream_t s) {
   if (ntiles <= 0) return;
-  gemm_fp64_kernel<<<grid, 128, 0, s>>>(tiles, ntiles, A, B, C, ws, counters);
+  gemm_fp64_kernel<<<grid, 128, 0, s>>>(tiles, ntiles, A, B, C, ws, counters, views, pool);
   TN_CUDA(cudaGetLastError());
 }
 

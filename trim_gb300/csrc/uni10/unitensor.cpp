@@ -528,6 +528,39 @@ UniTensor contract_const(const UniTensor& Ta, const UniTensor& Tb) {
   return UniTensor::contract_impl(const_cast<UniTensor&>(Ta), const_cast<UniTensor&>(Tb), true, false);
 }
 
+// The bonds and sector map a permute would produce, without its data.
+struct PermShape {
+  std::vector<Bond> bonds;
+  std::shared_ptr<const tn::SectorMap> smap;
+  std::vector<int> rsp;
+  bool moves = false;  // false: the permute is a no-op (same order and row count)
+};
+
+static PermShape permuted_shape(const UniTensor& src, const std::vector<int>& newLabels, int rowBondNum) {
+  PermShape p;
+  const std::vector<int> labels = src.label();
+  const int n = (int)labels.size();
+  if ((int)newLabels.size() != n)
+    throw std::runtime_error("The size of the input new labels does not match for the number of bonds.");
+  p.rsp.assign(n, 0);
+  int cnt = 0;
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < n; j++)
+      if (labels[i] == newLabels[j]) {
+        p.rsp[j] = i;
+        cnt++;
+      }
+  if (cnt != n) throw std::runtime_error("The input new labels do not 1-1 correspond to the labels of the tensor.");
+  bool inorder = true;
+  for (int i = 0; i < n; i++) inorder &= p.rsp[i] == i;
+  p.moves = !(inorder && (int)src.inBondNum() == rowBondNum);
+  const std::vector<Bond> b = src.bond();
+  for (int j = 0; j < n; j++) p.bonds.push_back(b[p.rsp[j]]);
+  for (int j = 0; j < n; j++) p.bonds[j].change(j < rowBondNum ? BD_IN : BD_OUT);
+  p.smap = tn::get_sectormap(to_sigs(p.bonds));  // cached per signature
+  return p;
+}
+
 // mutate: permute the operands in place like the reference (restored unless
 // fast); otherwise the permuted operands are temporaries and Ta, Tb are
 // never written.
@@ -567,27 +600,27 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
         newLabelC.push_back(Tb.labels[b]);
       }
     const int conBond = (int)interLabel.size();
-    UniTensor pa, pb;
-    if (mutate) {
-      Ta.permute(newLabelA, an - conBond);
-      Tb.permute(newLabelB, conBond);
-    } else {
-      pa = permuted(Ta, newLabelA, an - conBond);
-      pb = permuted(Tb, newLabelB, conBond);
-    }
-    const UniTensor& A_ = mutate ? Ta : pa;
-    const UniTensor& B_ = mutate ? Tb : pb;
+    // The permuted operands' shapes (bonds and sector maps) come first; the
+    // data of an operand is permuted only when the FP64 GEMM cannot read it
+    // in place through views of the source (the permute fused into the
+    // operand load: every sector on the FP64 kernel, operands left as they
+    // were, every sub-block a row-major view of the source).
+    tn::Ctx& c = C();
+    PermShape sa = permuted_shape(Ta, newLabelA, an - conBond);
+    PermShape sb = permuted_shape(Tb, newLabelB, conBond);
     std::vector<Bond> cBonds;
-    for (int i = 0; i < an - conBond; i++) cBonds.push_back(A_.bonds[i]);
-    for (int i = conBond; i < bn; i++) cBonds.push_back(B_.bonds[i]);
+    for (int i = 0; i < an - conBond; i++) cBonds.push_back(sa.bonds[i]);
+    for (int i = conBond; i < bn; i++) cBonds.push_back(sb.bonds[i]);
     UniTensor Tc(cBonds);
     if (!cBonds.empty()) Tc.setLabel(newLabelC);
     // every block of Ta with a block of the same charge in Tb is one sector GEMM
     std::vector<tn_sector_gemm> list;
-    const tn::SectorMap* ma = A_.smap.get();
-    const tn::SectorMap* mb = B_.smap.get();
+    std::vector<int> a_blk, b_blk;
+    const tn::SectorMap* ma = sa.smap.get();
+    const tn::SectorMap* mb = sb.smap.get();
     const tn::SectorMap* mc = Tc.smap.get();
-    for (const auto& ba : ma->blocks) {
+    for (size_t ia = 0; ia < ma->blocks.size(); ia++) {
+      const auto& ba = ma->blocks[ia];
       int ib = mb->find_block(ba.q);
       if (ib < 0) continue;
       const auto& bb = mb->blocks[ib];
@@ -604,8 +637,49 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
       g.b_off = bb.off;
       g.c_off = mc ? mc->blocks[ic].off : 0;
       list.push_back(g);
+      a_blk.push_back((int)ia);
+      b_blk.push_back(ib);
     }
-    tn::run_sector_gemms(C(), g_mode, list, dptr(A_.elem), dptr(B_.elem), dptr(Tc.elem));
+    tn::OpViewsP va, vb;
+    if ((!mutate || !fast) && tn::sectors_on_fp64(g_mode, list)) {
+      if (sa.moves) va = tn::get_op_views(c, *Ta.smap, *sa.smap, sa.rsp);
+      if (sb.moves) vb = tn::get_op_views(c, *Tb.smap, *sb.smap, sb.rsp);
+      if (va && !va->ok) va.reset();
+      if (vb && !vb->ok) vb.reset();
+      if (va && vb)  // the K segments of both views must agree (the contracted bonds' tuples)
+        for (size_t i = 0; i < list.size() && vb; i++) {
+          const tn::ViewHdr& ha = va->hdrs[va->hdr_of_block[a_blk[i]]];
+          const tn::ViewHdr& hb = vb->hdrs[vb->hdr_of_block[b_blk[i]]];
+          if (ha.nc != hb.nr || !std::equal(va->pool.begin() + ha.cs, va->pool.begin() + ha.cs + ha.nc + 1,
+                                            vb->pool.begin() + hb.rs))
+            vb.reset();
+        }
+    }
+    UniTensor pa, pb;
+    const double* Ap = dptr(Ta.elem);
+    const double* Bp = dptr(Tb.elem);
+    if (sa.moves && !va) {
+      if (mutate) {
+        Ta.permute(newLabelA, an - conBond);
+        Ap = dptr(Ta.elem);
+      } else {
+        pa = permuted(Ta, newLabelA, an - conBond);
+        Ap = dptr(pa.elem);
+      }
+    }
+    if (sb.moves && !vb) {
+      if (mutate) {
+        Tb.permute(newLabelB, conBond);
+        Bp = dptr(Tb.elem);
+      } else {
+        pb = permuted(Tb, newLabelB, conBond);
+        Bp = dptr(pb.elem);
+      }
+    }
+    if (va || vb)
+      tn::run_sector_gemms_views(c, list, Ap, Bp, dptr(Tc.elem), va, a_blk, vb, b_blk);
+    else
+      tn::run_sector_gemms(c, g_mode, list, Ap, Bp, dptr(Tc.elem));
     Tc.status |= UniTensor::HAVEELEM;
     if (conBond == 0) {  // outer product (UniTensorTools.cpp:206-225)
       int idx = 0;
@@ -618,6 +692,9 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
     if (mutate && !fast) {
       Ta.permute(oldLabelA, oldRnumA);
       Tb.permute(oldLabelB, oldRnumB);
+    } else if (mutate) {  // fast: the operands stay permuted (UniTensorTools.cpp:227-230)
+      Ta.permute(newLabelA, an - conBond);
+      Tb.permute(newLabelB, conBond);
     }
     return Tc;
   } else if (Ta.status & UniTensor::HAVEBOND) {

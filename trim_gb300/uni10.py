@@ -51,6 +51,17 @@ def plan_check_permute(src: SectorMap, dst: SectorMap, rsp, src_host: np.ndarray
     return d, w.value
 
 
+def plan_check_views(src: SectorMap, dst: SectorMap, rsp, src_host: np.ndarray):
+    """Build the permuted elements on the CPU through the operand views the
+    FP64 GEMM would read instead of the permuted copy; None when the permute
+    has no such views."""
+    s = np.ascontiguousarray(src_host, dtype=np.float64)
+    d = np.full(dst.elem_num, np.nan)
+    ok = C.c_int()
+    call("tn_plan_check_views", src.h, dst.h, int_array(rsp), s.ctypes.data, d.ctypes.data, C.byref(ok))
+    return d if ok.value else None
+
+
 def permute_device(src: SectorMap, dst: SectorMap, rsp, src_ptr: int, dst_ptr: int) -> None:
     call("tn_permute", None, src.h, dst.h, int_array(rsp), src_ptr, dst_ptr)
 
