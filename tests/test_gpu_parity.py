@@ -66,6 +66,34 @@ def test_contract_fp64(tu, case):
     assert a.labels() == case["A"]["labels"]
 
 
+def test_contract_output_blocks_without_sectors_are_zero(tu):
+    """A[x|k] . B[k|y] where k carries charges A's rows reach but B's columns
+    do not: output blocks with no sector GEMM stay zero, as the reference's
+    zero-filled result does; the other blocks match the oracle."""
+    x = wl.u1_bond(1, (-1, 0, 1), (2, 3, 2))
+    k = wl.u1_bond(-1, (-1, 0), (1, 2))  # no charge 1: output block 1 has no sector
+    y = wl.u1_bond(-1, (0, 1), (2, 3))
+    a_bonds, b_bonds = [x, k], [wl.change(k, 1), y]
+    rng = np.random.default_rng(31)
+    ea = rng.uniform(-1, 1, wl.elem_count(a_bonds))
+    eb = rng.uniform(-1, 1, wl.elem_count(b_bonds))
+    la, lb = [1, 2], [2, 3]
+    for fused in (False, True):  # with and without an operand permute in front
+        a = tu.UniTensor(a_bonds, la, ea)
+        b = tu.UniTensor(b_bonds, lb, eb)
+        if fused:
+            a.permute([2, 1], 1)  # the contraction permutes it back (a view)
+        c = tu.contract(a, b, fast=False, mode="fp64")
+        oa = st.UniTensor(to_obonds(a_bonds), la, ea)
+        if fused:
+            oa.permute([2, 1], 1)
+        ob = st.UniTensor(to_obonds(b_bonds), lb, eb)
+        oc = st.contract(oa, ob)
+        assert c.labels() == oc.labels
+        assert rel(c.get_elem(), oc.elem) <= FP64_TOL
+        assert np.count_nonzero(oc.elem == 0.0) > 0  # the case has a block without a sector
+
+
 def test_workload1_permute_and_contract(tu):
     c = G.cases()["u1_rank4"]
     spec = wl.u1_rank4()

@@ -611,14 +611,13 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
     std::vector<Bond> cBonds;
     for (int i = 0; i < an - conBond; i++) cBonds.push_back(sa.bonds[i]);
     for (int i = conBond; i < bn; i++) cBonds.push_back(sb.bonds[i]);
-    UniTensor Tc(cBonds);
-    if (!cBonds.empty()) Tc.setLabel(newLabelC);
     // every block of Ta with a block of the same charge in Tb is one sector GEMM
     std::vector<tn_sector_gemm> list;
     std::vector<int> a_blk, b_blk;
     const tn::SectorMap* ma = sa.smap.get();
     const tn::SectorMap* mb = sb.smap.get();
-    const tn::SectorMap* mc = Tc.smap.get();
+    std::shared_ptr<const tn::SectorMap> mcs = cBonds.empty() ? nullptr : tn::get_sectormap(to_sigs(cBonds));
+    const tn::SectorMap* mc = mcs.get();
     for (size_t ia = 0; ia < ma->blocks.size(); ia++) {
       const auto& ba = ma->blocks[ia];
       int ib = mb->find_block(ba.q);
@@ -640,6 +639,10 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
       a_blk.push_back((int)ia);
       b_blk.push_back(ib);
     }
+    // the reference zeroes the result first (UniTensorTools.cpp:185); only
+    // blocks no sector GEMM writes need it
+    UniTensor Tc = (!mc || list.size() == mc->blocks.size()) ? UniTensor(cBonds, "", NoFill{}) : UniTensor(cBonds);
+    if (!cBonds.empty()) Tc.setLabel(newLabelC);
     tn::OpViewsP va, vb;
     if ((!mutate || !fast) && tn::sectors_on_fp64(g_mode, list)) {
       if (sa.moves) va = tn::get_op_views(c, *Ta.smap, *sa.smap, sa.rsp);
@@ -767,11 +770,10 @@ void UniTensor::prepare_contract(const UniTensor& Ta, const UniTensor& Tb, Contr
   std::vector<Bond> cBonds;
   for (int i = 0; i < an - conBond; i++) cBonds.push_back(w.pa.bonds[i]);
   for (int i = conBond; i < bn; i++) cBonds.push_back(w.pb.bonds[i]);
-  w.tc = UniTensor(cBonds);
-  if (!cBonds.empty()) w.tc.setLabel(newLabelC);
   const tn::SectorMap* ma = w.pa.smap.get();
   const tn::SectorMap* mb = w.pb.smap.get();
-  const tn::SectorMap* mc = w.tc.smap.get();
+  std::shared_ptr<const tn::SectorMap> mcs = cBonds.empty() ? nullptr : tn::get_sectormap(to_sigs(cBonds));
+  const tn::SectorMap* mc = mcs.get();
   for (const auto& ba : ma->blocks) {
     int ib = mb->find_block(ba.q);
     if (ib < 0) continue;
@@ -783,6 +785,9 @@ void UniTensor::prepare_contract(const UniTensor& Ta, const UniTensor& Tb, Contr
       throw std::runtime_error("The dimensions the bonds to be contracted out are different.");
     w.sectors.push_back(tn_sector_gemm{ba.rows, bb.cols, ba.cols, ba.off, bb.off, mc ? mc->blocks[ic].off : 0});
   }
+  // only blocks no sector GEMM writes need the reference's zero fill
+  w.tc = (!mc || w.sectors.size() == mc->blocks.size()) ? UniTensor(cBonds, "", NoFill{}) : UniTensor(cBonds);
+  if (!cBonds.empty()) w.tc.setLabel(newLabelC);
   w.outer = conBond == 0;
   if (w.outer) {
     const int ra = Ta.RBondNum, rb = Tb.RBondNum;
