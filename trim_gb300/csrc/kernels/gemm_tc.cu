@@ -393,55 +393,58 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
     }
   } else if (warp == 1) {
     // ------------------------------------------------ MMA issue
-    if (lane == 0) {
-      const uint32_t idesc = idesc_bf16_f32(kTM, kTN);
-      uint32_t na = 0, nb = 0, nchunk = 0;
-      bool ok = true;
-      for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
-        const int4 w = items[it];
-        const TcSector& S = secs[w.x];
-        const int kb = w.w * S.kts, ke = min(S.nkt, kb + S.kts);
-        for (int k0 = kb; k0 < ke && ok; k0 += kChunk) {
-          const int k1 = min(ke, k0 + kChunk);
-          if (!mbar_wait(&sh.acc_empty, (nchunk & 1) ^ 1, &sh.abort)) { ok = false; break; }
+    // The whole warp runs the loop (every lane waits on the barriers and the
+    // outcome is made warp-uniform); one elected lane issues the MMAs and commits.
+    const uint32_t idesc = idesc_bf16_f32(kTM, kTN);
+    uint32_t na = 0, nb = 0, nchunk = 0;
+    bool ok = true;
+    for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+      const int4 w = items[it];
+      const TcSector& S = secs[w.x];
+      const int kb = w.w * S.kts, ke = min(S.nkt, kb + S.kts);
+      for (int k0 = kb; k0 < ke && ok; k0 += kChunk) {
+        const int k1 = min(ke, k0 + kChunk);
+        if (!__all_sync(0xffffffffu, mbar_wait(&sh.acc_empty, (nchunk & 1) ^ 1, &sh.abort))) { ok = false; break; }
+        tc_fence_after();
+        uint32_t touched = 0;
+        for (int kt = k0; kt < k1 && ok; kt++) {
+          const int sb = nb % kBRing;
+          if (!__all_sync(0xffffffffu, mbar_wait(&sh.fullB[sb], (nb / kBRing) & 1, &sh.abort))) { ok = false; break; }
           tc_fence_after();
-          uint32_t touched = 0;
-          for (int kt = k0; kt < k1 && ok; kt++) {
-            const int sb = nb % kBRing;
-            if (!mbar_wait(&sh.fullB[sb], (nb / kBRing) & 1, &sh.abort)) { ok = false; break; }
-            tc_fence_after();
-            const uint32_t b_addr = smem_u32(bbuf + sb * NS * kBTile);
-            for (int s = 0; s < NS; s++) {
-              const int sa = na % kARing;
-              if (!mbar_wait(&sh.fullA[sa], (na / kARing) & 1, &sh.abort)) { ok = false; break; }
-              tc_fence_after();
-              const uint64_t adesc = desc_sw128(smem_u32(abuf + sa * kATile));
-              for (int t = 0; t < NS && s + t <= (NS == 1 ? 0 : kMaxLevel); t++) {
-                const int lvl = min(s + t, LV - 1);
-                const uint64_t bdesc = desc_sw128(b_addr + t * kBTile);
-                const uint32_t d = tmem + lvl * kTN;
-#pragma unroll
-                for (int kk = 0; kk < kTK / 16; kk++) {
-                  // advancing K by 16 bf16 = 32 bytes inside the swizzle atom: +2 in the address field
-                  mma_bf16(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
-                  touched |= 1u << lvl;
-                }
-              }
-              mma_commit(&sh.emptyA[sa]);
-              na++;
+          const uint32_t b_addr = smem_u32(bbuf + sb * NS * kBTile);
+          for (int s = 0; s < NS; s++) {
+            const int sa = na % kARing;
+            if (!__all_sync(0xffffffffu, mbar_wait(&sh.fullA[sa], (na / kARing) & 1, &sh.abort))) {
+              ok = false;
+              break;
             }
-            mma_commit(&sh.emptyB[sb]);
-            nb++;
+            tc_fence_after();
+            const uint64_t adesc = desc_sw128(smem_u32(abuf + sa * kATile));
+            for (int t = 0; t < NS && s + t <= (NS == 1 ? 0 : kMaxLevel); t++) {
+              const int lvl = min(s + t, LV - 1);
+              const uint64_t bdesc = desc_sw128(b_addr + t * kBTile);
+              const uint32_t d = tmem + lvl * kTN;
+#pragma unroll
+              for (int kk = 0; kk < kTK / 16; kk++) {
+                // advancing K by 16 bf16 = 32 bytes inside the swizzle atom: +2 in the address field
+                mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
+                touched |= 1u << lvl;
+              }
+            }
+            mma_commit_elect(&sh.emptyA[sa]);
+            na++;
           }
-          mma_commit(&sh.acc_full);
-          nchunk++;
+          mma_commit_elect(&sh.emptyB[sb]);
+          nb++;
         }
+        mma_commit_elect(&sh.acc_full);
+        nchunk++;
       }
-      if (!ok) raise_timeout(sh, err);
-      // every MMA issued must complete before the tensor memory is released
-      mma_commit(&sh.mma_done);
-      mbar_wait(&sh.mma_done, 0, &sh.abort);
     }
+    if (!ok && lane == 0) raise_timeout(sh, err);
+    // every MMA issued must complete before the tensor memory is released
+    mma_commit_elect(&sh.mma_done);
+    mbar_wait(&sh.mma_done, 0, &sh.abort);
   } else {
     // ------------------------------------------------ epilogue
     const int quad = warp & 3;  // TMEM lanes 32*quad .. +31
