@@ -55,10 +55,17 @@ enum {
   TN_MODE_FAST_BF16 = 2, /* one BF16 slice, FP32 accumulation */
   TN_MODE_FAST_TF32 = 3, /* TF32 operands, FP32 accumulation */
   /* flag: in the tensor-core modes, send every sector to the tensor cores
-   * (by default a contraction under 5e7 FLOP, or a sector with K < 16,
-   * M < 32, N < 16 or under 16K multiply-adds, runs on the exact FP64
+   * (by default a sector with K < 16 or N < 16 runs on the exact FP64
    * kernel instead) */
-  TN_MODE_TC_ONLY = 0x100
+  TN_MODE_TC_ONLY = 0x100,
+  /* flags choosing the tensor-core form (by default: fused while every
+   * sector has K <= 576 and the contraction has at most 4 output tiles of
+   * 128 x 64 per SM, tiled above that).
+   * Fused: one launch, each CTA slices the operands of its own tile.
+   * Tiled: operand maxima and slices once per contraction, then the
+   * pipelined GEMM over pre-sliced tiles (3 launches). */
+  TN_MODE_TC_FUSED = 0x200,
+  TN_MODE_TC_TILED = 0x400
 };
 
 typedef struct tn_ctx_s* tn_ctx_t;

@@ -59,24 +59,55 @@ def _grouped(env, mode, shapes, seed, dist="uniform"):
     return errs
 
 
-def test_split_single_tile(env):
-    errs = _grouped(env, "split_tc", [(128, 64, 64)], 1)
+# the tensor-core forms: chosen by size, fused (one launch, per-item slicing)
+# and tiled (maxima + slices once, pipelined GEMM)
+SPLIT_FORMS = ("split_tc", "split_fused", "split_tiled")
+
+
+@pytest.mark.parametrize("mode", SPLIT_FORMS)
+def test_split_single_tile(env, mode):
+    errs = _grouped(env, mode, [(128, 64, 64)], 1)
     assert errs[0] <= SPLIT_TOL, errs
 
 
-def test_split_ragged_shapes(env):
+@pytest.mark.parametrize("mode", SPLIT_FORMS)
+def test_split_ragged_shapes(env, mode):
     shapes = [(1, 1, 1), (2, 3, 5), (33, 17, 9), (130, 70, 65), (127, 63, 129)]
-    errs = _grouped(env, "split_tc", shapes, 2)
+    errs = _grouped(env, mode, shapes, 2)
     assert max(errs) <= SPLIT_TOL, errs
 
 
-def test_split_long_k_chunks(env):
-    # several 256-k exact-accumulation chunks and a Gaussian operand
-    errs = _grouped(env, "split_tc", [(200, 150, 700), (64, 64, 3000)], 3, dist="normal")
+@pytest.mark.parametrize("mode", SPLIT_FORMS)
+def test_split_long_k_chunks(env, mode):
+    # several 576-k exact-accumulation chunks, drained into double-float
+    # (tiled) or 64-bit fixed point (fused); a Gaussian operand
+    errs = _grouped(env, mode, [(200, 150, 700), (64, 64, 3000)], 3, dist="normal")
     assert max(errs) <= SPLIT_TOL, errs
 
 
-def test_split_wide_dynamic_range(env):
+def test_split_fused_more_items_than_ctas(env):
+    # 16 x 11 + 3 x 2 + 11 = 193 output tiles on at most one CTA per SM: CTAs
+    # loop over tiles; K of 200 and 129 walks several 64-k blocks after a
+    # scale pass; repeated calls agree bit for bit
+    shapes = [(2000, 700, 200), (300, 70, 129), (5, 700, 64)]
+    torch, capi, tu = env
+    first = _grouped(env, "split_fused", shapes, 6)
+    assert max(first) <= SPLIT_TOL, first
+    gemms, na, nb, nc = _sectors(shapes)
+    rng = np.random.default_rng(7)
+    A = torch.from_numpy(rng.uniform(-1, 1, na)).cuda()
+    B = torch.from_numpy(rng.uniform(-1, 1, nb)).cuda()
+    outs = []
+    for _ in range(3):
+        Cd = torch.zeros(nc, dtype=torch.float64, device="cuda")
+        tu.contract_sectors("split_fused", gemms, A.data_ptr(), B.data_ptr(), Cd.data_ptr())
+        tu.sync()
+        outs.append(Cd.cpu().numpy())
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[0], outs[2])
+
+
+@pytest.mark.parametrize("mode", SPLIT_FORMS)
+def test_split_wide_dynamic_range(env, mode):
     torch, capi, tu = env
     m, n, k = 96, 80, 300
     rng = np.random.default_rng(4)
@@ -85,7 +116,7 @@ def test_split_wide_dynamic_range(env):
     A = torch.from_numpy(a.ravel()).cuda()
     B = torch.from_numpy(b.ravel()).cuda()
     Cd = torch.zeros(m * n, dtype=torch.float64, device="cuda")
-    tu.contract_sectors("split_tc", [(m, n, k, 0, 0, 0)], A.data_ptr(), B.data_ptr(), Cd.data_ptr())
+    tu.contract_sectors(mode, [(m, n, k, 0, 0, 0)], A.data_ptr(), B.data_ptr(), Cd.data_ptr())
     tu.sync()
     c = Cd.cpu().numpy().reshape(m, n)
     want = a @ b
@@ -97,8 +128,9 @@ def test_split_wide_dynamic_range(env):
     assert rel(c, want) <= SPLIT_TOL
 
 
-def test_fast_bf16_reports_bf16_level_error(env):
-    errs = _grouped(env, "bf16_tc", [(128, 64, 256), (50, 40, 30)], 5)
+@pytest.mark.parametrize("mode", ("bf16_tc", "bf16_fused", "bf16_tiled"))
+def test_fast_bf16_reports_bf16_level_error(env, mode):
+    errs = _grouped(env, mode, [(128, 64, 256), (50, 40, 30)], 5)
     assert max(errs) <= 1e-2, errs
 
 
@@ -122,7 +154,7 @@ def test_split_itebd_network(env):
         t = tu.UniTensor(s.bonds, s.labels, els[s.name])
         keep.append(t)
         net.put_tensor(s.name, t)
-    for mode in ("split", "split_tc"):
+    for mode in ("split", "split_tc", "split_fused", "split_tiled"):
         th = net.launch(mode=mode)
         assert rel(th.get_elem(), G.arr("itebd", "TH")) <= SPLIT_TOL, mode
 

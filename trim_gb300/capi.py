@@ -18,9 +18,14 @@ HEADER = os.path.join(ROOT, "include", "trim_gb300.h")
 TN_OK = 0
 TN_ERR = {1: "ARG", 2: "OOM", 3: "TIMEOUT", 4: "CUDA", 5: "SHAPE", 6: "LABEL", 7: "UNSUPPORTED", 8: "NOBLOCK", 9: "FILE"}
 MODE_FP64, MODE_SPLIT, MODE_FAST_BF16, MODE_FAST_TF32 = 0, 1, 2, 3
-MODE_TC_ONLY = 0x100
+MODE_TC_ONLY, MODE_TC_FUSED, MODE_TC_TILED = 0x100, 0x200, 0x400
 MODES = {"fp64": MODE_FP64, "split": MODE_SPLIT, "bf16": MODE_FAST_BF16, "tf32": MODE_FAST_TF32,
-         "split_tc": MODE_SPLIT | MODE_TC_ONLY, "bf16_tc": MODE_FAST_BF16 | MODE_TC_ONLY}
+         "split_tc": MODE_SPLIT | MODE_TC_ONLY, "bf16_tc": MODE_FAST_BF16 | MODE_TC_ONLY,
+         # every sector on the tensor cores, in one form
+         "split_fused": MODE_SPLIT | MODE_TC_ONLY | MODE_TC_FUSED,
+         "split_tiled": MODE_SPLIT | MODE_TC_ONLY | MODE_TC_TILED,
+         "bf16_fused": MODE_FAST_BF16 | MODE_TC_ONLY | MODE_TC_FUSED,
+         "bf16_tiled": MODE_FAST_BF16 | MODE_TC_ONLY | MODE_TC_TILED}
 
 
 class TnError(RuntimeError):

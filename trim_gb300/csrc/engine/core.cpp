@@ -284,6 +284,7 @@ void release_ctx(Ctx* c) {
   c->perm_cache.clear();
   c->gemm_cache.clear();
   c->tc_cache.clear();
+  c->fused_cache.clear();
   c->svd_cache.clear();
   c->workspace.reset();
   c->err_word.reset();

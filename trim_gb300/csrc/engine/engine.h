@@ -259,7 +259,7 @@ struct Ctx {
   int64_t launches = 0;
   std::mutex mu;
   std::unordered_map<std::string, PermPlanP> perm_cache;
-  std::unordered_map<uint64_t, std::shared_ptr<void>> gemm_cache, tc_cache;  // device work lists
+  std::unordered_map<uint64_t, std::shared_ptr<void>> gemm_cache, tc_cache, fused_cache;  // device work lists
   std::unordered_map<std::string, SectorMapP> smap_refs;  // keep cached maps alive per ctx
   DevBufP workspace;  // scratch for split-K partial tiles and operand slices
   DevBufP ensure_workspace(size_t bytes);
@@ -348,6 +348,13 @@ size_t tc_gemm_smem(int ns);
 void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems, const uint8_t* ws,
                     const unsigned long long* ea, const unsigned long long* eb, double* C, double* part, int* err,
                     int grid, cudaStream_t s);
+// Fused form for contractions of small sectors: one launch per contraction,
+// one CTA per 128 x 64 output tile (items: sector, row tile, column tile),
+// which slices its operands 64 k at a time into shared memory and runs the
+// digit products; levels are summed as 64-bit fixed point, exactly.
+size_t tc_fused_smem(int ns);
+void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems, const double* A, const double* B,
+                     double* C, int* err, int grid, cudaStream_t s);
 // C tile = sum over the K ranges of its FP64 partial tiles, in range order
 void launch_tc_reduce(const TcSector* secs, const int4* ritems, int nred, const double* part, double* C, int grid,
                       cudaStream_t s);

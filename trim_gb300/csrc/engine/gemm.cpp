@@ -276,19 +276,31 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
 // shapes no slower; the rest goes to the tcgen05 kernel.
 // the tensor-core modes' routing rule (see run_sector_gemms): true for a
 // sector the FP64 kernel takes
-static bool small_sector(const tn_sector_gemm& g, double total) {
-  return total < 5.0e7 || g.K < 16 || g.M < 32 || g.N < 16 || (double)g.M * g.N * g.K < 16384.0;
+void run_tc_fused(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
+                  double* C);
+int64_t fused_items(const std::vector<tn_sector_gemm>& list);
+
+constexpr int kModeFlags = TN_MODE_TC_ONLY | TN_MODE_TC_FUSED | TN_MODE_TC_TILED;
+
+// A sector too thin for a 128 x 64 x 16 MMA step to pay: in the tiled form
+// it stays on the exact FP64 kernel (unless TN_MODE_TC_ONLY).
+static bool thin_sector(const tn_sector_gemm& g) { return g.K < 16 || g.N < 16; }
+
+// The fused form fits a contraction of a few 128 x 64 output tiles per SM
+// whose sectors all have short K (its CTAs walk K serially).
+static bool fused_fits(const Ctx& ctx, const std::vector<tn_sector_gemm>& list) {
+  for (const auto& g : list)
+    if (g.K > 576) return false;
+  return fused_items(list) <= 4 * (int64_t)ctx.num_sms;
 }
 
 bool sectors_on_fp64(int mode, const std::vector<tn_sector_gemm>& list) {
-  const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0;
-  mode &= ~TN_MODE_TC_ONLY;
+  const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0, want_fused = (mode & TN_MODE_TC_FUSED) != 0;
+  mode &= ~kModeFlags;
   if (mode == TN_MODE_FP64) return true;
-  if (tc_only) return false;
-  double total = 0;
-  for (const auto& g : list) total += 2.0 * g.M * g.N * g.K;
+  if (tc_only || want_fused) return false;
   for (const auto& g : list)
-    if (!small_sector(g, total)) return false;
+    if (!thin_sector(g)) return false;
   return true;
 }
 
@@ -364,22 +376,31 @@ void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& lis
                       double* C) {
   if (list.empty()) return;
   const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0;
-  mode &= ~TN_MODE_TC_ONLY;
+  const bool want_fused = (mode & TN_MODE_TC_FUSED) != 0, want_tiled = (mode & TN_MODE_TC_TILED) != 0;
+  mode &= ~kModeFlags;
   if (mode == TN_MODE_FP64) {
     run_fp64(ctx, list, A, B, C);
     return;
   }
   if (mode == TN_MODE_FAST_TF32) fail(TN_ERR_UNSUPPORTED, "TF32 fast mode is not built; use TN_MODE_FAST_BF16");
   if (mode != TN_MODE_SPLIT && mode != TN_MODE_FAST_BF16) fail(TN_ERR_ARG, "unknown contraction mode");
-  double total = 0;
-  for (const auto& g : list) total += 2.0 * g.M * g.N * g.K;
-  std::vector<tn_sector_gemm> tc, f64;
-  for (const auto& g : list) {
-    const bool small = !tc_only && small_sector(g, total);
-    (small ? f64 : tc).push_back(g);
+  if (want_fused && want_tiled) fail(TN_ERR_ARG, "TN_MODE_TC_FUSED and TN_MODE_TC_TILED exclude each other");
+  const int ns = mode == TN_MODE_SPLIT ? 7 : 1;
+  if (!want_tiled && (want_fused || fused_fits(ctx, list))) {
+    // one fused launch for every sector, thin ones included (they cost a CTA
+    // each, side by side with the rest) -- unless all of them are thin
+    bool all_thin = !tc_only;
+    for (const auto& g : list) all_thin = all_thin && thin_sector(g);
+    if (all_thin && !want_fused)
+      run_fp64(ctx, list, A, B, C);
+    else
+      run_tc_fused(ctx, ns, list, A, B, C);
+    return;
   }
+  std::vector<tn_sector_gemm> tc, f64;
+  for (const auto& g : list) (!tc_only && thin_sector(g) ? f64 : tc).push_back(g);
   if (!f64.empty()) run_fp64(ctx, f64, A, B, C);
-  if (!tc.empty()) run_tc_gemms(ctx, mode == TN_MODE_SPLIT ? 7 : 1, tc, A, B, C);
+  if (!tc.empty()) run_tc_gemms(ctx, ns, tc, A, B, C);
 }
 
 }  // namespace tn

@@ -198,4 +198,109 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
   }
 }
 
+// ---------------------------------------------------------------- fused form
+// One launch per contraction: one item per (sector, 128-row tile, 64-column
+// tile); the CTA walks the sector's K itself.
+struct FusedPlan {
+  std::vector<tn_sector_gemm> list;
+  int ns = 7;
+  DevBufP meta;
+  size_t off_it = 0;
+  int nsec = 0, nitems = 0;
+  double flops = 0, in_bytes = 0;
+};
+
+constexpr int64_t kFusedMaxK = 8192;
+
+int64_t fused_items(const std::vector<tn_sector_gemm>& list) {
+  int64_t n = 0;
+  for (const auto& g : list)
+    if (g.M > 0 && g.N > 0 && g.K > 0) n += cdiv(g.M, kTM) * cdiv(g.N, kTN);
+  return n;
+}
+
+static std::shared_ptr<FusedPlan> build_fused_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns) {
+  auto P = std::make_shared<FusedPlan>();
+  P->list = list;
+  P->ns = ns;
+  std::vector<TcSector> secs;
+  std::vector<int4> items;
+  for (const auto& g : list) {
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
+    if (g.M > INT32_MAX / 2 || g.N > INT32_MAX / 2)
+      fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large for the tensor-core path");
+    if (g.K > kFusedMaxK)
+      fail(TN_ERR_UNSUPPORTED, "the fused tensor-core form sums K <= 8192 in 64-bit fixed point; use the tiled form");
+    TcSector s;
+    std::memset(&s, 0, sizeof(s));
+    s.a_off = g.a_off;
+    s.b_off = g.b_off;
+    s.c_off = g.c_off;
+    s.M = (int32_t)g.M;
+    s.N = (int32_t)g.N;
+    s.K = (int32_t)g.K;
+    s.nmt = (int32_t)cdiv(g.M, kTM);
+    s.nnt = (int32_t)cdiv(g.N, kTN);
+    s.nkt = (int32_t)cdiv(g.K, kTK);
+    s.nsplit = 1;
+    s.kts = s.nkt;
+    s.p_off = -1;
+    const int idx = (int)secs.size();
+    secs.push_back(s);
+    for (int mt = 0; mt < s.nmt; mt++)
+      for (int nt = 0; nt < s.nnt; nt++) items.push_back(make_int4(idx, mt, nt, 0));
+    P->flops += 2.0 * g.M * g.N * g.K;
+    P->in_bytes += 8.0 * ((double)g.M * g.K + (double)g.K * g.N);
+  }
+  // longest K first: the CTAs that walk the most 64-k blocks start first
+  std::stable_sort(items.begin(), items.end(),
+                   [&](const int4& x, const int4& y) { return secs[x.x].nkt > secs[y.x].nkt; });
+  P->nsec = (int)secs.size();
+  P->nitems = (int)items.size();
+  if (!P->nsec) return P;
+  P->off_it = (P->nsec * sizeof(TcSector) + 15) & ~(size_t)15;
+  const size_t bytes = P->off_it + items.size() * sizeof(int4);
+  std::vector<uint8_t> meta(bytes);
+  std::memcpy(meta.data(), secs.data(), P->nsec * sizeof(TcSector));
+  std::memcpy(meta.data() + P->off_it, items.data(), items.size() * sizeof(int4));
+  P->meta = std::make_shared<DevBuf>(bytes, ctx);
+  TN_CUDA(cudaMemcpyAsync(P->meta->ptr, meta.data(), bytes, cudaMemcpyHostToDevice, ctx.stream));
+  TN_CUDA(cudaStreamSynchronize(ctx.stream));  // the host copy dies here
+  return P;
+}
+
+static std::shared_ptr<FusedPlan> get_fused_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns) {
+  const uint64_t key = hash_list(list, 200 + ns);
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.fused_cache.find(key);
+    if (it != ctx.fused_cache.end()) {
+      auto P = std::static_pointer_cast<FusedPlan>(it->second);
+      if (P->ns == ns && P->list.size() == list.size() &&
+          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0) {
+        ctx.keep_alive(P);
+        return P;
+      }
+    }
+  }
+  auto P = build_fused_plan(ctx, list, ns);
+  std::lock_guard<std::mutex> lk(ctx.mu);
+  if (ctx.fused_cache.size() > 1024) ctx.fused_cache.clear();
+  ctx.fused_cache[key] = P;
+  ctx.keep_alive(P);
+  return P;
+}
+
+void run_tc_fused(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
+                  double* C) {
+  auto P = get_fused_plan(ctx, list, ns);
+  if (!P->nitems) return;
+  const uint8_t* mb = (const uint8_t*)P->meta->ptr;
+  ProfScope ps(ctx, ns == 7 ? "tc_fused_split" : "tc_fused_bf16", P->in_bytes, P->flops);
+  const int grid = (int)std::min<int64_t>((int64_t)P->nitems, (int64_t)ctx.num_sms);
+  launch_tc_fused(ns, (const TcSector*)mb, (const int4*)(mb + P->off_it), P->nitems, A, B, C,
+                  ctx.device_error_word(), grid, ctx.stream);
+  ctx.launched();
+}
+
 }  // namespace tn

@@ -29,6 +29,7 @@
 
 #include "../engine/engine.h"
 #include "sm103_ptx.cuh"
+#include "tc_digits.cuh"
 
 namespace tn {
 namespace {
@@ -44,10 +45,6 @@ constexpr int kLevels = 6;      // exact levels 0..4 + one shared accumulator fo
 constexpr int kMaxLevel = 7;    // digit products with s + t <= 7 are kept
 constexpr int kThreadsTc = 192;
 
-__device__ __forceinline__ uint32_t swz_off(int r, int c) {  // row r (0..), 16-byte chunk c (0..7)
-  return (uint32_t)((r >> 3) * 1024 + (r & 7) * 128 + ((c ^ (r & 7)) << 4));
-}
-
 __device__ __forceinline__ int find_seg(const int64_t* __restrict__ start, int n, int64_t v) {
   int lo = 0, hi = n - 1;  // largest i with start[i] <= v
   while (lo < hi) {
@@ -58,15 +55,6 @@ __device__ __forceinline__ int find_seg(const int64_t* __restrict__ start, int n
       hi = mid - 1;
   }
   return lo;
-}
-
-// power-of-two exponent e with |x| < 2^e for every x of a row/column whose
-// largest magnitude has bit pattern maxbits (0 -> 0)
-__device__ __forceinline__ int exp_of(uint64_t maxbits) {
-  if (maxbits == 0) return 0;
-  int ef = (int)(maxbits >> 52);
-  if (ef == 0) return (63 - __clzll((long long)maxbits)) - 1073;  // subnormal: |x| < 2^(msb+1-1074)
-  return ef - 1022;
 }
 
 // ---------------------------------------------------------------- exponents
@@ -142,62 +130,6 @@ __global__ void __launch_bounds__(256) tc_maxima(const TcSector* __restrict__ se
       __syncthreads();
     }
   }
-}
-
-// ---------------------------------------------------------------- slicing
-__constant__ float kDigitScale[8] = {1.0f, 0x1p-7f, 0x1p-14f, 0x1p-21f, 0x1p-28f, 0x1p-35f, 0x1p-42f, 0x1p-49f};
-
-// 8 consecutive-k values of one row -> NS slices of 8 bf16 (packed in uint4)
-template <int NS>
-__device__ __forceinline__ void make_slices(const double (&x)[8], int e, uint4 (&out)[NS]) {
-  uint32_t w[NS][4];
-#pragma unroll
-  for (int s = 0; s < NS; s++)
-#pragma unroll
-    for (int q = 0; q < 4; q++) w[s][q] = 0;
-#pragma unroll
-  for (int i = 0; i < 8; i++) {
-    const uint64_t bits = (uint64_t)__double_as_longlong(x[i]);
-    const uint32_t sign = (uint32_t)(bits >> 63);
-    (void)sign;
-    if (NS == 1) {
-      // fast mode: round-to-nearest BF16 of x * 2^(7-e)
-      const float f = (float)ldexp(x[i], 7 - e);
-      const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(f));
-      w[0][i >> 1] |= h << ((i & 1) * 16);
-    } else {
-      const int ef = (int)((bits >> 52) & 0x7FF);
-      uint64_t mant = bits & ((1ull << 52) - 1);
-      int E = -1022;
-      if (ef) {
-        mant |= 1ull << 52;
-        E = ef - 1023;
-      }
-      // X = |x| * 2^(7*NS - e) rounded to the nearest integer (at most 2^(7*NS))
-      const int sh = 52 + e - E - 7 * NS;
-      const uint64_t X = (sh >= 64) ? 0ull
-                         : (sh > 0 ? ((mant + (1ull << (sh - 1))) >> sh) : (mant << (-sh)));
-      // balanced digits, least significant first: d in [-64, 63], top digit
-      // |d_0| <= 129 -- every one exact in BF16
-      long long V = sign ? -(long long)X : (long long)X;
-      int d[NS];
-#pragma unroll
-      for (int s = NS - 1; s > 0; s--) {
-        const int low = (int)(V & 127);
-        d[s] = low >= 64 ? low - 128 : low;
-        V = (V - d[s]) >> 7;
-      }
-      d[0] = (int)V;
-#pragma unroll
-      for (int s = 0; s < NS; s++) {
-        const float f = __int2float_rn(d[s]) * kDigitScale[s];
-        const uint32_t h = (uint32_t)__bfloat16_as_ushort(__float2bfloat16_rn(f));
-        w[s][i >> 1] |= h << ((i & 1) * 16);
-      }
-    }
-  }
-#pragma unroll
-  for (int s = 0; s < NS; s++) out[s] = make_uint4(w[s][0], w[s][1], w[s][2], w[s][3]);
 }
 
 // A tile t: (sector, mt, kt) -> NS images of 128 rows x 64 k

@@ -1,0 +1,423 @@
+// Fused tensor-core sector GEMM for contractions made of small sectors (the
+// iTEBD theta network's blocks are at most a few hundred rows and columns with
+// K <= 68).  One launch does what the tiled form does in three (maxima,
+// slicing, GEMM).  A work item is one 128 x 64 output tile of one sector; its
+// CTA
+//   1. takes the power-of-two scale of each row of A and each column of B over
+//      the sector's K (from the 64-k block itself when K <= 64, else from a
+//      first pass over the rows and columns),
+//   2. per 64-k block: reads the A rows and B columns (FP64, global memory),
+//      writes the NS digit images of both into shared memory in the tcgen05
+//      K-major 128-byte swizzled layout and issues the digit products (34 for
+//      NS = 7, s + t <= 7) as tcgen05.mma kind::f16 into 6 TMEM accumulators
+//      (levels 0..4 exact, 5..7 shared), only the 16-k steps that hold data,
+//   3. every 128 k (the exact-accumulation chunk) and at the end, drains the
+//      levels into 64-bit fixed point in units of 2^-35: the exact levels
+//      convert without rounding (FP32 magic-number conversion) and the
+//      integer sum is exact in any order; |sum| < K * 2^49.03 < 2^63 for
+//      K <= 8192,
+//   4. converts the fixed-point sums to FP64 (round to nearest even) with the
+//      scale 2^(ea + eb - 14 - 35) folded into the exponent, and writes the
+//      tile through a shared-memory stage (coalesced).
+// GB300 runs FP64 arithmetic at ~2 operations per clock per SM, so the drain
+// and the conversion use integer operations only.
+//
+// CTA: 512 threads; all slice, warp 0 issues the MMAs (converged warp, one
+// elected lane), all 16 warps drain TMEM (lane quadrant warp & 3, 16-column
+// group warp >> 2).  Every wait on the MMA barrier is bounded.
+#include <cuda_bf16.h>
+
+#include <cstdint>
+
+#include "../engine/engine.h"
+#include "sm103_ptx.cuh"
+#include "tc_digits.cuh"
+
+namespace tn {
+namespace {
+
+using namespace ptx;
+
+constexpr int kFM = 128, kFN = 64, kFK = 64;
+constexpr int kFThreads = 512;
+constexpr int kFixUnit = 35;   // fixed-point sums in units of 2^-35
+constexpr int kFLevels = 6;    // exact levels 0..4 + one shared accumulator for 5..7
+constexpr int kFMaxLevel = 7;  // digit products with s + t <= 7 are kept
+constexpr int kAImg = kFM * kFK * 2;  // bytes of one A digit image
+constexpr int kBImg = kFN * kFK * 2;  // bytes of one B digit image
+constexpr int kStride = kFN + 1;      // row stride (doubles) of the FP64 stages
+
+template <int NS>
+struct FusedLayout {
+  static constexpr int dig = NS * (kAImg + kBImg);
+  static constexpr int ostage = kFM * kStride * 8;  // FP64 output tile, reuses the digit images
+  static constexpr int region0 = dig > ostage ? dig : ostage;
+  static constexpr int bstage = kFK * kStride * 8;  // FP64 B block
+  static constexpr int bytes = region0 + bstage + 1024;  // + alignment of the swizzle base
+};
+
+struct __align__(8) FusedShared {
+  uint64_t mma_bar;
+  uint32_t tmem_base;
+  int abort;
+  int ea[kFM];
+  int eb[kFN];
+  unsigned long long colpart[kFThreads / kFN][kFN];
+};
+
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+
+// nearest integer to v for |v| < 2^22 (ties to even): the FP32 add of
+// 1.5 * 2^23 lands the integer in the low mantissa bits
+__device__ __forceinline__ int magic_int(float v) {
+  return (int)(__float_as_uint(v + 12582912.0f) - 0x4B400000u);
+}
+
+// One TMEM level sum in units of 2^-35.  Level l < 5 holds integers times
+// 2^-7l, at most 28800 * 128 < 2^22 of them over a 128-k chunk, so
+// v * 2^7l converts exactly; the shared level 5..7 (at most ~16600 * 2^-34
+// per k) is rounded to units of 2^-34.
+template <int LVL>
+__device__ __forceinline__ long long level_fixed(float v) {
+  if constexpr (LVL < 5)
+    return (long long)magic_int(v * (float)(1 << (7 * LVL))) << (kFixUnit - 7 * LVL);
+  else
+    return (long long)magic_int(v * 0x1p34f) << 1;
+}
+
+// d * 2^q for a finite double d, the exponent adjusted as an integer when the
+// result stays normal
+__device__ __forceinline__ double scale_pow2(double d, int q) {
+  const uint64_t b = (uint64_t)__double_as_longlong(d);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0 || ex + q < 1 || ex + q > 2046) return ldexp(d, q);
+  return __longlong_as_double((long long)(b + ((uint64_t)(int64_t)q << 52)));
+}
+
+// S * 2^q as the nearest double (ties to even), integer operations only (the
+// FP64 units and FP64 conversions run at ~2 per clock per SM on GB300)
+__device__ __forceinline__ double fixed_to_double(long long S, int q) {
+  if (S == 0) return 0.0;
+  const uint64_t sign = (uint64_t)S & (1ull << 63);
+  uint64_t mag = S < 0 ? (uint64_t)(-S) : (uint64_t)S;
+  const int lz = __clzll((long long)mag);
+  mag <<= lz;                                        // leading one at bit 63
+  const int E = 63 - lz + q;                         // value = mag * 2^(E - 63)
+  const uint32_t rem = (uint32_t)mag & 0x7FFu;
+  const uint64_t r = (mag >> 11) + (uint64_t)((rem > 0x400u) | ((rem == 0x400u) & (uint32_t)(mag >> 11)));  // ties to even; may reach 2^53
+  if (E < -1021 || E > 1022) return ldexp(__ll2double_rn(S), q);     // near the ends of the range: slow path
+  // the hidden bit of r adds one to the exponent field (two when r carried to 2^53)
+  return __longlong_as_double((long long)(sign | (((uint64_t)(E + 1022) << 52) + r)));
+}
+
+template <int NS>
+__global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restrict__ secs,
+                                                         const int4* __restrict__ items, int nitems,
+                                                         const double* __restrict__ A, const double* __restrict__ B,
+                                                         double* __restrict__ C, int* __restrict__ err) {
+  using L = FusedLayout<NS>;
+  constexpr int LV = (NS == 1) ? 1 : kFLevels;
+  constexpr int kGroups = kFThreads / kFN;  // column-maximum partials per column
+  // 64-k blocks per exact-accumulation chunk: 128 k keeps every exact level
+  // under 2^22 (split); fast mode sums the whole K in FP32
+  constexpr int kChunk = (NS == 1) ? (1 << 30) : 2;
+  extern __shared__ uint8_t dyn[];
+  __shared__ FusedShared sh;
+  uint8_t* base = (uint8_t*)(((uintptr_t)dyn + 1023) & ~(uintptr_t)1023);
+  uint8_t* adig = base;                        // NS x 16 KB
+  uint8_t* bdig = base + NS * kAImg;           // NS x 8 KB
+  double* ost = (double*)base;                 // [128][65], once the last MMAs are done
+  double* bst = (double*)(base + L::region0);  // [64][65]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  if (tid == 0) {
+    mbar_init(&sh.mma_bar, 1);
+    sh.abort = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(&sh.tmem_base, 512);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = sh.tmem_base;
+  uint32_t phase = 0;
+  bool ok = true;
+  // drain geometry: TMEM lane quadrant, 16-column group
+  const int qd = warp & 3, cg = warp >> 2, rl = qd * 32 + lane;
+
+  for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
+    const int4 w = items[it];
+    const TcSector& S = secs[w.x];
+    const int mt = w.y, nt = w.z, n0 = nt * kFN, K = S.K, nkt = S.nkt;
+    const int64_t row0 = (int64_t)mt * kFM;
+    if (nkt > 1) {
+      // ---- scales over the whole K: rows (8 lanes per row) and columns (8 partials)
+#pragma unroll
+      for (int p = 0; p < (kFM * 8) / kFThreads; p++) {
+        const int v = tid + p * kFThreads, r = v >> 3, c = v & 7;
+        unsigned long long m = 0;
+        if (row0 + r < S.M) {
+          const double* src = A + S.a_off + (row0 + r) * S.K;
+          for (int k = c * 8; k < K; k += kFK)
+#pragma unroll
+            for (int q = 0; q < 8; q++)
+              if (k + q < K) {
+                const unsigned long long bts = abs_bits(__ldg(src + k + q));
+                m = bts > m ? bts : m;
+              }
+        }
+#pragma unroll
+        for (int o = 4; o; o >>= 1) {
+          const unsigned long long x = __shfl_xor_sync(0xffffffffu, m, o);
+          m = x > m ? x : m;
+        }
+        if (c == 0) sh.ea[r] = exp_of(m);
+      }
+      {
+        const int n = tid & 63, g = tid >> 6;
+        unsigned long long m = 0;
+        if (n0 + n < S.N)
+          for (int k = g; k < K; k += kGroups) {
+            const unsigned long long bts = abs_bits(__ldg(B + S.b_off + (int64_t)k * S.N + n0 + n));
+            m = bts > m ? bts : m;
+          }
+        sh.colpart[g][n] = m;
+      }
+      __syncthreads();
+      if (tid < kFN) {
+        unsigned long long m = sh.colpart[0][tid];
+#pragma unroll
+        for (int g = 1; g < kGroups; g++) m = sh.colpart[g][tid] > m ? sh.colpart[g][tid] : m;
+        sh.eb[tid] = exp_of(m);
+      }
+      __syncthreads();
+    }
+    long long acc[16];  // split: fixed-point sums of the levels
+    float accf[16];     // fast mode: the FP32 sum
+#pragma unroll
+    for (int j = 0; j < 16; j++) {
+      acc[j] = 0;
+      accf[j] = 0.f;
+    }
+    for (int kt = 0; kt < nkt; kt++) {
+      const int k0 = kt * kFK, kval = min(kFK, K - k0);
+      const int nks = (kval + 15) >> 4, nch = 2 * nks;  // 16-k MMA steps, 8-k chunks holding data
+      // ---- B block -> FP64 stage, coalesced along n (asynchronous copies,
+      // in flight while A is sliced)
+#pragma unroll
+      for (int j = 0; j < (kFK * kFN) / kFThreads; j++) {
+        const int f = tid + j * kFThreads, k = f >> 6, n = f & 63;
+        const bool valid = k < kval && n0 + n < S.N;
+        cp_async8(bst + k * kStride + n, valid ? B + S.b_off + (int64_t)(k0 + k) * S.N + n0 + n : B, valid);
+      }
+      // ---- A: thread (row r, 8-k chunk c), both of its chunks loaded first
+      constexpr int kPairs = (kFM * 8) / kFThreads;
+      double xa[kPairs][8];
+#pragma unroll
+      for (int p = 0; p < kPairs; p++) {
+        const int v = tid + p * kFThreads, r = v >> 3, c = v & 7;
+        const int64_t i = row0 + r;
+        const double* src = A + S.a_off + i * S.K + k0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) xa[p][q] = (i < S.M && c * 8 + q < kval) ? __ldg(src + c * 8 + q) : 0.0;
+      }
+#pragma unroll
+      for (int p = 0; p < kPairs; p++) {
+        const int v = tid + p * kFThreads, r = v >> 3, c = v & 7;
+        unsigned long long m = 0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) {
+          const unsigned long long bts = abs_bits(xa[p][q]);
+          m = bts > m ? bts : m;
+        }
+        int e;
+        if (nkt == 1) {  // the row's scale from its 8 lanes
+#pragma unroll
+          for (int o = 4; o; o >>= 1) {
+            const unsigned long long y = __shfl_xor_sync(0xffffffffu, m, o);
+            m = y > m ? y : m;
+          }
+          e = exp_of(m);
+          if (c == 0) sh.ea[r] = e;
+        } else {
+          e = sh.ea[r];
+        }
+        if (c < nch) {
+          uint4 o[NS];
+          make_slices<NS>(xa[p], e, o);
+          const uint32_t off = swz_off(r, c);
+#pragma unroll
+          for (int s = 0; s < NS; s++) *(uint4*)(adig + s * kAImg + off) = o[s];
+        }
+      }
+      cp_async_wait_all();
+      __syncthreads();  // B stage complete
+      if (nkt == 1) {   // column scales from the stage
+        const int n = tid & 63, g = tid >> 6;
+        unsigned long long m = 0;
+#pragma unroll
+        for (int k = g * (kFK / kGroups); k < (g + 1) * (kFK / kGroups); k++) {
+          const unsigned long long bts = abs_bits(bst[k * kStride + n]);
+          m = bts > m ? bts : m;
+        }
+        sh.colpart[g][n] = m;
+        __syncthreads();
+        if (tid < kFN) {
+          unsigned long long mm = sh.colpart[0][tid];
+#pragma unroll
+          for (int q = 1; q < kGroups; q++) mm = sh.colpart[q][tid] > mm ? sh.colpart[q][tid] : mm;
+          sh.eb[tid] = exp_of(mm);
+        }
+        __syncthreads();
+      }
+      // ---- B: thread (column r, 8-k chunk c), consecutive lanes -> consecutive columns
+      for (int v = tid; v < kFN * 8; v += kFThreads) {
+        const int r = v & 63, c = v >> 6;
+        if (c < nch) {
+          double x[8];
+#pragma unroll
+          for (int q = 0; q < 8; q++) x[q] = bst[(c * 8 + q) * kStride + r];
+          uint4 o[NS];
+          make_slices<NS>(x, sh.eb[r], o);
+          const uint32_t off = swz_off(r, c);
+#pragma unroll
+          for (int s = 0; s < NS; s++) *(uint4*)(bdig + s * kBImg + off) = o[s];
+        }
+      }
+      // the digit images were written by the generic proxy; the tensor cores read them
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tc_fence_before();
+      __syncthreads();
+      tc_fence_after();
+      // ---- digit products
+      if (warp == 0) {
+        // bar.sync does not reconverge a warp: elect.sync below needs all 32
+        // lanes together, and a diverged warp pays for it on every product
+        __syncwarp();
+        // straight-line issue (all loops unrolled, descriptors base + constant);
+        // a level's first product of the block overwrites its accumulator at
+        // the start of a chunk: (s, t, kk) = (0, l, 0) in this order, the
+        // shared level first met at (0, 5, 0)
+        const uint32_t carry = (kt % kChunk) != 0;
+        const uint32_t idesc = idesc_bf16_f32(kFM, kFN);
+        const uint64_t a0 = desc_sw128(smem_u32(adig)), b0 = desc_sw128(smem_u32(bdig));
+#pragma unroll
+        for (int s = 0; s < NS; s++)
+#pragma unroll
+          for (int t = 0; t < NS; t++)
+            if (s + t <= (NS == 1 ? 0 : kFMaxLevel)) {
+              const int lvl = min(s + t, LV - 1);
+#pragma unroll
+              for (int kk = 0; kk < kFK / 16; kk++)
+                if (kk < nks) {
+                  const bool first = s == 0 && kk == 0 && t <= LV - 1;
+                  // +32 bytes per 16-k step inside the swizzle atom: +2 in the address field
+                  mma_bf16_elect(tmem + lvl * kFN, a0 + (uint64_t)(s * (kAImg >> 4) + 2 * kk),
+                                 b0 + (uint64_t)(t * (kBImg >> 4) + 2 * kk), idesc, first ? carry : 1u);
+                }
+            }
+        mma_commit_elect(&sh.mma_bar);
+      }
+      // warp 0 waits for the products; the others sleep in the barrier
+      // (spinning warps would take issue slots from the MMA warp)
+      const bool done = warp == 0 ? mbar_wait(&sh.mma_bar, phase & 1, &sh.abort) : true;
+      phase++;
+      if (__syncthreads_or(!done)) {
+        ok = false;
+        break;
+      }
+      tc_fence_after();
+      if (kt % kChunk == kChunk - 1 || kt == nkt - 1) {
+        // ---- drain the chunk: fixed point (split) or the FP32 sum (fast)
+        const uint32_t la = tmem + ((uint32_t)(qd * 32) << 16) + cg * 16;
+        float v[16];
+        if constexpr (NS == 1) {
+          tmem_ld16(la, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) accf[j] += v[j];
+        } else {
+          tmem_ld16(la, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) acc[j] += level_fixed<0>(v[j]);
+          tmem_ld16(la + 1 * kFN, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) acc[j] += level_fixed<1>(v[j]);
+          tmem_ld16(la + 2 * kFN, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) acc[j] += level_fixed<2>(v[j]);
+          tmem_ld16(la + 3 * kFN, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) acc[j] += level_fixed<3>(v[j]);
+          tmem_ld16(la + 4 * kFN, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) acc[j] += level_fixed<4>(v[j]);
+          tmem_ld16(la + 5 * kFN, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) acc[j] += level_fixed<5>(v[j]);
+        }
+        tc_fence_before();
+      }
+      __syncthreads();  // digit images, stage and accumulators are reused by the next block
+    }
+    if (!ok) break;
+    // ---- FP64 tile through the stage (reusing the digit images), coalesced writes
+    {
+      const int q = sh.ea[rl] - 14;
+#pragma unroll
+      for (int j = 0; j < 16; j++) {
+        const int qj = q + sh.eb[cg * 16 + j];
+        ost[rl * kStride + cg * 16 + j] =
+            NS == 1 ? scale_pow2((double)accf[j], qj) : fixed_to_double(acc[j], qj - kFixUnit);
+      }
+    }
+    __syncthreads();
+    for (int f = tid; f < kFM * kFN; f += kFThreads) {
+      const int r = f >> 6, c = f & 63;
+      const int64_t i = row0 + r;
+      if (i < S.M && n0 + c < S.N) C[S.c_off + i * S.N + n0 + c] = ost[r * kStride + c];
+    }
+    __syncthreads();  // the stage is the next item's digit images
+  }
+  if (!ok) {
+    if (tid == 0) atomicExch(err, TN_ERR_TIMEOUT);
+    // the MMAs still in flight must finish before the tensor memory is released
+    mbar_wait(&sh.mma_bar, (phase - 1) & 1, &sh.abort);
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  if (warp == 0) tmem_dealloc(tmem, 512);
+}
+
+}  // namespace
+
+size_t tc_fused_smem(int ns) { return ns == 7 ? (size_t)FusedLayout<7>::bytes : (size_t)FusedLayout<1>::bytes; }
+
+void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems, const double* A, const double* B,
+                     double* C, int* err, int grid, cudaStream_t s) {
+  if (nitems <= 0) return;
+  const size_t smem = tc_fused_smem(ns);
+  if (ns == 7) {
+    static bool attr = false;
+    if (!attr) {
+      TN_CUDA(cudaFuncSetAttribute(tc_fused<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = true;
+    }
+    tc_fused<7><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, err);
+  } else {
+    static bool attr = false;
+    if (!attr) {
+      TN_CUDA(cudaFuncSetAttribute(tc_fused<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = true;
+    }
+    tc_fused<1><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, err);
+  }
+  TN_CUDA(cudaGetLastError());
+}
+
+}  // namespace tn

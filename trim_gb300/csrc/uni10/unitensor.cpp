@@ -18,7 +18,7 @@ using tn::DevBuf;
 
 static thread_local int g_mode = TN_MODE_FP64;
 void setContractMode(int mode) {
-  const int m = mode & ~TN_MODE_TC_ONLY;
+  const int m = mode & ~(TN_MODE_TC_ONLY | TN_MODE_TC_FUSED | TN_MODE_TC_TILED);
   if (m < TN_MODE_FP64 || m > TN_MODE_FAST_TF32) throw std::runtime_error("unknown contraction mode");
   g_mode = mode;
 }
