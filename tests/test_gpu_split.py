@@ -255,3 +255,27 @@ def test_contract_batch_matches_pairwise(env):
         outs = tu.contract_batch(A, B, mode)
         for o, r in zip(outs, ref):
             assert rel(o.get_elem(), r) <= tol, mode
+
+
+def test_fused_form_reads_permuted_operands_in_place(env):
+    """Where the FP64 kernel reads a permuted operand through views (no permute
+    launch), the fused tensor-core form does too; results stay within the
+    split tolerance of the reference's outputs, and a contraction whose
+    operands need no permute gives the same numbers through either path."""
+    torch, capi, tu = env
+    seen_views = 0
+    for case in [c for c in G.cases().values() if c["kind"] == "contract"]:
+        a = tu.UniTensor(G.bonds_of(case["A"]), case["A"]["labels"], G.arr(case["id"], "A"))
+        b = tu.UniTensor(G.bonds_of(case["B"]), case["B"]["labels"], G.arr(case["id"], "B"))
+        counts = {}
+        for mode in ("fp64", "split_fused"):
+            tu.prof_enable(True)
+            c = tu.contract(a, b, mode=mode)
+            prof = tu.prof_read()
+            tu.prof_enable(False)
+            counts[mode] = prof.get("permute", {}).get("launches", 0)
+            tol = 1e-13 if mode == "fp64" else SPLIT_TOL
+            assert rel(c.get_elem(), G.arr(case["id"], "C")) <= tol, (case["id"], mode)
+        assert counts["split_fused"] <= counts["fp64"], (case["id"], counts)
+        seen_views += counts["fp64"] == 0
+    assert seen_views > 0

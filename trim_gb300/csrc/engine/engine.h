@@ -185,6 +185,7 @@ struct TcSector {
   int32_t nmt, nnt, nkt;        // 128-row, 64-column and 64-k tile counts
   int32_t nsplit;               // K ranges per output tile (chunk aligned)
   int32_t kts;                  // 64-k tiles per K range (a multiple of the 512-k chunk)
+  int32_t a_vw, b_vw;           // fused form: operand views (ViewHdr index), -1: contiguous row-major
 };
 
 // One sector of the cluster Jacobi SVD (M x N, row-major).  Stage 1 (FP32):
@@ -286,6 +287,10 @@ struct Ctx {
   }
   bool autotune = false;            // FP64 GEMM policies timed per sector histogram
   std::unordered_map<uint64_t, Fp64Policy> tuned;
+  // tensor-core modes: for a contraction the fused form fits, the faster of
+  // the fused form and the FP64 kernel, measured once per sector-size
+  // histogram (1: fused, 0: FP64)
+  std::unordered_map<uint64_t, int> route_tuned;
   std::unordered_map<uint64_t, std::shared_ptr<void>> svd_cache;  // SVD batch plans
   std::unordered_map<std::string, OpViewsP> view_cache;           // operand views per permute
 };
@@ -313,14 +318,19 @@ void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& lis
 // operand views of a permute (cached; ->ok false when it cannot be fused)
 OpViewsP get_op_views(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
 std::shared_ptr<OpViews> build_op_views(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
-// true when these sectors run on the FP64 kernel in this mode (views apply)
-bool sectors_on_fp64(int mode, const std::vector<tn_sector_gemm>& list);
-// the FP64 grouped GEMM with operands read through views: va / vb may be
-// null (contiguous operand); a_blk[i] / b_blk[i] name the view block of
-// sector i; A / B are then the unpermuted source buffers
-void run_sector_gemms_views(Ctx& ctx, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
-                            double* C, const OpViewsP& va, const std::vector<int>& a_blk, const OpViewsP& vb,
-                            const std::vector<int>& b_blk);
+// The form one contraction's sector GEMMs take in a mode: the FP64 kernel,
+// the fused tensor-core kernel (small sectors, one launch) or the tiled
+// tensor-core path (maxima + slices + pipelined GEMM; thin sectors on FP64)
+enum class GemmRoute { Fp64, Fused, Tiled };
+GemmRoute sector_route(const Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list);
+// true when that form reads operands through views (FP64 and fused)
+bool sectors_take_views(const Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list);
+// the sector GEMMs with operands read through views: va / vb may be null
+// (contiguous operand); a_blk[i] / b_blk[i] name the view block of sector i;
+// A / B are then the unpermuted source buffers
+void run_sector_gemms_views(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A,
+                            const double* B, double* C, const OpViewsP& va, const std::vector<int>& a_blk,
+                            const OpViewsP& vb, const std::vector<int>& b_blk);
 
 // FP64 tile plan: 512-entry output tiles shaped to each sector's width, K
 // split to the policy's items per SM; with ws_cap_elems >= 0 the split is
@@ -354,7 +364,7 @@ void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems,
 // digit products; levels are summed as 64-bit fixed point, exactly.
 size_t tc_fused_smem(int ns);
 void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems, const double* A, const double* B,
-                     double* C, int* err, int grid, cudaStream_t s);
+                     double* C, const ViewHdr* views, const int64_t* pool, int* err, int grid, cudaStream_t s);
 // C tile = sum over the K ranges of its FP64 partial tiles, in range order
 void launch_tc_reduce(const TcSector* secs, const int4* ritems, int nred, const double* part, double* C, int grid,
                       cudaStream_t s);

@@ -277,7 +277,8 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
 // the tensor-core modes' routing rule (see run_sector_gemms): true for a
 // sector the FP64 kernel takes
 void run_tc_fused(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
-                  double* C);
+                  double* C, const std::vector<std::pair<int, int>>* vw = nullptr, const ViewHdr* views = nullptr,
+                  const int64_t* pool = nullptr, const void* table = nullptr);
 int64_t fused_items(const std::vector<tn_sector_gemm>& list);
 
 constexpr int kModeFlags = TN_MODE_TC_ONLY | TN_MODE_TC_FUSED | TN_MODE_TC_TILED;
@@ -294,14 +295,80 @@ static bool fused_fits(const Ctx& ctx, const std::vector<tn_sector_gemm>& list) 
   return fused_items(list) <= 4 * (int64_t)ctx.num_sms;
 }
 
-bool sectors_on_fp64(int mode, const std::vector<tn_sector_gemm>& list) {
-  const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0, want_fused = (mode & TN_MODE_TC_FUSED) != 0;
+static uint64_t route_key(int mode, const std::vector<tn_sector_gemm>& list) {
+  return sector_histogram_key(list) ^ ((uint64_t)(mode & 0xFF) * 0x9E3779B97F4A7C15ull);
+}
+
+// the static choice before any measurement (flags force a form)
+static GemmRoute static_route(const Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list) {
+  const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0;
+  const bool want_fused = (mode & TN_MODE_TC_FUSED) != 0, want_tiled = (mode & TN_MODE_TC_TILED) != 0;
   mode &= ~kModeFlags;
-  if (mode == TN_MODE_FP64) return true;
-  if (tc_only || want_fused) return false;
-  for (const auto& g : list)
-    if (!thin_sector(g)) return false;
-  return true;
+  if (mode == TN_MODE_FP64) return GemmRoute::Fp64;
+  if (mode == TN_MODE_FAST_TF32) fail(TN_ERR_UNSUPPORTED, "TF32 fast mode is not built; use TN_MODE_FAST_BF16");
+  if (mode != TN_MODE_SPLIT && mode != TN_MODE_FAST_BF16) fail(TN_ERR_ARG, "unknown contraction mode");
+  if (want_fused && want_tiled) fail(TN_ERR_ARG, "TN_MODE_TC_FUSED and TN_MODE_TC_TILED exclude each other");
+  if (want_tiled) return GemmRoute::Tiled;
+  if (want_fused) return GemmRoute::Fused;
+  bool all_thin = !tc_only;
+  for (const auto& g : list) all_thin = all_thin && thin_sector(g);
+  if (all_thin) return GemmRoute::Fp64;
+  // one fused launch for every sector, thin ones included (they cost a CTA
+  // each, side by side with the rest)
+  if (fused_fits(ctx, list)) return GemmRoute::Fused;
+  return GemmRoute::Tiled;
+}
+
+// true when the choice between the fused form and the FP64 kernel is left to
+// a measurement (no flag forces a form)
+static bool route_tunable(int mode, GemmRoute st) {
+  return st == GemmRoute::Fused && !(mode & kModeFlags);
+}
+
+GemmRoute sector_route(const Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list) {
+  const GemmRoute st = static_route(ctx, mode, list);
+  if (!route_tunable(mode, st)) return st;
+  auto it = ctx.route_tuned.find(route_key(mode, list));
+  if (it == ctx.route_tuned.end()) return st;
+  return it->second ? GemmRoute::Fused : GemmRoute::Fp64;
+}
+
+// Times the fused form and the FP64 kernel (both write the same output) and
+// keeps the faster for this histogram; the chosen form runs last, so the
+// output holds its result.  Not measured while a graph is being captured.
+template <class Fused, class Fp64>
+static GemmRoute tune_route(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, Fused&& fused, Fp64&& fp64) {
+  const GemmRoute st = static_route(ctx, mode, list);
+  if (!route_tunable(mode, st)) return st;
+  const uint64_t key = route_key(mode, list);
+  auto it = ctx.route_tuned.find(key);
+  if (it != ctx.route_tuned.end()) return it->second ? GemmRoute::Fused : GemmRoute::Fp64;
+  if (capturing(ctx)) return st;
+  cudaEvent_t e0, e1;
+  TN_CUDA(cudaEventCreate(&e0));
+  TN_CUDA(cudaEventCreate(&e1));
+  auto time_of = [&](auto&& fn) {
+    fn();  // warm-up: plans and workspace in place
+    TN_CUDA(cudaEventRecord(e0, ctx.stream));
+    for (int r = 0; r < 3; r++) fn();
+    TN_CUDA(cudaEventRecord(e1, ctx.stream));
+    TN_CUDA(cudaEventSynchronize(e1));
+    float ms = 0;
+    TN_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    return ms;
+  };
+  const float t_fused = time_of(fused), t_fp64 = time_of(fp64);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const bool use_fused = t_fused < t_fp64;
+  ctx.route_tuned[key] = use_fused ? 1 : 0;
+  if (use_fused) fused();  // the output holds the chosen form's result
+  return use_fused ? GemmRoute::Fused : GemmRoute::Fp64;
+}
+
+bool sectors_take_views(const Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list) {
+  const GemmRoute r = sector_route(ctx, mode, list);
+  return r == GemmRoute::Fp64 || r == GemmRoute::Fused;
 }
 
 // The views of one contraction's two operands as one device table.
@@ -353,54 +420,59 @@ static std::shared_ptr<ViewTable> get_view_table(Ctx& ctx, const OpViewsP& va, c
   return T;
 }
 
-void run_sector_gemms_views(Ctx& ctx, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
-                            double* C, const OpViewsP& va, const std::vector<int>& a_blk, const OpViewsP& vb,
-                            const std::vector<int>& b_blk) {
+void run_sector_gemms_views(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A,
+                            const double* B, double* C, const OpViewsP& va, const std::vector<int>& a_blk,
+                            const OpViewsP& vb, const std::vector<int>& b_blk) {
   if (list.empty()) return;
   if (!va && !vb) {
-    run_fp64(ctx, list, A, B, C);
+    run_sector_gemms(ctx, mode, list, A, B, C);
     return;
   }
+  if (sector_route(ctx, mode, list) == GemmRoute::Tiled)
+    fail(TN_ERR_ARG, "operand views reach the FP64 and fused forms only");
   auto T = get_view_table(ctx, va, vb);
   std::vector<std::pair<int, int>> vw(list.size(), {-1, -1});
   for (size_t i = 0; i < list.size(); i++) {
     if (va) vw[i].first = va->hdr_of_block.at(a_blk.at(i));
     if (vb) vw[i].second = T->na + vb->hdr_of_block.at(b_blk.at(i));
   }
-  auto P = get_fp64_plan(ctx, list, Fp64Policy(), &vw, T.get());
-  if (!P->ntiles) return;
-  launch_fp64_plan(ctx, *P, A, B, C, (const ViewHdr*)T->hdrs->ptr, (const int64_t*)T->pool->ptr);
+  const ViewHdr* views = (const ViewHdr*)T->hdrs->ptr;
+  const int64_t* pool = (const int64_t*)T->pool->ptr;
+  const int ns = (mode & ~kModeFlags) == TN_MODE_SPLIT ? 7 : 1;
+  auto fused = [&] { run_tc_fused(ctx, ns, list, A, B, C, &vw, views, pool, T.get()); };
+  auto fp64 = [&] {
+    auto P = get_fp64_plan(ctx, list, Fp64Policy(), &vw, T.get());
+    if (P->ntiles) launch_fp64_plan(ctx, *P, A, B, C, views, pool);
+  };
+  const bool tuned = ctx.route_tuned.count(route_key(mode, list)) > 0;
+  const GemmRoute route = tune_route(ctx, mode, list, fused, fp64);
+  if (!tuned && ctx.route_tuned.count(route_key(mode, list))) return;  // measured just now: C holds the result
+  if (route == GemmRoute::Fused)
+    fused();
+  else
+    fp64();
 }
 
 void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
                       double* C) {
   if (list.empty()) return;
   const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0;
-  const bool want_fused = (mode & TN_MODE_TC_FUSED) != 0, want_tiled = (mode & TN_MODE_TC_TILED) != 0;
-  mode &= ~kModeFlags;
-  if (mode == TN_MODE_FP64) {
+  const int ns = (mode & ~kModeFlags) == TN_MODE_SPLIT ? 7 : 1;
+  const bool tuned = ctx.route_tuned.count(route_key(mode, list)) > 0;
+  const GemmRoute route = tune_route(
+      ctx, mode, list, [&] { run_tc_fused(ctx, ns, list, A, B, C); }, [&] { run_fp64(ctx, list, A, B, C); });
+  if (!tuned && ctx.route_tuned.count(route_key(mode, list))) return;  // measured just now: C holds the result
+  if (route == GemmRoute::Fp64) {
     run_fp64(ctx, list, A, B, C);
-    return;
+  } else if (route == GemmRoute::Fused) {
+    run_tc_fused(ctx, ns, list, A, B, C);
+  } else {
+    // tiled: thin sectors on the FP64 kernel (unless TN_MODE_TC_ONLY)
+    std::vector<tn_sector_gemm> tc, f64;
+    for (const auto& g : list) (!tc_only && thin_sector(g) ? f64 : tc).push_back(g);
+    if (!f64.empty()) run_fp64(ctx, f64, A, B, C);
+    if (!tc.empty()) run_tc_gemms(ctx, ns, tc, A, B, C);
   }
-  if (mode == TN_MODE_FAST_TF32) fail(TN_ERR_UNSUPPORTED, "TF32 fast mode is not built; use TN_MODE_FAST_BF16");
-  if (mode != TN_MODE_SPLIT && mode != TN_MODE_FAST_BF16) fail(TN_ERR_ARG, "unknown contraction mode");
-  if (want_fused && want_tiled) fail(TN_ERR_ARG, "TN_MODE_TC_FUSED and TN_MODE_TC_TILED exclude each other");
-  const int ns = mode == TN_MODE_SPLIT ? 7 : 1;
-  if (!want_tiled && (want_fused || fused_fits(ctx, list))) {
-    // one fused launch for every sector, thin ones included (they cost a CTA
-    // each, side by side with the rest) -- unless all of them are thin
-    bool all_thin = !tc_only;
-    for (const auto& g : list) all_thin = all_thin && thin_sector(g);
-    if (all_thin && !want_fused)
-      run_fp64(ctx, list, A, B, C);
-    else
-      run_tc_fused(ctx, ns, list, A, B, C);
-    return;
-  }
-  std::vector<tn_sector_gemm> tc, f64;
-  for (const auto& g : list) (!tc_only && thin_sector(g) ? f64 : tc).push_back(g);
-  if (!f64.empty()) run_fp64(ctx, f64, A, B, C);
-  if (!tc.empty()) run_tc_gemms(ctx, ns, tc, A, B, C);
 }
 
 }  // namespace tn

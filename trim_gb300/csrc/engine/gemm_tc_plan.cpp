@@ -75,6 +75,7 @@ static std::shared_ptr<TcPlan> build_tc_plan(Ctx& ctx, const std::vector<tn_sect
     s.nsplit = 1;
     s.kts = s.nkt;
     s.p_off = -1;
+    s.a_vw = s.b_vw = -1;
     secs.push_back(s);
     rb.push_back(P->nrb);
     cb.push_back(P->ncb);
@@ -203,6 +204,8 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
 // tile); the CTA walks the sector's K itself.
 struct FusedPlan {
   std::vector<tn_sector_gemm> list;
+  std::vector<std::pair<int, int>> vw;  // per sector: (A view, B view) header indices, -1: none
+  const void* table = nullptr;          // the view table the indices refer to
   int ns = 7;
   DevBufP meta;
   size_t off_it = 0;
@@ -219,13 +222,17 @@ int64_t fused_items(const std::vector<tn_sector_gemm>& list) {
   return n;
 }
 
-static std::shared_ptr<FusedPlan> build_fused_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns) {
+static std::shared_ptr<FusedPlan> build_fused_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns,
+                                                   const std::vector<std::pair<int, int>>* vw, const void* table) {
   auto P = std::make_shared<FusedPlan>();
   P->list = list;
+  if (vw) P->vw = *vw;
+  P->table = table;
   P->ns = ns;
   std::vector<TcSector> secs;
   std::vector<int4> items;
-  for (const auto& g : list) {
+  for (size_t gi = 0; gi < list.size(); gi++) {
+    const auto& g = list[gi];
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX / 2 || g.N > INT32_MAX / 2)
       fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large for the tensor-core path");
@@ -245,6 +252,8 @@ static std::shared_ptr<FusedPlan> build_fused_plan(Ctx& ctx, const std::vector<t
     s.nsplit = 1;
     s.kts = s.nkt;
     s.p_off = -1;
+    s.a_vw = vw ? (*vw)[gi].first : -1;
+    s.b_vw = vw ? (*vw)[gi].second : -1;
     const int idx = (int)secs.size();
     secs.push_back(s);
     for (int mt = 0; mt < s.nmt; mt++)
@@ -269,21 +278,25 @@ static std::shared_ptr<FusedPlan> build_fused_plan(Ctx& ctx, const std::vector<t
   return P;
 }
 
-static std::shared_ptr<FusedPlan> get_fused_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns) {
-  const uint64_t key = hash_list(list, 200 + ns);
+static std::shared_ptr<FusedPlan> get_fused_plan(Ctx& ctx, const std::vector<tn_sector_gemm>& list, int ns,
+                                                 const std::vector<std::pair<int, int>>* vw, const void* table) {
+  uint64_t key = hash_list(list, 200 + ns) ^ ((uint64_t)(uintptr_t)table * 0x9E3779B97F4A7C15ull);
+  if (vw)
+    for (const auto& p : *vw) key = (key ^ (uint64_t)(uint32_t)p.first ^ ((uint64_t)(uint32_t)p.second << 32)) * 1099511628211ull;
   {
     std::lock_guard<std::mutex> lk(ctx.mu);
     auto it = ctx.fused_cache.find(key);
     if (it != ctx.fused_cache.end()) {
       auto P = std::static_pointer_cast<FusedPlan>(it->second);
-      if (P->ns == ns && P->list.size() == list.size() &&
-          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0) {
+      if (P->ns == ns && P->table == table && P->list.size() == list.size() &&
+          std::memcmp(P->list.data(), list.data(), list.size() * sizeof(tn_sector_gemm)) == 0 &&
+          (vw ? P->vw == *vw : P->vw.empty())) {
         ctx.keep_alive(P);
         return P;
       }
     }
   }
-  auto P = build_fused_plan(ctx, list, ns);
+  auto P = build_fused_plan(ctx, list, ns, vw, table);
   std::lock_guard<std::mutex> lk(ctx.mu);
   if (ctx.fused_cache.size() > 1024) ctx.fused_cache.clear();
   ctx.fused_cache[key] = P;
@@ -292,13 +305,14 @@ static std::shared_ptr<FusedPlan> get_fused_plan(Ctx& ctx, const std::vector<tn_
 }
 
 void run_tc_fused(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, const double* A, const double* B,
-                  double* C) {
-  auto P = get_fused_plan(ctx, list, ns);
+                  double* C, const std::vector<std::pair<int, int>>* vw, const ViewHdr* views, const int64_t* pool,
+                  const void* table) {
+  auto P = get_fused_plan(ctx, list, ns, vw, table);
   if (!P->nitems) return;
   const uint8_t* mb = (const uint8_t*)P->meta->ptr;
   ProfScope ps(ctx, ns == 7 ? "tc_fused_split" : "tc_fused_bf16", P->in_bytes, P->flops);
   const int grid = (int)std::min<int64_t>((int64_t)P->nitems, (int64_t)ctx.num_sms);
-  launch_tc_fused(ns, (const TcSector*)mb, (const int4*)(mb + P->off_it), P->nitems, A, B, C,
+  launch_tc_fused(ns, (const TcSector*)mb, (const int4*)(mb + P->off_it), P->nitems, A, B, C, views, pool,
                   ctx.device_error_word(), grid, ctx.stream);
   ctx.launched();
 }

@@ -6,7 +6,9 @@
 //   1. takes the power-of-two scale of each row of A and each column of B over
 //      the sector's K (from the 64-k block itself when K <= 64, else from a
 //      first pass over the rows and columns),
-//   2. per 64-k block: reads the A rows and B columns (FP64, global memory),
+//   2. per 64-k block: reads the A rows and B columns (FP64, global memory;
+//      an operand may be read through views of its unpermuted source, the
+//      permute fused into the load),
 //      writes the NS digit images of both into shared memory in the tcgen05
 //      K-major 128-byte swizzled layout and issues the digit products (34 for
 //      NS = 7, s + t <= 7) as tcgen05.mma kind::f16 into 6 TMEM accumulators
@@ -69,6 +71,69 @@ __device__ __forceinline__ unsigned long long abs_bits(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
 }
 
+// ---- operand addressing: plain row-major, or through a view of the
+// unpermuted source (the permute fused into the load): sub-block (row tuple,
+// column tuple) of the operand at pool (base, ld), element (r, c) of it at
+// base + r * ld + c
+__device__ __forceinline__ int find_start(const int64_t* __restrict__ st, int n, int64_t v) {
+  int lo = 0, hi = n - 1;  // largest i with st[i] <= v
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (__ldg(st + mid) <= v)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// A(i, k) for k = kc .. kc+7 below klim (0 above it); ri = row tuple of i when viewed
+__device__ __forceinline__ void load_a8(const double* __restrict__ A, const TcSector& S, const ViewHdr* av,
+                                        const int64_t* __restrict__ pool, int64_t i, int ri, int kc, int klim,
+                                        double (&x)[8]) {
+  if (!av) {
+    const double* src = A + S.a_off + i * S.K;
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = (kc + q < klim) ? __ldg(src + kc + q) : 0.0;
+    return;
+  }
+  if (kc >= klim) {
+#pragma unroll
+    for (int q = 0; q < 8; q++) x[q] = 0.0;
+    return;
+  }
+  const int64_t* cs = pool + av->cs;
+  int sk = find_start(cs, av->nc, kc);
+  const int64_t row = i - __ldg(pool + av->rs + ri);
+  int64_t send = __ldg(cs + sk + 1);
+  const int64_t* pr = pool + av->tab + 2 * ((int64_t)ri * av->nc + sk);
+  int64_t base = __ldg(pr) + row * __ldg(pr + 1) - __ldg(cs + sk);
+#pragma unroll
+  for (int q = 0; q < 8; q++) {
+    const int k = kc + q;
+    if (k < klim) {
+      if (k >= send) {  // next column tuple
+        sk++;
+        send = __ldg(cs + sk + 1);
+        pr += 2;
+        base = __ldg(pr) + row * __ldg(pr + 1) - __ldg(cs + sk);
+      }
+      x[q] = __ldg(A + base + k);
+    } else {
+      x[q] = 0.0;
+    }
+  }
+}
+
+// element index of B(k, n); cj = column tuple of n when viewed
+__device__ __forceinline__ int64_t b_index(const TcSector& S, const ViewHdr* bv, const int64_t* __restrict__ pool,
+                                           int k, int n, int cj) {
+  if (!bv) return S.b_off + (int64_t)k * S.N + n;
+  const int sk = find_start(pool + bv->rs, bv->nr, k);
+  const int64_t* pr = pool + bv->tab + 2 * ((int64_t)sk * bv->nc + cj);
+  return __ldg(pr) + (k - __ldg(pool + bv->rs + sk)) * __ldg(pr + 1) + (n - __ldg(pool + bv->cs + cj));
+}
+
 // nearest integer to v for |v| < 2^22 (ties to even): the FP32 add of
 // 1.5 * 2^23 lands the integer in the low mantissa bits
 __device__ __forceinline__ int magic_int(float v) {
@@ -116,7 +181,8 @@ template <int NS>
 __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restrict__ secs,
                                                          const int4* __restrict__ items, int nitems,
                                                          const double* __restrict__ A, const double* __restrict__ B,
-                                                         double* __restrict__ C, int* __restrict__ err) {
+                                                         double* __restrict__ C, const ViewHdr* __restrict__ views,
+                                                         const int64_t* __restrict__ pool, int* __restrict__ err) {
   using L = FusedLayout<NS>;
   constexpr int LV = (NS == 1) ? 1 : kFLevels;
   constexpr int kGroups = kFThreads / kFN;  // column-maximum partials per column
@@ -155,21 +221,34 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
     const TcSector& S = secs[w.x];
     const int mt = w.y, nt = w.z, n0 = nt * kFN, K = S.K, nkt = S.nkt;
     const int64_t row0 = (int64_t)mt * kFM;
+    const ViewHdr* av = S.a_vw >= 0 ? views + S.a_vw : nullptr;
+    const ViewHdr* bv = S.b_vw >= 0 ? views + S.b_vw : nullptr;
+    constexpr int kPairs = (kFM * 8) / kFThreads;  // (row, 8-k chunk) pairs per thread
+    // this thread's A rows (their row tuples when viewed) and B column (its column tuple)
+    int ri[kPairs];
+#pragma unroll
+    for (int p = 0; p < kPairs; p++) {
+      const int64_t i = row0 + ((tid + p * kFThreads) >> 3);
+      ri[p] = (av && i < S.M) ? find_start(pool + av->rs, av->nr, i) : 0;
+    }
+    const int bn = tid & 63;
+    const int cj = (bv && n0 + bn < S.N) ? find_start(pool + bv->cs, bv->nc, n0 + bn) : 0;
     if (nkt > 1) {
       // ---- scales over the whole K: rows (8 lanes per row) and columns (8 partials)
 #pragma unroll
-      for (int p = 0; p < (kFM * 8) / kFThreads; p++) {
+      for (int p = 0; p < kPairs; p++) {
         const int v = tid + p * kFThreads, r = v >> 3, c = v & 7;
         unsigned long long m = 0;
         if (row0 + r < S.M) {
-          const double* src = A + S.a_off + (row0 + r) * S.K;
-          for (int k = c * 8; k < K; k += kFK)
+          for (int k = c * 8; k < K; k += kFK) {
+            double x[8];
+            load_a8(A, S, av, pool, row0 + r, ri[p], k, K, x);
 #pragma unroll
-            for (int q = 0; q < 8; q++)
-              if (k + q < K) {
-                const unsigned long long bts = abs_bits(__ldg(src + k + q));
-                m = bts > m ? bts : m;
-              }
+            for (int q = 0; q < 8; q++) {
+              const unsigned long long bts = abs_bits(x[q]);
+              m = bts > m ? bts : m;
+            }
+          }
         }
 #pragma unroll
         for (int o = 4; o; o >>= 1) {
@@ -179,14 +258,14 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
         if (c == 0) sh.ea[r] = exp_of(m);
       }
       {
-        const int n = tid & 63, g = tid >> 6;
+        const int g = tid >> 6;
         unsigned long long m = 0;
-        if (n0 + n < S.N)
+        if (n0 + bn < S.N)
           for (int k = g; k < K; k += kGroups) {
-            const unsigned long long bts = abs_bits(__ldg(B + S.b_off + (int64_t)k * S.N + n0 + n));
+            const unsigned long long bts = abs_bits(__ldg(B + b_index(S, bv, pool, k, n0 + bn, cj)));
             m = bts > m ? bts : m;
           }
-        sh.colpart[g][n] = m;
+        sh.colpart[g][bn] = m;
       }
       __syncthreads();
       if (tid < kFN) {
@@ -211,20 +290,17 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       // in flight while A is sliced)
 #pragma unroll
       for (int j = 0; j < (kFK * kFN) / kFThreads; j++) {
-        const int f = tid + j * kFThreads, k = f >> 6, n = f & 63;
-        const bool valid = k < kval && n0 + n < S.N;
-        cp_async8(bst + k * kStride + n, valid ? B + S.b_off + (int64_t)(k0 + k) * S.N + n0 + n : B, valid);
+        const int k = (tid >> 6) + j * (kFThreads / kFN);  // f = tid + j * 512: n = f & 63 = bn, k = f >> 6
+        const bool valid = k < kval && n0 + bn < S.N;
+        cp_async8(bst + k * kStride + bn, valid ? B + b_index(S, bv, pool, k0 + k, n0 + bn, cj) : B, valid);
       }
       // ---- A: thread (row r, 8-k chunk c), both of its chunks loaded first
-      constexpr int kPairs = (kFM * 8) / kFThreads;
       double xa[kPairs][8];
 #pragma unroll
       for (int p = 0; p < kPairs; p++) {
         const int v = tid + p * kFThreads, r = v >> 3, c = v & 7;
         const int64_t i = row0 + r;
-        const double* src = A + S.a_off + i * S.K + k0;
-#pragma unroll
-        for (int q = 0; q < 8; q++) xa[p][q] = (i < S.M && c * 8 + q < kval) ? __ldg(src + c * 8 + q) : 0.0;
+        load_a8(A, S, av, pool, i, ri[p], k0 + c * 8, i < S.M ? K : 0, xa[p]);
       }
 #pragma unroll
       for (int p = 0; p < kPairs; p++) {
@@ -399,7 +475,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
 size_t tc_fused_smem(int ns) { return ns == 7 ? (size_t)FusedLayout<7>::bytes : (size_t)FusedLayout<1>::bytes; }
 
 void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems, const double* A, const double* B,
-                     double* C, int* err, int grid, cudaStream_t s) {
+                     double* C, const ViewHdr* views, const int64_t* pool, int* err, int grid, cudaStream_t s) {
   if (nitems <= 0) return;
   const size_t smem = tc_fused_smem(ns);
   if (ns == 7) {
@@ -408,14 +484,14 @@ void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems
       TN_CUDA(cudaFuncSetAttribute(tc_fused<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr = true;
     }
-    tc_fused<7><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, err);
+    tc_fused<7><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, views, pool, err);
   } else {
     static bool attr = false;
     if (!attr) {
       TN_CUDA(cudaFuncSetAttribute(tc_fused<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr = true;
     }
-    tc_fused<1><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, err);
+    tc_fused<1><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, views, pool, err);
   }
   TN_CUDA(cudaGetLastError());
 }

@@ -644,7 +644,7 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
     UniTensor Tc = (!mc || list.size() == mc->blocks.size()) ? UniTensor(cBonds, "", NoFill{}) : UniTensor(cBonds);
     if (!cBonds.empty()) Tc.setLabel(newLabelC);
     tn::OpViewsP va, vb;
-    if ((!mutate || !fast) && tn::sectors_on_fp64(g_mode, list)) {
+    if ((!mutate || !fast) && tn::sectors_take_views(c, g_mode, list)) {
       if (sa.moves) va = tn::get_op_views(c, *Ta.smap, *sa.smap, sa.rsp);
       if (sb.moves) vb = tn::get_op_views(c, *Tb.smap, *sb.smap, sb.rsp);
       if (va && !va->ok) va.reset();
@@ -680,7 +680,7 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
       }
     }
     if (va || vb)
-      tn::run_sector_gemms_views(c, list, Ap, Bp, dptr(Tc.elem), va, a_blk, vb, b_blk);
+      tn::run_sector_gemms_views(c, g_mode, list, Ap, Bp, dptr(Tc.elem), va, a_blk, vb, b_blk);
     else
       tn::run_sector_gemms(c, g_mode, list, Ap, Bp, dptr(Tc.elem));
     Tc.status |= UniTensor::HAVEELEM;
