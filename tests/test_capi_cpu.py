@@ -101,6 +101,11 @@ def test_permute_plans_of_workloads_bit_exact():
     O = m["tensors"][3]
     cases.append((O.bonds, [0, 1, 2, 3, 4, 5], [4, 5, 0, 1, 2, 3], 2))
     cases.append((O.bonds, [0, 1, 2, 3, 4, 5], [5, 3, 1, 0, 2, 4], 3))
+    # the MERA ascend's permutes whose two contiguous bonds are both short:
+    # transpose tiles of several stacked planes
+    for perm, rn in (((0, 3, 5, 1, 2, 4), 3), ((1, 2, 3, 5, 0, 4), 4), ((2, 3, 5, 0, 1, 4), 3),
+                     ((0, 2, 3, 5, 1, 4), 4), ((3, 5, 0, 1, 2, 4), 2)):
+        cases.append((O.bonds, [0, 1, 2, 3, 4, 5], list(perm), rn))
     for bonds, labels, new, rn in cases:
         x = rng.uniform(-1, 1, wl.elem_count(bonds))
         t = st.UniTensor(to_bonds(bonds), labels, x)

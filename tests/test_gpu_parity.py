@@ -211,6 +211,22 @@ def test_large_dense_permute_bit_exact(tu):
     assert np.array_equal(t.get_elem(), want2)
 
 
+def test_dense_permutes_with_short_contiguous_bonds_bit_exact(tu):
+    """The MERA ascend's permutes where both the destination- and the
+    source-contiguous bond are short (chi = 12 here): transpose tiles of
+    several stacked planes, ragged in every direction (chi = 13)."""
+    for chi in (12, 13):
+        bonds = [wl.dense_bond(1, chi)] * 3 + [wl.dense_bond(-1, chi)] * 3
+        rng = np.random.default_rng(chi)
+        x = rng.standard_normal(chi ** 6)
+        for perm, rn in (((0, 3, 5, 1, 2, 4), 3), ((1, 2, 3, 5, 0, 4), 4), ((2, 3, 5, 0, 1, 4), 3),
+                         ((0, 2, 3, 5, 1, 4), 4), ((3, 5, 0, 1, 2, 4), 2)):
+            t = tu.UniTensor(bonds, list(range(6)), x)
+            t.permute(list(perm), rn)
+            want = x.reshape([chi] * 6).transpose(perm).ravel()
+            assert np.array_equal(t.get_elem(), want), (chi, perm)
+
+
 def test_errors_on_device_path(tu):
     from trim_gb300 import capi
 

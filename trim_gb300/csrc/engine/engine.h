@@ -119,10 +119,12 @@ struct PermSub {
   int32_t ydim;   // index of the source-contiguous dim used as tile y (-1: none)
   int32_t tx, ty; // tile extents along x (= dims[ndim-1]) and y
   int32_t ntx, nty;
-  int64_t nouter;     // product of the dims other than x and y
+  int32_t zdim;   // mode 2: a third dim stacked into the tile (-1: none)
+  int32_t tz, ntz;
+  int64_t nouter;     // product of the dims other than x, y and z
   int64_t tile_begin; // first tile index of this sub-block
   double sign;        // +1 (bosonic); a fermionic sign would go here
-  int32_t mode;       // 0: lanes along x; 1: shared-memory transpose (x, y)
+  int32_t mode;       // 0: lanes along x; 1: shared-memory transpose (x, y); 2: the same over tz planes (x, y, z)
 };
 struct PermPlan {
   DevBufP subs;  // PermSub[nsub]

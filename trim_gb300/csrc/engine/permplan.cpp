@@ -20,9 +20,16 @@ struct Dim {
 //         best source dim); y = the next destination dim, several rows/tile.
 // mode 1: 2-D transpose through shared memory: loads run along y (the
 //         source-contiguous dim), stores along x.
+// mode 2: when a transpose tile of x and y is small (short bonds, e.g. 24 x
+//         24), a third dim z is stacked into it (tz planes of x by y) so
+//         that each tile still moves thousands of elements; z is the dim
+//         with the smallest source or destination stride (it extends a
+//         contiguous run on one side).
 void choose_tile(PermSub& ps) {
   const int n = ps.ndim;
   ps.ydim = -1;
+  ps.zdim = -1;
+  ps.tz = ps.ntz = 1;
   ps.mode = 0;
   if (n == 0) {
     ps.tx = ps.ty = 1;
@@ -54,11 +61,31 @@ void choose_tile(PermSub& ps) {
       ps.ty = 1;
     }
   }
+  if (ps.mode == 1 && (int64_t)ps.tx * ps.ty <= 2048 && n >= 3) {
+    int z = -1;
+    int64_t best = 0;
+    for (int i = 0; i < n; i++) {
+      if (i == x || i == y) continue;
+      const int64_t c = std::min(ps.sstride[i], ps.dstride[i]);
+      if (z < 0 || c < best) {
+        z = i;
+        best = c;
+      }
+    }
+    const int64_t tz = std::min<int64_t>({(int64_t)ps.dims[z], (int64_t)(64 * 65) / ((int64_t)ps.ty * (ps.tx + 1)),
+                                         (int64_t)4096 / ((int64_t)ps.tx * ps.ty)});
+    if (tz > 1) {
+      ps.mode = 2;
+      ps.zdim = z;
+      ps.tz = (int32_t)tz;
+    }
+  }
   ps.ntx = (int32_t)((ps.dims[x] + ps.tx - 1) / ps.tx);
   ps.nty = ps.ydim >= 0 ? (int32_t)((ps.dims[ps.ydim] + ps.ty - 1) / ps.ty) : 1;
+  ps.ntz = ps.zdim >= 0 ? (int32_t)((ps.dims[ps.zdim] + ps.tz - 1) / ps.tz) : 1;
   int64_t outer = 1;
   for (int i = 0; i < n; i++)
-    if (i != x && i != ps.ydim) outer *= ps.dims[i];
+    if (i != x && i != ps.ydim && i != ps.zdim) outer *= ps.dims[i];
   ps.nouter = outer;
 }
 
@@ -381,7 +408,7 @@ PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num) {
   for (auto& ps : subs) {
     ps.tile_begin = tiles;
     tile_start.push_back(tiles);
-    tiles += ps.nouter * ps.ntx * ps.nty;
+    tiles += ps.nouter * ps.ntx * ps.nty * ps.ntz;
   }
   tile_start.push_back(tiles);
   plan->nsub = (int)subs.size();

@@ -341,6 +341,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
         uint32_t touched = 0;
         for (int kt = k0; kt < k1 && ok; kt++) {
           const int sb = nb % kBRing;
+          const int nks = min(kTK, S.K - kt * kTK + 15) >> 4;  // 16-k steps of this tile holding data
           if (!__all_sync(0xffffffffu, mbar_wait(&sh.fullB[sb], (nb / kBRing) & 1, &sh.abort))) { ok = false; break; }
           tc_fence_after();
           const uint32_t b_addr = smem_u32(bbuf + sb * NS * kBTile);
@@ -356,11 +357,18 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
               const int lvl = min(s + t, LV - 1);
               const uint64_t bdesc = desc_sw128(b_addr + t * kBTile);
               const uint32_t d = tmem + lvl * kTN;
+              if (nks == kTK / 16) {  // a full 64-k tile: no per-step guard in the issue stream
 #pragma unroll
-              for (int kk = 0; kk < kTK / 16; kk++) {
-                // advancing K by 16 bf16 = 32 bytes inside the swizzle atom: +2 in the address field
-                mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
-                touched |= 1u << lvl;
+                for (int kk = 0; kk < kTK / 16; kk++) {
+                  // advancing K by 16 bf16 = 32 bytes inside the swizzle atom: +2 in the address field
+                  mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
+                  touched |= 1u << lvl;
+                }
+              } else {  // the last tile of a ragged K: only the 16-k steps that hold data
+                for (int kk = 0; kk < nks; kk++) {
+                  mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
+                  touched |= 1u << lvl;
+                }
               }
             }
             mma_commit_elect(&sh.emptyA[sa]);

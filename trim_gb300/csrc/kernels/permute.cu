@@ -5,7 +5,8 @@
 // 2-D piece (x, y) of one canonical sub-block copy (see PermSub): x is the
 // destination-contiguous dim, so stores are coalesced; in mode 1 y is the
 // source-contiguous dim and the tile is transposed through shared memory so
-// loads are coalesced too.  Remaining dims are decoded once per tile.
+// loads are coalesced too; mode 2 stacks tz planes of a third dim z into a
+// small transpose tile.  Remaining dims are decoded once per tile.
 #include <vector>
 
 #include "../engine/engine.h"
@@ -19,9 +20,9 @@ constexpr int kSmem = 64 * 65;  // >= ty * (tx + 1) of every transpose tile (che
 
 struct TileInfo {
   int64_t bs, bd;     // base offsets of the tile origin
-  int64_t sx, sy, dx, dy;
-  int32_t nx, ny;     // valid extents of this tile
-  int32_t tx, ty;     // full tile extents
+  int64_t sx, sy, sz, dx, dy, dz;
+  int32_t nx, ny, nz; // valid extents of this tile
+  int32_t tx, ty, tz; // full tile extents
   int32_t mode, neg;
 };
 
@@ -45,20 +46,22 @@ __host__ __device__ inline TileInfo decode_tile(const PermSub& P, int64_t local)
   int64_t bs = P.src_base, bd = P.dst_base;
   TileInfo w;
   if (n == 0) {
-    w.nx = w.ny = w.tx = w.ty = 1;
-    w.sx = w.sy = w.dx = w.dy = 0;
+    w.nx = w.ny = w.nz = w.tx = w.ty = w.tz = 1;
+    w.sx = w.sy = w.sz = w.dx = w.dy = w.dz = 0;
     w.mode = 0;
   } else {
-    const int x = n - 1, y = P.ydim;
-    int64_t xt, yt;
+    const int x = n - 1, y = P.ydim, z = P.zdim;
+    int64_t xt, yt, zt;
     if (local < 0x7fffffffLL) {  // 32-bit division is several times cheaper
       uint32_t l = (uint32_t)local;
       xt = l % (uint32_t)P.ntx;
       l /= (uint32_t)P.ntx;
       yt = l % (uint32_t)P.nty;
       l /= (uint32_t)P.nty;
+      zt = l % (uint32_t)P.ntz;
+      l /= (uint32_t)P.ntz;
       for (int i = n - 1; i >= 0 && l; --i) {  // outer dims, innermost first
-        if (i == x || i == y) continue;
+        if (i == x || i == y || i == z) continue;
         uint32_t c = l % (uint32_t)P.dims[i];
         l /= (uint32_t)P.dims[i];
         bs += (int64_t)c * P.sstride[i];
@@ -69,13 +72,27 @@ __host__ __device__ inline TileInfo decode_tile(const PermSub& P, int64_t local)
       local /= P.ntx;
       yt = local % P.nty;
       local /= P.nty;
+      zt = local % P.ntz;
+      local /= P.ntz;
       for (int i = n - 1; i >= 0; --i) {
-        if (i == x || i == y) continue;
+        if (i == x || i == y || i == z) continue;
         int64_t c = local % P.dims[i];
         local /= P.dims[i];
         bs += c * P.sstride[i];
         bd += c * P.dstride[i];
       }
+    }
+    if (z >= 0) {
+      const int64_t z0 = zt * P.tz;
+      bs += z0 * P.sstride[z];
+      bd += z0 * P.dstride[z];
+      w.sz = P.sstride[z];
+      w.dz = P.dstride[z];
+      w.tz = P.tz;
+      w.nz = (int32_t)((P.dims[z] - z0) < P.tz ? (P.dims[z] - z0) : P.tz);
+    } else {
+      w.sz = w.dz = 0;
+      w.tz = w.nz = 1;
     }
     int64_t x0 = xt * P.tx;
     bs += x0 * P.sstride[x];
@@ -127,7 +144,21 @@ __device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, con
     const PermSub& P = subs[find_sub(tile_start, nsub, t)];
     const TileInfo w = decode_tile(P, t - P.tile_begin);
     if (threadIdx.x == 0) *info = w;
-    if (w.mode == 0) {
+    if (w.mode == 2) {
+      // [z][y][x] with pitch tx + 1; lanes along y (source-contiguous), then x, then z
+      const int pitch = w.tx + 1, e_end = w.tz * w.ty * w.tx;
+      const uint64_t my = ((1ull << 32) + w.ty - 1) / w.ty, mx = ((1ull << 32) + w.tx - 1) / w.tx;
+#pragma unroll 4
+      for (int k = 0; k < kPerThread; k++) {
+        const uint32_t e = threadIdx.x + k * kThreads;
+        if ((int)e >= e_end) break;
+        const uint32_t ry = (uint32_t)(((uint64_t)e * my) >> 32), yy = e - ry * w.ty;  // e / ty, e % ty
+        const uint32_t zz = (uint32_t)(((uint64_t)ry * mx) >> 32), xx = ry - zz * w.tx;
+        if ((int)xx < w.nx && (int)yy < w.ny && (int)zz < w.nz)
+          cp_async8(buf + (zz * w.ty + yy) * pitch + xx,
+                    src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx + (int64_t)zz * w.sz);
+      }
+    } else if (w.mode == 0) {
       const int q = kThreads / w.tx, r = kThreads - q * w.tx;
       const int y0 = threadIdx.x / w.tx, x0 = threadIdx.x - y0 * w.tx;
       if (r == 0) {  // constant step: q whole rows
@@ -176,6 +207,22 @@ __device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, con
 
 // Store a landed tile from shared memory with lanes along x (destination-contiguous).
 __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf, double* __restrict__ dst) {
+  if (w.mode == 2) {  // lanes along x, then y, then z
+    const int pitch = w.tx + 1, e_end = w.tz * w.ty * w.tx;
+    const uint64_t mx = ((1ull << 32) + w.tx - 1) / w.tx, my = ((1ull << 32) + w.ty - 1) / w.ty;
+#pragma unroll 4
+    for (int k = 0; k < kPerThread; k++) {
+      const uint32_t e = threadIdx.x + k * kThreads;
+      if ((int)e >= e_end) break;
+      const uint32_t rx = (uint32_t)(((uint64_t)e * mx) >> 32), xx = e - rx * w.tx;  // e / tx, e % tx
+      const uint32_t zz = (uint32_t)(((uint64_t)rx * my) >> 32), yy = rx - zz * w.ty;
+      if ((int)xx < w.nx && (int)yy < w.ny && (int)zz < w.nz) {
+        const double v = buf[(zz * w.ty + yy) * pitch + xx];
+        dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx + (int64_t)zz * w.dz] = w.neg ? -v : v;
+      }
+    }
+    return;
+  }
   const int pitch = w.mode == 0 ? w.tx : w.tx + 1;
   const int q = kThreads / w.tx, r = kThreads - q * w.tx;
   const int y0 = threadIdx.x / w.tx, x0 = threadIdx.x - y0 * w.tx;
@@ -251,18 +298,24 @@ int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double*
   for (int64_t t = 0; t < plan.ntiles; t++) {
     const PermSub& P = plan.host_subs[find_sub(plan.host_tile_start.data(), plan.nsub, t)];
     TileInfo w = decode_tile(P, t - P.tile_begin);
-    if (w.nx > w.tx || w.ny > w.ty || w.nx <= 0 || w.ny <= 0) fail(TN_ERR_ARG, "plan check: bad tile extents");
-    if (w.mode == 1 && w.ty * (w.tx + 1) > kSmem) fail(TN_ERR_ARG, "plan check: tile exceeds shared memory");
-    if ((int64_t)w.tx * w.ty > (int64_t)kThreads * kPerThread) fail(TN_ERR_ARG, "plan check: tile exceeds thread walk");
-    for (int yy = 0; yy < w.ny; yy++)
-      for (int xx = 0; xx < w.nx; xx++) {
-        int64_t so = w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx;
-        int64_t d = w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx;
-        if (so < 0 || so >= n || d < 0 || d >= n) fail(TN_ERR_ARG, "plan check: offset out of range");
-        if (hit[d]++) fail(TN_ERR_ARG, "plan check: destination written twice");
-        dst[d] = w.neg ? -src[so] : src[so];
-        written++;
-      }
+    if (w.nx > w.tx || w.ny > w.ty || w.nz > w.tz || w.nx <= 0 || w.ny <= 0 || w.nz <= 0)
+      fail(TN_ERR_ARG, "plan check: bad tile extents");
+    if (w.mode != 2 && w.tz != 1) fail(TN_ERR_ARG, "plan check: stacked planes outside mode 2");
+    if (w.mode >= 1 && (int64_t)w.tz * w.ty * (w.tx + 1) > kSmem) fail(TN_ERR_ARG, "plan check: tile exceeds shared memory");
+    if ((int64_t)w.tx * w.ty * w.tz > (int64_t)kThreads * kPerThread)
+      fail(TN_ERR_ARG, "plan check: tile exceeds thread walk");
+    if (w.mode == 2 && ((int64_t)w.tx * w.ty * w.tz >= (1 << 16) || w.tx > 4096 || w.ty > 4096))
+      fail(TN_ERR_ARG, "plan check: tile index exceeds the multiply-high division range");
+    for (int zz = 0; zz < w.nz; zz++)
+      for (int yy = 0; yy < w.ny; yy++)
+        for (int xx = 0; xx < w.nx; xx++) {
+          int64_t so = w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx + (int64_t)zz * w.sz;
+          int64_t d = w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx + (int64_t)zz * w.dz;
+          if (so < 0 || so >= n || d < 0 || d >= n) fail(TN_ERR_ARG, "plan check: offset out of range");
+          if (hit[d]++) fail(TN_ERR_ARG, "plan check: destination written twice");
+          dst[d] = w.neg ? -src[so] : src[so];
+          written++;
+        }
   }
   return written;
 }
