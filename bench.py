@@ -425,9 +425,10 @@ def permute_main(args, rank, local, world):
     t = tu.UniTensor(bonds, list(range(6)))
     torch.cuda.synchronize()
     tu.capi.call("tn_tensor_set_elem_device", t.h, x.data_ptr(), n)
-    perm = [4, 5, 0, 1, 2, 3]
+    perm = [int(v) for v in args.perm.split(",")]
+    rn = args.perm_rownum
     src_map = tu.SectorMap(bonds)
-    dst_bonds = [wl.change(bonds[p], 1 if i < 2 else -1) for i, p in enumerate(perm)]
+    dst_bonds = [wl.change(bonds[p], 1 if i < rn else -1) for i, p in enumerate(perm)]
     dst_map = tu.SectorMap(dst_bonds)
     y = torch.empty_like(x)
     for _ in range(args.warmup):
@@ -695,7 +696,8 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="split", choices=["fp64", "split", "bf16"])
+    ap.add_argument("--mode", default="split", choices=["fp64", "split", "bf16", "split_fused", "split_tiled"],
+                    help="iTEBD: the tensor-core mode timed beside FP64 (split_fused / split_tiled force that form)")
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--clock-seconds", type=float, default=1.0,
@@ -706,6 +708,8 @@ def main():
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--modes", default="split,bf16")
     ap.add_argument("--chi", type=int, default=24)
+    ap.add_argument("--perm", default="4,5,0,1,2,3", help="permute workload: the new bond order")
+    ap.add_argument("--perm-rownum", type=int, default=2, help="permute workload: incoming bonds after the permute")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, local, world = dist_env()

@@ -428,7 +428,11 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
 #pragma unroll
         for (int j = 0; j < kTN; j++) {
           const int64_t jj = (int64_t)w.z * kTN + j;
-          if (jj < S.N) crow[jj] = ldexp((double)hi[j] + (double)lo[j], e_i + exp_of(eb[S.eb_off + jj]) - 14);
+          // three FP64-pipe operations per output (two conversions, one add),
+          // the power-of-two scale on the exponent field: the epilogue warps
+          // share their schedulers with the MMA and load warps, so a long
+          // integer sequence here would slow the MMA issue instead
+          if (jj < S.N) crow[jj] = scale_pow2((double)hi[j] + (double)lo[j], e_i + exp_of(eb[S.eb_off + jj]) - 14);
         }
       }
     }

@@ -121,6 +121,12 @@ __host__ __device__ inline TileInfo decode_tile(const PermSub& P, int64_t local)
   return w;
 }
 
+// x with its sign flipped when flip is set: an integer XOR on the sign bit
+// (a floating-point negation would run on the FP64 pipe, ~2 per clock per SM)
+__device__ __forceinline__ double flip_sign(double x, uint64_t flip) {
+  return __longlong_as_double((long long)((uint64_t)__double_as_longlong(x) ^ flip));
+}
+
 __device__ __forceinline__ void cp_async8(double* smem, const double* gmem) {
   unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
@@ -145,18 +151,24 @@ __device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, con
     const TileInfo w = decode_tile(P, t - P.tile_begin);
     if (threadIdx.x == 0) *info = w;
     if (w.mode == 2) {
-      // [z][y][x] with pitch tx + 1; lanes along y (source-contiguous), then x, then z
-      const int pitch = w.tx + 1, e_end = w.tz * w.ty * w.tx;
-      const uint64_t my = ((1ull << 32) + w.ty - 1) / w.ty, mx = ((1ull << 32) + w.tx - 1) / w.tx;
+      // [z][y][x] with pitch tx + 1; lanes along y (source-contiguous), then
+      // x, then z.  Each thread steps its (y, x, z) counter by kThreads
+      // elements with carries (no division per element).
+      const int pitch = w.tx + 1;
+      const int dy = kThreads % w.ty, t1 = kThreads / w.ty, dx = t1 % w.tx, dz = t1 / w.tx;
+      int yy = threadIdx.x % w.ty, xx = (threadIdx.x / w.ty) % w.tx, zz = threadIdx.x / (w.ty * w.tx);
 #pragma unroll 4
-      for (int k = 0; k < kPerThread; k++) {
-        const uint32_t e = threadIdx.x + k * kThreads;
-        if ((int)e >= e_end) break;
-        const uint32_t ry = (uint32_t)(((uint64_t)e * my) >> 32), yy = e - ry * w.ty;  // e / ty, e % ty
-        const uint32_t zz = (uint32_t)(((uint64_t)ry * mx) >> 32), xx = ry - zz * w.tx;
-        if ((int)xx < w.nx && (int)yy < w.ny && (int)zz < w.nz)
+      for (int k = 0; k < kPerThread && zz < w.tz; k++) {
+        if (xx < w.nx && yy < w.ny && zz < w.nz)
           cp_async8(buf + (zz * w.ty + yy) * pitch + xx,
                     src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx + (int64_t)zz * w.sz);
+        yy += dy;
+        const int c1 = yy >= w.ty;
+        yy -= c1 * w.ty;
+        xx += dx + c1;
+        const int c2 = xx >= w.tx;
+        xx -= c2 * w.tx;
+        zz += dz + c2;
       }
     } else if (w.mode == 0) {
       const int q = kThreads / w.tx, r = kThreads - q * w.tx;
@@ -207,19 +219,24 @@ __device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, con
 
 // Store a landed tile from shared memory with lanes along x (destination-contiguous).
 __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf, double* __restrict__ dst) {
-  if (w.mode == 2) {  // lanes along x, then y, then z
-    const int pitch = w.tx + 1, e_end = w.tz * w.ty * w.tx;
-    const uint64_t mx = ((1ull << 32) + w.tx - 1) / w.tx, my = ((1ull << 32) + w.ty - 1) / w.ty;
+  const uint64_t flip = w.neg ? 0x8000000000000000ull : 0ull;
+  if (w.mode == 2) {  // lanes along x, then y, then z; counters stepped as in the loads
+    const int pitch = w.tx + 1;
+    const int dx = kThreads % w.tx, t1 = kThreads / w.tx, dy = t1 % w.ty, dz = t1 / w.ty;
+    int xx = threadIdx.x % w.tx, yy = (threadIdx.x / w.tx) % w.ty, zz = threadIdx.x / (w.tx * w.ty);
 #pragma unroll 4
-    for (int k = 0; k < kPerThread; k++) {
-      const uint32_t e = threadIdx.x + k * kThreads;
-      if ((int)e >= e_end) break;
-      const uint32_t rx = (uint32_t)(((uint64_t)e * mx) >> 32), xx = e - rx * w.tx;  // e / tx, e % tx
-      const uint32_t zz = (uint32_t)(((uint64_t)rx * my) >> 32), yy = rx - zz * w.ty;
-      if ((int)xx < w.nx && (int)yy < w.ny && (int)zz < w.nz) {
+    for (int k = 0; k < kPerThread && zz < w.tz; k++) {
+      if (xx < w.nx && yy < w.ny && zz < w.nz) {
         const double v = buf[(zz * w.ty + yy) * pitch + xx];
-        dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx + (int64_t)zz * w.dz] = w.neg ? -v : v;
+        dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx + (int64_t)zz * w.dz] = flip_sign(v, flip);
       }
+      xx += dx;
+      const int c1 = xx >= w.tx;
+      xx -= c1 * w.tx;
+      yy += dy + c1;
+      const int c2 = yy >= w.ty;
+      yy -= c2 * w.ty;
+      zz += dz + c2;
     }
     return;
   }
@@ -233,7 +250,7 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf,
       double* g = dst + w.bd + (int64_t)y0 * w.dy + (int64_t)x0 * w.dx;
       const int64_t gstep = (int64_t)q * w.dy;
       if (w.neg) {
-        for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = -*sp;
+        for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = flip_sign(*sp, flip);
       } else {
         for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = *sp;
       }
@@ -245,7 +262,7 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf,
   for (int k = 0; k < kPerThread; k++) {
     if (yy < w.ny && xx < w.nx) {
       double v = buf[yy * pitch + xx];
-      dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx] = w.neg ? -v : v;
+      dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx] = flip_sign(v, flip);
     }
     xx += r;
     yy += q;

@@ -87,5 +87,31 @@ __device__ __forceinline__ void make_slices(const double (&x)[8], int e, uint4 (
                         __byte_perm(hbits[s][4], hbits[s][5], 0x7632), __byte_perm(hbits[s][6], hbits[s][7], 0x7632));
 }
 
+// S * 2^q as the nearest double (ties to even), integer operations only (the
+// FP64 units and FP64 conversions run at ~2 per clock per SM on GB300)
+__device__ __forceinline__ double fixed_to_double(long long S, int q) {
+  if (S == 0) return 0.0;
+  const uint64_t sign = (uint64_t)S & (1ull << 63);
+  uint64_t mag = S < 0 ? (uint64_t)(-S) : (uint64_t)S;
+  const int lz = __clzll((long long)mag);
+  mag <<= lz;                                        // leading one at bit 63
+  const int E = 63 - lz + q;                         // value = mag * 2^(E - 63)
+  const uint32_t rem = (uint32_t)mag & 0x7FFu;
+  const uint64_t r = (mag >> 11) + (uint64_t)((rem > 0x400u) | ((rem == 0x400u) & (uint32_t)(mag >> 11)));  // ties to even; may reach 2^53
+  if (E < -1021 || E > 1022) return ldexp(__ll2double_rn(S), q);     // near the ends of the range: slow path
+  // the hidden bit of r adds one to the exponent field (two when r carried to 2^53)
+  return __longlong_as_double((long long)(sign | (((uint64_t)(E + 1022) << 52) + r)));
+}
+
+
+// d * 2^q for a finite double d, the exponent field adjusted as an integer
+// when the result stays normal (else ldexp)
+__device__ __forceinline__ double scale_pow2(double d, int q) {
+  const uint64_t b = (uint64_t)__double_as_longlong(d);
+  const int ex = (int)((b >> 52) & 0x7FF);
+  if (ex == 0 || ex + q < 1 || ex + q > 2046) return ldexp(d, q);
+  return __longlong_as_double((long long)(b + ((uint64_t)(int64_t)q << 52)));
+}
+
 }  // namespace
 }  // namespace tn
