@@ -157,7 +157,10 @@ struct GemmTile {
 struct Fp64Policy {
   int tn_rule = 0;
   int items_per_sm = 8;
-  bool operator==(const Fp64Policy& o) const { return tn_rule == o.tn_rule && items_per_sm == o.items_per_sm; }
+  int spread = 4;  // with fewer than spread x SMs tiles, K is split until there are about that many items (0: never)
+  bool operator==(const Fp64Policy& o) const {
+    return tn_rule == o.tn_rule && items_per_sm == o.items_per_sm && spread == o.spread;
+  }
 };
 
 // A permuted operand read in place by the FP64 GEMM (the permute fused into

@@ -48,8 +48,9 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
     int nsplit = 1;
     if (allow_split) {
       nsplit = (int)std::ceil((double)g.K / kmax);
-      if (tiles < (int64_t)num_sms * 4)  // few tiles: spread the K loop over the chip
-        nsplit = std::max<int>(nsplit, (int)std::min<int64_t>((num_sms * 4 + tiles - 1) / tiles, (g.K + 15) / 16));
+      if (pol.spread > 0 && tiles < (int64_t)num_sms * pol.spread)  // few tiles: spread the K loop over the chip
+        nsplit = std::max<int>(nsplit, (int)std::min<int64_t>(((int64_t)num_sms * pol.spread + tiles - 1) / tiles,
+                                                              (g.K + 15) / 16));
       nsplit = std::max(1, std::min(nsplit, 256));
     }
     const int kchunk = (int)((g.K + nsplit - 1) / nsplit);
@@ -114,7 +115,7 @@ static std::shared_ptr<Fp64Plan> get_fp64_plan(Ctx& ctx, const std::vector<tn_se
                                                const Fp64Policy& pol,
                                                const std::vector<std::pair<int, int>>* vw = nullptr,
                                                const void* table = nullptr) {
-  uint64_t key = hash_list(list, 64 + 16 * pol.tn_rule + pol.items_per_sm);
+  uint64_t key = hash_list(list, 64 + 16 * pol.tn_rule + pol.items_per_sm + 1024 * pol.spread);
   if (vw) {
     for (const auto& v : *vw) key = (key ^ (uint64_t)(uint32_t)v.first ^ ((uint64_t)(uint32_t)v.second << 32)) * 1099511628211ull;
     key ^= (uint64_t)(uintptr_t)table;
@@ -201,33 +202,39 @@ const std::vector<Fp64Policy>& fp64_candidates() {
   static const std::vector<Fp64Policy> c = [] {
     std::vector<Fp64Policy> v;
     for (int rule : {0, 1})
-      for (int items : {4, 8, 16}) {
-        Fp64Policy p;
-        p.tn_rule = rule;
-        p.items_per_sm = items;
-        v.push_back(p);
-      }
+      for (int items : {2, 8, 16})
+        for (int spread : {0, 1, 2, 4}) {
+          Fp64Policy p;
+          p.tn_rule = rule;
+          p.items_per_sm = items;
+          p.spread = spread;
+          v.push_back(p);
+        }
     return v;
   }();
   return c;
 }
 
-// Times every candidate once on this call's operands (CUDA events on the
-// context's stream, outside any graph capture) and keeps the fastest for the
-// histogram key; the winner's result is the one left in C.
+// Times every candidate on this call's operands (CUDA events on the
+// context's stream, outside any graph capture; three launches after a warm-up)
+// and keeps the fastest for the histogram key; the caller then runs the
+// winner, whose result is the one left in C.  With vw the operands are read
+// through views (table = the view table, views / pool its device arrays).
 static Fp64Policy tune_fp64(Ctx& ctx, uint64_t key, const std::vector<tn_sector_gemm>& list, const double* A,
-                            const double* B, double* C) {
+                            const double* B, double* C, const std::vector<std::pair<int, int>>* vw = nullptr,
+                            const void* table = nullptr, const ViewHdr* views = nullptr,
+                            const int64_t* pool = nullptr) {
   cudaEvent_t e0, e1;
   TN_CUDA(cudaEventCreate(&e0));
   TN_CUDA(cudaEventCreate(&e1));
   Fp64Policy best;
   float best_ms = -1.0f;
   for (const auto& pol : fp64_candidates()) {
-    auto P = get_fp64_plan(ctx, list, pol);
+    auto P = get_fp64_plan(ctx, list, pol, vw, table);
     if (!P->ntiles) continue;
-    launch_fp64_plan(ctx, *P, A, B, C);  // warm the plan and the caches
+    launch_fp64_plan(ctx, *P, A, B, C, views, pool);  // warm the plan and the caches
     TN_CUDA(cudaEventRecord(e0, ctx.stream));
-    launch_fp64_plan(ctx, *P, A, B, C);
+    for (int r = 0; r < 3; r++) launch_fp64_plan(ctx, *P, A, B, C, views, pool);
     TN_CUDA(cudaEventRecord(e1, ctx.stream));
     TN_CUDA(cudaEventSynchronize(e1));
     float ms = 0;
@@ -441,7 +448,16 @@ void run_sector_gemms_views(Ctx& ctx, int mode, const std::vector<tn_sector_gemm
   const int ns = (mode & ~kModeFlags) == TN_MODE_SPLIT ? 7 : 1;
   auto fused = [&] { run_tc_fused(ctx, ns, list, A, B, C, &vw, views, pool, T.get()); };
   auto fp64 = [&] {
-    auto P = get_fp64_plan(ctx, list, Fp64Policy(), &vw, T.get());
+    Fp64Policy pol;
+    if (ctx.autotune) {  // the FP64 tile policy tuned per histogram, as run_fp64 does
+      const uint64_t key = sector_histogram_key(list) ^ 0x5A17ull;  // views: a key of its own
+      auto it = ctx.tuned.find(key);
+      if (it != ctx.tuned.end())
+        pol = it->second;
+      else if (!capturing(ctx))
+        pol = tune_fp64(ctx, key, list, A, B, C, &vw, T.get(), views, pool);
+    }
+    auto P = get_fp64_plan(ctx, list, pol, &vw, T.get());
     if (P->ntiles) launch_fp64_plan(ctx, *P, A, B, C, views, pool);
   };
   const bool tuned = ctx.route_tuned.count(route_key(mode, list)) > 0;
