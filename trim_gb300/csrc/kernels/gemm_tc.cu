@@ -22,7 +22,9 @@
 // (16 KB per slice); B tile: 64 columns x 64 k (8 KB per slice).
 //
 // GEMM CTA (192 threads): warp 0 = loads (bulk copies), warp 1 = MMA issue +
-// TMEM allocation, warps 2..5 = epilogue (TMEM lane quadrants 2,3,0,1).
+// TMEM allocation, warps 2..9 = epilogue (TMEM lane quadrants 2,3,0,1,2,3,0,1;
+// warps 2..5 drain columns 0..31 of every accumulator, warps 6..9 columns
+// 32..63, so a chunk's drain -- during which the MMAs wait -- takes half as long).
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -43,7 +45,8 @@ constexpr int kARing = 6, kBRing = 2;
 constexpr int kChunkTiles = 9;  // 576 k per exact-accumulation chunk
 constexpr int kLevels = 6;      // exact levels 0..4 + one shared accumulator for 5..7
 constexpr int kMaxLevel = 7;    // digit products with s + t <= 7 are kept
-constexpr int kThreadsTc = 192;
+constexpr int kThreadsTc = 320;
+constexpr int kEpiCols = kTN / 2;  // accumulator columns per epilogue warp
 
 __device__ __forceinline__ int find_seg(const int64_t* __restrict__ start, int n, int64_t v) {
   int lo = 0, hi = n - 1;  // largest i with start[i] <= v
@@ -272,7 +275,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
       mbar_init(&sh.emptyB[i], 1);
     }
     mbar_init(&sh.acc_full, 1);
-    mbar_init(&sh.acc_empty, 4);
+    mbar_init(&sh.acc_empty, 8);
     mbar_init(&sh.mma_done, 1);
     sh.abort = 0;
     fence_mbar_init();
@@ -388,15 +391,16 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
   } else {
     // ------------------------------------------------ epilogue
     const int quad = warp & 3;  // TMEM lanes 32*quad .. +31
-    const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16);
+    const int half = (warp - 2) >> 2;  // accumulator columns half*32 .. +31
+    const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16) + half * kEpiCols;
     uint32_t nchunk = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
       const int4 w = items[it];
       const TcSector& S = secs[w.x];
-      float hi[kTN], lo[kTN];
+      float hi[kEpiCols], lo[kEpiCols];
 #pragma unroll
-      for (int j = 0; j < kTN; j++) hi[j] = lo[j] = 0.f;
+      for (int j = 0; j < kEpiCols; j++) hi[j] = lo[j] = 0.f;
       const int kb = w.w * S.kts, ke = min(S.nkt, kb + S.kts);
       for (int k0 = kb; k0 < ke; k0 += kChunk) {
         if (!mbar_wait(&sh.acc_full, nchunk & 1, &sh.abort)) { ok = false; break; }
@@ -404,7 +408,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
 #pragma unroll
         for (int l = 0; l < LV; l++) {
 #pragma unroll
-          for (int cg = 0; cg < kTN / 16; cg++) {
+          for (int cg = 0; cg < kEpiCols / 16; cg++) {
             float v[16];
             tmem_ld16(lane_addr + l * kTN + cg * 16, v);
 #pragma unroll
@@ -426,8 +430,8 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
                                  (quad * 32 + lane) * kTN - (int64_t)w.z * kTN
                            : C + S.c_off + i * S.N;
 #pragma unroll
-        for (int j = 0; j < kTN; j++) {
-          const int64_t jj = (int64_t)w.z * kTN + j;
+        for (int j = 0; j < kEpiCols; j++) {
+          const int64_t jj = (int64_t)w.z * kTN + half * kEpiCols + j;
           // three FP64-pipe operations per output (two conversions, one add),
           // the power-of-two scale on the exponent field: the epilogue warps
           // share their schedulers with the MMA and load warps, so a long
