@@ -22,9 +22,9 @@
 // (16 KB per slice); B tile: 64 columns x 64 k (8 KB per slice).
 //
 // GEMM CTA (192 threads): warp 0 = loads (bulk copies), warp 1 = MMA issue +
-// TMEM allocation, warps 2..9 = epilogue (TMEM lane quadrants 2,3,0,1,2,3,0,1;
-// warps 2..5 drain columns 0..31 of every accumulator, warps 6..9 columns
-// 32..63, so a chunk's drain -- during which the MMAs wait -- takes half as long).
+// TMEM allocation, warps 2..17 = epilogue: warp w drains TMEM lane quadrant
+// w & 3 and columns 16 * ((w - 2) >> 2) .. +15 of every accumulator, so a
+// chunk's drain -- during which the MMAs wait -- is spread over 16 warps.
 #include <cuda_bf16.h>
 
 #include <cstdint>
@@ -45,8 +45,9 @@ constexpr int kARing = 6, kBRing = 2;
 constexpr int kChunkTiles = 9;  // 576 k per exact-accumulation chunk
 constexpr int kLevels = 6;      // exact levels 0..4 + one shared accumulator for 5..7
 constexpr int kMaxLevel = 7;    // digit products with s + t <= 7 are kept
-constexpr int kThreadsTc = 320;
-constexpr int kEpiCols = kTN / 2;  // accumulator columns per epilogue warp
+constexpr int kEpiWarps = 16;
+constexpr int kThreadsTc = 64 + 32 * kEpiWarps;
+constexpr int kEpiCols = kTN * 4 / kEpiWarps;  // accumulator columns per epilogue warp
 
 __device__ __forceinline__ int find_seg(const int64_t* __restrict__ start, int n, int64_t v) {
   int lo = 0, hi = n - 1;  // largest i with start[i] <= v
@@ -275,7 +276,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
       mbar_init(&sh.emptyB[i], 1);
     }
     mbar_init(&sh.acc_full, 1);
-    mbar_init(&sh.acc_empty, 8);
+    mbar_init(&sh.acc_empty, kEpiWarps);
     mbar_init(&sh.mma_done, 1);
     sh.abort = 0;
     fence_mbar_init();
@@ -391,7 +392,7 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
   } else {
     // ------------------------------------------------ epilogue
     const int quad = warp & 3;  // TMEM lanes 32*quad .. +31
-    const int half = (warp - 2) >> 2;  // accumulator columns half*32 .. +31
+    const int half = (warp - 2) >> 2;  // accumulator columns half * kEpiCols .. +kEpiCols-1
     const uint32_t lane_addr = tmem + ((uint32_t)(quad * 32) << 16) + half * kEpiCols;
     uint32_t nchunk = 0;
     bool ok = true;
