@@ -247,25 +247,31 @@ def gpu_main(args, rank, local, world):
         prof = tu.prof_read()
         tu.prof_enable(False)
         flops = sum(v["flops"] for k_, v in prof.items() if "gemm" in k_) / args.steps
-        # end to end through the C ABI: pinned host inputs -> device tensors ->
-        # network, graph replay, theta -> pinned host
+        # end to end through the C ABI: the graph recaptured with the pinned
+        # host inputs bound (copied into the network's tensors at its start)
+        # and theta bound to a pinned host buffer (copied out at its end); a
+        # step is one replay and the synchronisation that completes it
         pinned = {n: torch.from_numpy(els[n]).pin_memory() for n in names}
         out_host = torch.empty(vals.size, dtype=torch.float64).pin_memory()
+        for n in names:
+            net.bind_host_input(n, pinned[n].data_ptr(), els[n].size)
+        net.bind_host_output(out_host.data_ptr(), vals.size)
+        net.capture(mode)
+        net.replay()
+        tu.sync()
+        e2e_ok = bool(np.array_equal(out_host.numpy(), vals))
         e2e = []
         for k in range(args.steps):
             with torch.cuda.stream(stream):
                 flush.fill_(float(k))
             torch.cuda.synchronize()
             w0 = time.perf_counter()
-            for n in names:
-                dev[n].set_elem_host_ptr(pinned[n].data_ptr(), els[n].size)
-                net.put_tensor(n, dev[n])
             net.replay()
-            tu.capi.call("tn_tensor_get_elem", out.h, out_host.data_ptr(), vals.size)
+            tu.sync()
             e2e.append((time.perf_counter() - w0) * 1e3)
         res[mode] = {"ms_graph": ms_graph, "ms_eager": ms_eager, "flops": flops, "err_vs_fp64": err,
                      "graph_matches_eager": graph_ok, "launches": int(launches), "clocks": clocks, "timed_repeats": reps,
-                     "e2e_ms": statistics.median(e2e), "prof": prof,
+                     "e2e_ms": statistics.median(e2e), "e2e_matches_device": e2e_ok, "prof": prof,
                      "h2d": sum(8 * els[n].size for n in names), "d2h": 8 * vals.size}
     if world > 1:
         for m in res:

@@ -215,6 +215,11 @@ int tn_tensor_destroy(tn_tensor_t t);
 int tn_tensor_copy(tn_tensor_t t, tn_tensor_t* out);
 /* setElem(const Real*, bool ongpu=false) / host read-back of getElem() */
 int tn_tensor_set_elem(tn_tensor_t t, const double* host, int64_t n);
+/* setElem without waiting for the copy (no reference counterpart): the host
+ * buffer must stay valid and unchanged until a synchronising call (e.g.
+ * tn_tensor_get_elem) returns; with pinned host memory the copy overlaps the
+ * caller's next calls */
+int tn_tensor_set_elem_async(tn_tensor_t t, const double* host, int64_t n);
 int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n);
 /* device-resident element buffer (getElem() on a device build) */
 int tn_tensor_device_elem(tn_tensor_t t, double** dev, int64_t* n);
@@ -268,6 +273,14 @@ int tn_network_tree(tn_network_t net, char* buf, int cap);
 int tn_network_capture(tn_network_t net, int mode);
 int tn_network_replay(tn_network_t net);
 int tn_network_output(tn_network_t net, tn_tensor_t* out);
+/* Host buffers (pinned memory) bound before tn_network_capture: the graph
+ * copies each bound input into the named tensor at its start and the result
+ * into the bound output at its end, so one replay is a whole host-to-host
+ * step (complete after the next synchronising call, e.g. tn_ctx_sync).  The
+ * buffers must stay valid while the graph exists; binding drops a captured
+ * graph.  No reference counterpart. */
+int tn_network_bind_host_input(tn_network_t net, const char* name, const double* host, int64_t n);
+int tn_network_bind_host_output(tn_network_t net, double* host, int64_t n);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,13 @@ class Network {
   void replay();
   const UniTensor& output() const;
   bool captured() const { return graph_exec != nullptr; }
+  // Not in the reference: host buffers (pinned memory) bound before capture()
+  // make the graph copy them into the named tensors at its start and the
+  // result into `out` at its end, so one replay() is a whole host-to-host
+  // step; the buffers must stay valid while the graph exists, and the output
+  // is complete after the next synchronising call.
+  void bindHostInput(const std::string& name, const double* host, size_t n);
+  void bindHostOutput(double* host, size_t n);
 
  private:
   Network() = default;
@@ -85,6 +92,10 @@ class Network {
   // device work lists and workspace the graph's kernels read, kept alive
   // while the graph exists (the context may replace or evict its own copies)
   std::vector<std::shared_ptr<void>> graph_keep;
+  std::vector<std::pair<size_t, const double*>> host_in;  // (tensor index, pinned buffer)
+  std::vector<size_t> host_in_n;
+  double* host_out = nullptr;
+  size_t host_out_n = 0;
   void drop_graph();
 };
 

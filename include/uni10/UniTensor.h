@@ -48,6 +48,11 @@ class UniTensor {
   // elements
   void setElem(const double* elem, bool _ongpu = false);
   void setElem(const std::vector<double>& elem, bool _ongpu = false);
+  // Not in the reference: setElem from host memory without waiting for the
+  // copy; the host buffer must stay valid and unchanged until the library's
+  // stream has passed it (any synchronising call, e.g. getElem to the host).
+  // With pinned host memory the copy overlaps the caller's next calls.
+  void setElemAsync(const double* host);
   double* getElem();               // device pointer
   std::vector<double> hostElem() const;
   double at(size_t idx) const;

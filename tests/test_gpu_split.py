@@ -279,3 +279,41 @@ def test_fused_form_reads_permuted_operands_in_place(env):
         assert counts["split_fused"] <= counts["fp64"], (case["id"], counts)
         seen_views += counts["fp64"] == 0
     assert seen_views > 0
+
+
+def test_graph_with_host_bound_inputs_and_output(env):
+    """Network capture with pinned host buffers bound: every replay copies the
+    current host inputs in and theta out; bit-identical to eager launches on
+    the same values, and it follows new host contents."""
+    torch, capi, tu = env
+    spec = wl.itebd()
+    rng = np.random.default_rng(spec["seed"])
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    net = tu.Network(spec["net"])
+    ts = {s.name: tu.UniTensor(s.bonds, s.labels, els[s.name]) for s in spec["tensors"]}
+    for n, t in ts.items():
+        net.put_tensor(n, t)
+    for mode in ("fp64", "split"):
+        eager = net.launch(mode).get_elem()
+        pinned = {n: torch.from_numpy(v.copy()).pin_memory() for n, v in els.items()}
+        out = torch.full((eager.size,), np.nan, dtype=torch.float64).pin_memory()
+        for n in ts:
+            net.bind_host_input(n, pinned[n].data_ptr(), els[n].size)
+        net.bind_host_output(out.data_ptr(), eager.size)
+        net.capture(mode)
+        net.replay()
+        tu.sync()
+        assert np.array_equal(out.numpy(), eager), mode
+        for i, n in enumerate(ts):
+            pinned[n].mul_(1.0 + 0.25 * (i + 1))
+        net.replay()
+        tu.sync()
+        for n, t in ts.items():
+            t.set_elem(pinned[n].numpy())
+            net.put_tensor(n, t)
+        eager2 = net.launch(mode).get_elem()
+        assert np.array_equal(out.numpy(), eager2), mode
+        assert not np.array_equal(eager2, eager)
+        for n, t in ts.items():  # back to the original values for the next mode
+            t.set_elem(els[n])
+            net.put_tensor(n, t)

@@ -79,6 +79,7 @@ _PROTOS = {
     "tn_tensor_destroy": (_I, [_P]),
     "tn_tensor_copy": (_I, [_P, C.POINTER(_P)]),
     "tn_tensor_set_elem": (_I, [_P, _DP, _I64]),
+    "tn_tensor_set_elem_async": (_I, [_P, _DP, _I64]),
     "tn_tensor_get_elem": (_I, [_P, _DP, _I64]),
     "tn_tensor_device_elem": (_I, [_P, C.POINTER(_P), _I64P]),
     "tn_tensor_set_elem_device": (_I, [_P, _DP, _I64]),
@@ -100,6 +101,8 @@ _PROTOS = {
     "tn_network_tree": (_I, [_P, C.c_char_p, _I]),
     "tn_network_capture": (_I, [_P, _I]),
     "tn_network_replay": (_I, [_P]),
+    "tn_network_bind_host_input": (_I, [_P, C.c_char_p, _DP, _I64]),
+    "tn_network_bind_host_output": (_I, [_P, _DP, _I64]),
     "tn_network_output": (_I, [_P, C.POINTER(_P)]),
 }
 

@@ -392,6 +392,15 @@ int tn_tensor_set_elem(tn_tensor_t t, const double* host, int64_t n) {
   });
 }
 
+int tn_tensor_set_elem_async(tn_tensor_t t, const double* host, int64_t n) {
+  return guard([&] {
+    need(t, "tensor");
+    if ((size_t)n != t->t.elemNum()) tn::fail(TN_ERR_ARG, "element count does not match the tensor");
+    need(host, "host");
+    t->t.setElemAsync(host);
+  });
+}
+
 int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n) {
   return guard([&] {
     need(t, "tensor");
@@ -598,6 +607,24 @@ int tn_network_replay(tn_network_t net) {
   return guard([&] {
     need(net, "net");
     net->net->replay();
+  });
+}
+
+int tn_network_bind_host_input(tn_network_t net, const char* name, const double* host, int64_t n) {
+  return guard([&] {
+    need(net, "net");
+    need(name, "name");
+    need(host, "host");
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative element count");
+    net->net->bindHostInput(std::string(name), host, (size_t)n);
+  });
+}
+
+int tn_network_bind_host_output(tn_network_t net, double* host, int64_t n) {
+  return guard([&] {
+    need(net, "net");
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative element count");
+    net->net->bindHostOutput(host, (size_t)n);
   });
 }
 

@@ -241,12 +241,18 @@ int* Ctx::device_error_word() {
 }
 
 void Ctx::check_device_error() {
+  if (!err_word) {
+    TN_CUDA(cudaStreamSynchronize(stream));
+    return;
+  }
+  // the status word travels with the stream's work: one synchronisation
+  if (!err_host) TN_CUDA(cudaMallocHost((void**)&err_host, sizeof(int)));
+  TN_CUDA(cudaMemcpyAsync(err_host, err_word->ptr, sizeof(int), cudaMemcpyDeviceToHost, stream));
   TN_CUDA(cudaStreamSynchronize(stream));
-  if (!err_word) return;
-  int e = 0;
-  TN_CUDA(cudaMemcpy(&e, err_word->ptr, sizeof(int), cudaMemcpyDeviceToHost));
+  const int e = *err_host;
   if (e) {
-    TN_CUDA(cudaMemset(err_word->ptr, 0, sizeof(int)));
+    TN_CUDA(cudaMemsetAsync(err_word->ptr, 0, sizeof(int), stream));
+    TN_CUDA(cudaStreamSynchronize(stream));
     fail(e, "a device-side wait gave up (bounded spin limit reached); results of the last kernels are invalid");
   }
 }
@@ -288,6 +294,8 @@ void release_ctx(Ctx* c) {
   c->svd_cache.clear();
   c->workspace.reset();
   c->err_word.reset();
+  if (c->err_host) cudaFreeHost(c->err_host);
+  c->err_host = nullptr;
   release_solver(c);
   for (auto s : c->side) cudaStreamDestroy(s);
   for (auto e : c->side_ev) cudaEventDestroy(e);

@@ -272,6 +272,7 @@ struct Ctx {
   bool prof = false;
   std::vector<ProfRec> prof_recs;
   DevBufP err_word;  // device status word written by kernels with bounded waits
+  int* err_host = nullptr;  // pinned copy of it, read after the stream synchronises
   int* device_error_word();
   void check_device_error();  // syncs the stream; throws TN_ERR_TIMEOUT if a wait gave up
   void launched(int n = 1) { launches += n; }

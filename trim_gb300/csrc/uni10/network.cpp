@@ -495,9 +495,21 @@ void Network::capture() {
   }
   c.keep = &graph_keep;  // plans and workspace the recorded kernels read
   try {
+    for (size_t i = 0; i < host_in.size(); i++) {  // bound host inputs into the put tensors
+      UniTensor* t = tensors[host_in[i].first];
+      if (host_in_n[i] != t->elemNum())
+        throw std::runtime_error("Network::capture: a bound host input does not match its tensor's element count");
+      TN_CUDA(cudaMemcpyAsync(t->getElem(), host_in[i].second, host_in_n[i] * sizeof(double), cudaMemcpyHostToDevice,
+                              cap));
+    }
     UniTensor r = launch();
     TN_CUDA(cudaMemcpyAsync(graph_out.getElem(), r.getElem(), r.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
                             cap));
+    if (host_out) {
+      if (host_out_n != r.elemNum())
+        throw std::runtime_error("Network::capture: the bound host output does not match the result's element count");
+      TN_CUDA(cudaMemcpyAsync(host_out, graph_out.getElem(), host_out_n * sizeof(double), cudaMemcpyDeviceToHost, cap));
+    }
   } catch (...) {
     c.keep = nullptr;
     graph_keep.clear();
@@ -519,6 +531,28 @@ void Network::capture() {
   graph_exec = e;
   graph_kernels = c.launches - l0;  // kernels inside the graph
   c.launches = l0;
+}
+
+void Network::bindHostInput(const std::string& name, const double* host, size_t n) {
+  auto it = name2pos.find(name);
+  if (it == name2pos.end()) throw std::runtime_error("There is no tensor named '" + name + "' in the network file");
+  if (!host) throw std::runtime_error("Network::bindHostInput: null buffer");
+  for (size_t i = 0; i < host_in.size(); i++)
+    if (host_in[i].first == it->second) {
+      host_in[i].second = host;
+      host_in_n[i] = n;
+      drop_graph();
+      return;
+    }
+  host_in.push_back({it->second, host});
+  host_in_n.push_back(n);
+  drop_graph();  // a graph records the bindings it was captured with
+}
+
+void Network::bindHostOutput(double* host, size_t n) {
+  host_out = host;
+  host_out_n = host ? n : 0;
+  drop_graph();
 }
 
 void Network::replay() {

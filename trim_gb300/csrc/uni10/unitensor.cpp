@@ -144,6 +144,12 @@ void UniTensor::setElem(const double* e, bool _ongpu) {
   status |= HAVEELEM;
 }
 
+void UniTensor::setElemAsync(const double* host) {
+  if (!elem) throw std::runtime_error("Setting elements to an empty tensor is not supported.");
+  TN_CUDA(cudaMemcpyAsync(dptr(elem), host, m_elemNum * sizeof(double), cudaMemcpyHostToDevice, C().stream));
+  status |= HAVEELEM;
+}
+
 void UniTensor::setElem(const std::vector<double>& e, bool _ongpu) {
   if (e.size() != m_elemNum) {
     std::ostringstream err;

@@ -180,6 +180,11 @@ class UniTensor:
     def set_elem_host_ptr(self, ptr: int, n: int) -> None:
         call("tn_tensor_set_elem", self.h, ptr, n)
 
+    def set_elem_host_ptr_async(self, ptr: int, n: int) -> None:
+        """setElem from host memory without waiting: the buffer (pinned, for
+        an overlapping copy) must stay unchanged until a synchronising call."""
+        call("tn_tensor_set_elem_async", self.h, ptr, n)
+
     def get_elem(self) -> np.ndarray:
         out = np.empty(self.elem_num())
         call("tn_tensor_get_elem", self.h, out.ctypes.data, out.size)
@@ -291,6 +296,16 @@ class Network:
 
     def replay(self) -> None:
         call("tn_network_replay", self.h)
+
+    def bind_host_input(self, name: str, ptr: int, n: int) -> None:
+        """Pinned host buffer copied into tensor `name` at the start of every
+        replay of the next captured graph."""
+        call("tn_network_bind_host_input", self.h, name.encode(), ptr, n)
+
+    def bind_host_output(self, ptr: int, n: int) -> None:
+        """Pinned host buffer the result is copied into at the end of every
+        replay of the next captured graph (0 unbinds)."""
+        call("tn_network_bind_host_output", self.h, ptr, n)
 
     def output(self) -> UniTensor:
         h = C.c_void_p()
