@@ -151,24 +151,16 @@ __device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, con
     const TileInfo w = decode_tile(P, t - P.tile_begin);
     if (threadIdx.x == 0) *info = w;
     if (w.mode == 2) {
-      // [z][y][x] with pitch tx + 1; lanes along y (source-contiguous), then
-      // x, then z.  Each thread steps its (y, x, z) counter by kThreads
-      // elements with carries (no division per element).
-      const int pitch = w.tx + 1;
-      const int dy = kThreads % w.ty, t1 = kThreads / w.ty, dx = t1 % w.tx, dz = t1 / w.tx;
-      int yy = threadIdx.x % w.ty, xx = (threadIdx.x / w.ty) % w.tx, zz = threadIdx.x / (w.ty * w.tx);
-#pragma unroll 4
-      for (int k = 0; k < kPerThread && zz < w.tz; k++) {
-        if (xx < w.nx && yy < w.ny && zz < w.nz)
-          cp_async8(buf + (zz * w.ty + yy) * pitch + xx,
-                    src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx + (int64_t)zz * w.sz);
-        yy += dy;
-        const int c1 = yy >= w.ty;
-        yy -= c1 * w.ty;
-        xx += dx + c1;
-        const int c2 = xx >= w.tx;
-        xx -= c2 * w.tx;
-        zz += dz + c2;
+      // [z][y][x] with pitch tx + 1.  A thread takes (y, x) pairs with lanes
+      // along y (source-contiguous) and walks the tile's z planes for each
+      // with a constant source step: one division per pair, not per element.
+      const int pitch = w.tx + 1, plane = w.ty * pitch, pairs = w.ty * w.tx;
+      for (int p = threadIdx.x; p < pairs; p += kThreads) {
+        const int xx = p / w.ty, yy = p - xx * w.ty;
+        if (xx >= w.nx || yy >= w.ny) continue;
+        const double* g = src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx;
+        double* sp = buf + yy * pitch + xx;
+        for (int zz = 0; zz < w.nz; zz++, g += w.sz, sp += plane) cp_async8(sp, g);
       }
     } else if (w.mode == 0) {
       const int q = kThreads / w.tx, r = kThreads - q * w.tx;
@@ -220,23 +212,14 @@ __device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, con
 // Store a landed tile from shared memory with lanes along x (destination-contiguous).
 __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf, double* __restrict__ dst) {
   const uint64_t flip = w.neg ? 0x8000000000000000ull : 0ull;
-  if (w.mode == 2) {  // lanes along x, then y, then z; counters stepped as in the loads
-    const int pitch = w.tx + 1;
-    const int dx = kThreads % w.tx, t1 = kThreads / w.tx, dy = t1 % w.ty, dz = t1 / w.ty;
-    int xx = threadIdx.x % w.tx, yy = (threadIdx.x / w.tx) % w.ty, zz = threadIdx.x / (w.tx * w.ty);
-#pragma unroll 4
-    for (int k = 0; k < kPerThread && zz < w.tz; k++) {
-      if (xx < w.nx && yy < w.ny && zz < w.nz) {
-        const double v = buf[(zz * w.ty + yy) * pitch + xx];
-        dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx + (int64_t)zz * w.dz] = flip_sign(v, flip);
-      }
-      xx += dx;
-      const int c1 = xx >= w.tx;
-      xx -= c1 * w.tx;
-      yy += dy + c1;
-      const int c2 = yy >= w.ty;
-      yy -= c2 * w.ty;
-      zz += dz + c2;
+  if (w.mode == 2) {  // (x, y) pairs with lanes along x; the z planes with a constant step
+    const int pitch = w.tx + 1, plane = w.ty * pitch, pairs = w.ty * w.tx;
+    for (int p = threadIdx.x; p < pairs; p += kThreads) {
+      const int yy = p / w.tx, xx = p - yy * w.tx;
+      if (xx >= w.nx || yy >= w.ny) continue;
+      const double* sp = buf + yy * pitch + xx;
+      double* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx;
+      for (int zz = 0; zz < w.nz; zz++, sp += plane, g += w.dz) *g = flip_sign(*sp, flip);
     }
     return;
   }
