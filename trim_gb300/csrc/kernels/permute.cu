@@ -162,6 +162,13 @@ __device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, con
         double* sp = buf + yy * pitch + xx;
         for (int zz = 0; zz < w.nz; zz++, g += w.sz, sp += plane) cp_async8(sp, g);
       }
+    } else if (w.mode == 0 && w.tx >= kThreads) {  // long rows: lanes stride along each row
+      for (int yy = 0; yy < w.ny; yy++) {
+        const double* g = src + w.bs + (int64_t)yy * w.sy + (int64_t)threadIdx.x * w.sx;
+        const int64_t gstep = (int64_t)kThreads * w.sx;
+        double* sp = buf + yy * w.tx + threadIdx.x;
+        for (int xx = threadIdx.x; xx < w.nx; xx += kThreads, g += gstep, sp += kThreads) cp_async8(sp, g);
+      }
     } else if (w.mode == 0) {
       const int q = kThreads / w.tx, r = kThreads - q * w.tx;
       const int y0 = threadIdx.x / w.tx, x0 = threadIdx.x - y0 * w.tx;
@@ -220,6 +227,15 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf,
       const double* sp = buf + yy * pitch + xx;
       double* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx;
       for (int zz = 0; zz < w.nz; zz++, sp += plane, g += w.dz) *g = flip_sign(*sp, flip);
+    }
+    return;
+  }
+  if (w.mode == 0 && w.tx >= kThreads) {  // long rows, as loaded
+    for (int yy = 0; yy < w.ny; yy++) {
+      const double* sp = buf + yy * w.tx + threadIdx.x;
+      double* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)threadIdx.x * w.dx;
+      const int64_t gstep = (int64_t)kThreads * w.dx;
+      for (int xx = threadIdx.x; xx < w.nx; xx += kThreads, sp += kThreads, g += gstep) *g = flip_sign(*sp, flip);
     }
     return;
   }
