@@ -107,11 +107,21 @@ static std::shared_ptr<TcPlan> build_tc_plan(Ctx& ctx, const std::vector<tn_sect
         s.kts = s.nkt;
       }
     }
-    for (int mt = 0; mt < s.nmt; mt++)
-      for (int nt = 0; nt < s.nnt; nt++) {
-        for (int q = 0; q < s.nsplit; q++) items.push_back(make_int4(idx, mt, nt, q));
-        if (s.nsplit > 1) ritems.push_back(make_int4(idx, mt, nt, 0));
-      }
+    // the tiles in flight at once (consecutive items) share the operand that
+    // has fewer tiles and stream the other: the inner loop runs over the
+    // shorter tile count, so each image of the longer operand is brought in
+    // once and reused by the neighbouring items from L2
+    auto add = [&](int mt, int nt) {
+      for (int q = 0; q < s.nsplit; q++) items.push_back(make_int4(idx, mt, nt, q));
+      if (s.nsplit > 1) ritems.push_back(make_int4(idx, mt, nt, 0));
+    };
+    if (s.nnt <= s.nmt) {
+      for (int mt = 0; mt < s.nmt; mt++)
+        for (int nt = 0; nt < s.nnt; nt++) add(mt, nt);
+    } else {
+      for (int nt = 0; nt < s.nnt; nt++)
+        for (int mt = 0; mt < s.nmt; mt++) add(mt, nt);
+    }
   }
   P->nsec = (int)secs.size();
   P->nitems = (int)items.size();
