@@ -337,19 +337,21 @@ GemmRoute sector_route(const Ctx& ctx, int mode, const std::vector<tn_sector_gem
   if (!route_tunable(mode, st)) return st;
   auto it = ctx.route_tuned.find(route_key(mode, list));
   if (it == ctx.route_tuned.end()) return st;
-  return it->second ? GemmRoute::Fused : GemmRoute::Fp64;
+  return (GemmRoute)it->second;
 }
 
-// Times the fused form and the FP64 kernel (both write the same output) and
-// keeps the faster for this histogram; the chosen form runs last, so the
-// output holds its result.  Not measured while a graph is being captured.
-template <class Fused, class Fp64>
-static GemmRoute tune_route(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, Fused&& fused, Fp64&& fp64) {
+// Times the candidate forms (each writes the same output) and keeps the
+// fastest for this histogram; the chosen form runs last, so the output holds
+// its result.  Not measured while a graph is being captured.  The tiled form
+// is a candidate only where the operands are not read through views.
+template <class Fused, class Fp64, class Tiled>
+static GemmRoute tune_route(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list, Fused&& fused, Fp64&& fp64,
+                            Tiled* tiled) {
   const GemmRoute st = static_route(ctx, mode, list);
   if (!route_tunable(mode, st)) return st;
   const uint64_t key = route_key(mode, list);
   auto it = ctx.route_tuned.find(key);
-  if (it != ctx.route_tuned.end()) return it->second ? GemmRoute::Fused : GemmRoute::Fp64;
+  if (it != ctx.route_tuned.end()) return (GemmRoute)it->second;
   if (capturing(ctx)) return st;
   cudaEvent_t e0, e1;
   TN_CUDA(cudaEventCreate(&e0));
@@ -364,13 +366,21 @@ static GemmRoute tune_route(Ctx& ctx, int mode, const std::vector<tn_sector_gemm
     TN_CUDA(cudaEventElapsedTime(&ms, e0, e1));
     return ms;
   };
-  const float t_fused = time_of(fused), t_fp64 = time_of(fp64);
+  GemmRoute best = GemmRoute::Fused;
+  float best_ms = time_of(fused);
+  const float t_fp64 = time_of(fp64);
+  if (t_fp64 < best_ms) {
+    best = GemmRoute::Fp64;
+    best_ms = t_fp64;
+  }
+  if (tiled && time_of(*tiled) < best_ms) best = GemmRoute::Tiled;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  const bool use_fused = t_fused < t_fp64;
-  ctx.route_tuned[key] = use_fused ? 1 : 0;
-  if (use_fused) fused();  // the output holds the chosen form's result
-  return use_fused ? GemmRoute::Fused : GemmRoute::Fp64;
+  ctx.route_tuned[key] = (int)best;
+  // the output holds the result of the last form timed: rerun the choice
+  if (best == GemmRoute::Fused) fused();
+  else if (best == GemmRoute::Fp64 && tiled) fp64();
+  return best;
 }
 
 bool sectors_take_views(const Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& list) {
@@ -461,7 +471,7 @@ void run_sector_gemms_views(Ctx& ctx, int mode, const std::vector<tn_sector_gemm
     if (P->ntiles) launch_fp64_plan(ctx, *P, A, B, C, views, pool);
   };
   const bool tuned = ctx.route_tuned.count(route_key(mode, list)) > 0;
-  const GemmRoute route = tune_route(ctx, mode, list, fused, fp64);
+  const GemmRoute route = tune_route(ctx, mode, list, fused, fp64, (decltype(fp64)*)nullptr);
   if (!tuned && ctx.route_tuned.count(route_key(mode, list))) return;  // measured just now: C holds the result
   if (route == GemmRoute::Fused)
     fused();
@@ -475,20 +485,21 @@ void run_sector_gemms(Ctx& ctx, int mode, const std::vector<tn_sector_gemm>& lis
   const bool tc_only = (mode & TN_MODE_TC_ONLY) != 0;
   const int ns = (mode & ~kModeFlags) == TN_MODE_SPLIT ? 7 : 1;
   const bool tuned = ctx.route_tuned.count(route_key(mode, list)) > 0;
-  const GemmRoute route = tune_route(
-      ctx, mode, list, [&] { run_tc_fused(ctx, ns, list, A, B, C); }, [&] { run_fp64(ctx, list, A, B, C); });
-  if (!tuned && ctx.route_tuned.count(route_key(mode, list))) return;  // measured just now: C holds the result
-  if (route == GemmRoute::Fp64) {
-    run_fp64(ctx, list, A, B, C);
-  } else if (route == GemmRoute::Fused) {
-    run_tc_fused(ctx, ns, list, A, B, C);
-  } else {
-    // tiled: thin sectors on the FP64 kernel (unless TN_MODE_TC_ONLY)
+  auto tiled = [&] {
     std::vector<tn_sector_gemm> tc, f64;
     for (const auto& g : list) (!tc_only && thin_sector(g) ? f64 : tc).push_back(g);
     if (!f64.empty()) run_fp64(ctx, f64, A, B, C);
     if (!tc.empty()) run_tc_gemms(ctx, ns, tc, A, B, C);
-  }
+  };
+  const GemmRoute route = tune_route(
+      ctx, mode, list, [&] { run_tc_fused(ctx, ns, list, A, B, C); }, [&] { run_fp64(ctx, list, A, B, C); }, &tiled);
+  if (!tuned && ctx.route_tuned.count(route_key(mode, list))) return;  // measured just now: C holds the result
+  if (route == GemmRoute::Fp64)
+    run_fp64(ctx, list, A, B, C);
+  else if (route == GemmRoute::Fused)
+    run_tc_fused(ctx, ns, list, A, B, C);
+  else
+    tiled();  // thin sectors on the FP64 kernel (unless TN_MODE_TC_ONLY)
 }
 
 }  // namespace tn
