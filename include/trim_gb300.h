@@ -58,9 +58,10 @@ enum {
    * (by default a sector with K < 16 or N < 16 runs on the exact FP64
    * kernel instead) */
   TN_MODE_TC_ONLY = 0x100,
-  /* flags choosing the tensor-core form (by default: fused while every
-   * sector has K <= 576 and the contraction has at most 4 output tiles of
-   * 128 x 64 per SM, tiled above that).
+  /* flags choosing the tensor-core form (by default: where every sector
+   * has K <= 576 and the contraction has at most 4 output tiles of 128 x 64
+   * per SM, the fastest of the fused form, the tiled form and the FP64
+   * kernel, timed once per sector-size histogram; the tiled form above that).
    * Fused: one launch, each CTA slices the operands of its own tile.
    * Tiled: operand maxima and slices once per contraction, then the
    * pipelined GEMM over pre-sliced tiles (3 launches). */
