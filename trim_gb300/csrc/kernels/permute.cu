@@ -139,17 +139,24 @@ __device__ __forceinline__ void cp_async_wait() {
 
 constexpr int kStages = 3;  // tiles in flight per CTA: 2 loading while 1 is stored
 
-// Issue the asynchronous loads of tile t into one stage buffer.  Mode 0 keeps
-// the tile as [y][x] (pitch tx), mode 1 as [y][x] with pitch tx + 1; loads
-// run with lanes along x (mode 0) or along y, the source-contiguous dim
-// (mode 1).  Thread 0 records the tile's decode for the store phase.
-__device__ __forceinline__ void issue_tile(const PermSub* __restrict__ subs, const int64_t* __restrict__ tile_start,
-                                           int nsub, int64_t ntiles, int64_t t, const double* __restrict__ src,
-                                           double* buf, TileInfo* info) {
+// Decode of tile t, or an empty tile (mode -1) past the end of the list.
+__device__ __forceinline__ TileInfo decode_at(const PermSub* __restrict__ subs, const int64_t* __restrict__ tile_start,
+                                              int nsub, int64_t ntiles, int64_t t) {
   if (t < ntiles) {
     const PermSub& P = subs[find_sub(tile_start, nsub, t)];
-    const TileInfo w = decode_tile(P, t - P.tile_begin);
-    if (threadIdx.x == 0) *info = w;
+    return decode_tile(P, t - P.tile_begin);
+  }
+  TileInfo w{};
+  w.mode = -1;
+  return w;
+}
+
+// Issue the asynchronous loads of a decoded tile into one stage buffer.
+// Mode 0 keeps the tile as [y][x] (pitch tx), mode 1 as [y][x] with pitch
+// tx + 1; loads run with lanes along x (mode 0) or along y, the
+// source-contiguous dim (mode 1).
+__device__ __forceinline__ void issue_tile(const TileInfo& w, const double* __restrict__ src, double* buf) {
+  if (w.mode >= 0) {
     if (w.mode == 2) {
       // [z][y][x] with pitch tx + 1.  A thread takes (y, x) pairs with lanes
       // along y (source-contiguous) and walks the tile's z planes for each
@@ -269,27 +276,55 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf,
   }
 }
 
-// Persistent pipeline over the tiles t = blockIdx.x + i * gridDim.x: the
-// loads of tiles i+1 and i+2 are in flight while tile i is written out.
+// Persistent pipeline over the tiles t = blockIdx.x + k * gridDim.x: the
+// loads of tiles k+1 and k+2 are in flight while tile k is written out.
+// The tile decodes live in a shared ring of kRing slots (slot k % kRing),
+// filled by warp 0 in batches of 32 tiles, one per lane: the divisions of a
+// decode run once per tile, in parallel across the lanes, not once per
+// thread.  Batch 0 is decoded before the loop; in iteration i with i % 32 ==
+// 0 warp 0 decodes tiles i+32 .. i+63 into the slots of tiles i-32 .. i-1,
+// which were stored in earlier iterations.  The issue of iteration i reads
+// slot (i+2) % kRing and the store slot i % kRing, neither in that batch;
+// the batch is first read 30 iterations later, after the barriers between.
+constexpr int kRing = 64;
+
+__device__ __forceinline__ void decode_batch(TileInfo* ring, const PermSub* __restrict__ subs,
+                                             const int64_t* __restrict__ tile_start, int nsub, int64_t ntiles,
+                                             int64_t k0) {
+  const int lane = threadIdx.x & 31;
+  const int64_t k = k0 + lane;
+  ring[k % kRing] = decode_at(subs, tile_start, nsub, ntiles, blockIdx.x + k * (int64_t)gridDim.x);
+}
+
 __global__ void __launch_bounds__(kThreads, 2) permute_kernel(const PermSub* __restrict__ subs,
                                                               const int64_t* __restrict__ tile_start, int nsub,
                                                               int64_t ntiles, const double* __restrict__ src,
                                                               double* __restrict__ dst) {
   extern __shared__ double smem[];  // kStages * kSmem doubles
-  __shared__ TileInfo info[kStages];
+  __shared__ TileInfo ring[kRing];
   const int64_t G = gridDim.x;
-  int64_t t_issue = blockIdx.x;
+  if (threadIdx.x < 32) decode_batch(ring, subs, tile_start, nsub, ntiles, 0);
+  __syncthreads();
 #pragma unroll
-  for (int s = 0; s < kStages - 1; s++, t_issue += G)
-    issue_tile(subs, tile_start, nsub, ntiles, t_issue, src, smem + s * kSmem, &info[s]);
+  for (int s = 0; s < kStages - 1; s++) {
+    const TileInfo w = ring[s];
+    issue_tile(w, src, smem + s * kSmem);
+  }
   int stage = 0;
-  for (int64_t t = blockIdx.x; t < ntiles; t += G) {
+  int64_t i = 0;
+  for (int64_t t = blockIdx.x; t < ntiles; t += G, i++) {
     const int ns = (stage + kStages - 1) % kStages;  // stored in the previous iteration
-    issue_tile(subs, tile_start, nsub, ntiles, t_issue, src, smem + ns * kSmem, &info[ns]);
-    t_issue += G;
+    {
+      const TileInfo w = ring[(i + kStages - 1) % kRing];
+      issue_tile(w, src, smem + ns * kSmem);
+    }
+    if (threadIdx.x < 32 && (i & 31) == 0) decode_batch(ring, subs, tile_start, nsub, ntiles, i + 32);
     cp_async_wait<kStages - 1>();  // this thread's loads of tile t have landed
     __syncthreads();               // ... and every other thread's
-    store_tile(info[stage], smem + stage * kSmem, dst);
+    {
+      const TileInfo w = ring[i % kRing];
+      store_tile(w, smem + stage * kSmem, dst);
+    }
     __syncthreads();  // the stage is reloaded in the next iteration
     stage = (stage + 1) % kStages;
   }
