@@ -280,6 +280,7 @@ def gpu_main(args, rank, local, world):
             res[m]["ms_graph"], res[m]["e2e_ms"] = float(t[0]), float(t[1])
 
     svd = itebd_svd_section(args, torch, tu, stream, flush, spec, els, ref64, rank, world)
+    eigh = itebd_eigh_section(args, torch, tu, stream, flush, spec, els, ref64, rank, world)
 
     head = modes[-1]
     R = res[head]
@@ -354,11 +355,69 @@ def gpu_main(args, rank, local, world):
             "clocks": R["clocks"],
             "gpu_launches": R["launches"],
             "svd_truncate": svd,
+            "eigh": eigh,
             "itebd_step_ms": {"contract_graph": R["ms_graph"], "svd_truncate": svd["ms_gpu"],
                               "total": R["ms_graph"] + svd["ms_gpu"],
                               "cpu_port_total": (svd["ms_cpu_port"] + (flops / cpu["value"] / 1e9 if cpu else 0.0))
                               if svd["ms_cpu_port"] is not None and cpu else None},
         }))
+
+
+def itebd_eigh_section(args, torch, tu, stream, flush, spec, els, theta64, rank, world):
+    """Block::eigh of every (square) sector of the iTEBD theta, lower triangle
+    read as dsyev 'U' reads the reference's row-major buffer: one batched call
+    (scaled shift, cluster-Jacobi SVD, Rayleigh quotients).  Wall time per
+    call, kernel device times, and the eigenvalue error against LAPACK dsyev
+    per sector (the oracle), which is also the timed CPU port."""
+    from oracle import symtensor as st
+
+    names, dev, net = _itebd_device(tu, spec, els)
+    th = net.launch("fp64")
+    blocks = [b for b in th.sector_map().blocks() if b[1] == b[2]]
+    secs, eo = [], 0
+    for _, r, _, off in blocks:
+        secs.append((r, off, eo, off))
+        eo += r
+    E = torch.empty(max(eo, 1), dtype=torch.float64, device="cuda")
+    V = torch.empty(max(th.elem_num(), 1), dtype=torch.float64, device="cuda")
+    run = lambda: tu.eigh_sectors(secs, th.device_ptr(), E.data_ptr(), V.data_ptr())
+    for _ in range(args.warmup):
+        run()
+    torch.cuda.synchronize()
+    wall = []
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(k))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        run()
+        tu.sync()
+        wall.append((time.perf_counter() - t0) * 1e3)
+    tu.prof_enable(True)
+    run()
+    prof = tu.prof_read()
+    tu.prof_enable(False)
+    e = E.cpu().numpy()
+    out = {"sectors": len(secs), "ms_gpu": statistics.median(wall), "kernels_ms": {k_: v["ms"] for k_, v in prof.items()}}
+    cpu_ms = None
+    if rank == 0 and world == 1:
+        mats = [theta64[off:off + r * r].reshape(r, r) for _, r, _, off in blocks]
+        t0 = time.perf_counter()
+        ref = [st.block_eigh(m)[0] for m in mats]
+        dt1 = time.perf_counter() - t0
+        err = max(float(np.max(np.abs(e[o:o + r] - er)) / max(np.max(np.abs(er)), 1e-300))
+                  for (r, _, o, _), er in zip(secs, ref))
+        n = 0 if args.no_cpu else max(1, min(50, int(0.2 * args.cpu_seconds / max(dt1, 1e-3))))
+        if n:
+            t0 = time.perf_counter()
+            for _ in range(n):
+                for m in mats:
+                    st.block_eigh(m)
+            cpu_ms = (time.perf_counter() - t0) / n * 1e3
+        out.update({"eig_max_err_rel": err,
+                    "cpu_port_sample": f"{n} x {len(mats)} Block::eigh (LAPACK dsyev, numpy) on {os.cpu_count()} threads"})
+    out["ms_cpu_port"] = cpu_ms
+    return out
 
 
 def itebd_svd_section(args, torch, tu, stream, flush, spec, els, theta64, rank, world):

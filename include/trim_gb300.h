@@ -192,6 +192,27 @@ typedef struct {
 int tn_svd_sectors(tn_ctx_t ctx, int n, const tn_svd_sector* list, const double* A, double* U, double* S,
                    double* VT, int* sweeps);
 
+/* One sector of a batched symmetric eigendecomposition: A[N x N] (row-major)
+ * at a_off; E[N] at e_off receives the eigenvalues in ascending order and
+ * V[N x N] at v_off the eigenvectors as rows (row j belongs to E[j]).  Only
+ * the lower triangle of A (row >= column) is read.  Replaces Block::eigh
+ * (data-structure/lib/BlockReal.cpp:359-391), i.e. LAPACK dsyev 'V','U' on
+ * the row-major buffer (numeric/lapack/lib/uni10_lapack_cpu.cpp:131-152),
+ * whose column-major eigenvectors read row-major are these rows. */
+typedef struct {
+  int64_t N;
+  int64_t a_off, e_off, v_off;
+} tn_eigh_sector;
+
+/* All n sector eigendecompositions in FP64 on the GPU, in one batch: each
+ * sector is scaled by an exact power of two and shifted to a positive
+ * definite matrix whose SVD (the batched Jacobi SVD above) gives the
+ * eigenpairs.  Eigenvalue errors are a few units of roundoff of ||A||_inf;
+ * eigenvector signs are arbitrary, as dsyev's are.  sweeps as for
+ * tn_svd_sectors. */
+int tn_eigh_sectors(tn_ctx_t ctx, int n, const tn_eigh_sector* list, const double* A, double* E, double* V,
+                    int* sweeps);
+
 /* Cluster shape the SVD of an M x N sector would use (no GPU needed):
  * cluster size P (0: the sector goes to the cuSOLVER fallback), columns per
  * block b, record length L and shared memory per CTA. */

@@ -30,6 +30,9 @@ class Block {
   double norm() const;
   // Block::svd (data-structure/lib/BlockReal.cpp:226-250): {U, S (diag), VT}
   std::vector<Matrix> svd() const;
+  // Block::eigh (data-structure/lib/BlockReal.cpp:359-391): {Eig (diagonal,
+  // ascending), EigVec (row j = eigenvector j)}
+  std::vector<Matrix> eigh() const;
 
  protected:
   friend class UniTensor;

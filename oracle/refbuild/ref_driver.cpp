@@ -18,6 +18,7 @@
 //   copy OUT SRC                   deep copy
 //   save NAME PATH                 UniTensor::save (current binary layout)
 //   svd NAME U1 PRT PRTF PREFIX    Block::svd of one block -> PREFIX.{U,S,VT}
+//   eigh NAME U1 PRT PRTF PREFIX   Block::eigh of one block -> PREFIX.{E,V}
 //   blocks NAME PATH               writes "U1 PRT PRTF ROWS COLS" per block
 //   time ITERS <command...>        runs the command ITERS times (on copies
 //                                  for in-place ones) and prints seconds/iter
@@ -124,6 +125,17 @@ static void run(const std::vector<std::string>& w) {
     std::vector<Matrix> r = get(w[1]).getBlock(q).svd();
     const char* suf[3] = {".U", ".S", ".VT"};
     for (int k = 0; k < 3; k++) {
+      FILE* fp = std::fopen((w[5] + suf[k]).c_str(), "wb");
+      size_t rc[2] = {r[k].row(), r[k].col()};
+      std::fwrite(rc, sizeof(size_t), 2, fp);
+      std::fwrite(r[k].getElem(), sizeof(double), r[k].elemNum(), fp);
+      std::fclose(fp);
+    }
+  } else if (op == "eigh") {
+    Qnum q(parityFType(std::atoi(w[4].c_str())), std::atoi(w[2].c_str()), parityType(std::atoi(w[3].c_str())));
+    std::vector<Matrix> r = get(w[1]).getBlock(q).eigh();
+    const char* suf[2] = {".E", ".V"};
+    for (int k = 0; k < 2; k++) {
       FILE* fp = std::fopen((w[5] + suf[k]).c_str(), "wb");
       size_t rc[2] = {r[k].row(), r[k].col()};
       std::fwrite(rc, sizeof(size_t), 2, fp);

@@ -68,6 +68,11 @@ class RefSession:
         self.files[key] = prefix
         self.lines.append(f"svd {name} {q[0]} {q[1]} {q[2]} {prefix}")
 
+    def eigh(self, name: str, q, key: str) -> None:
+        prefix = os.path.join(self.tmp.name, f"eigh_{key}")
+        self.files[key] = prefix
+        self.lines.append(f"eigh {name} {q[0]} {q[1]} {q[2]} {prefix}")
+
     def run(self, env=None) -> dict:
         script = os.path.join(self.tmp.name, "script.txt")
         with open(script, "w") as f:
@@ -81,7 +86,8 @@ class RefSession:
         out = {k: uni10_io.read_tensor(v) for k, v in self.saves.items()}
         for k, prefix in self.files.items():
             mats = []
-            for suf in (".U", ".S", ".VT"):
+            sufs = (".E", ".V") if os.path.exists(prefix + ".E") else (".U", ".S", ".VT")
+            for suf in sufs:
                 raw = np.fromfile(prefix + suf, dtype="<u8", count=2)
                 m = np.fromfile(prefix + suf, dtype="<f8", offset=16)
                 # a diagonal Matrix (the singular values) stores min(r, c) values

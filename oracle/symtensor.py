@@ -18,6 +18,8 @@ It restates, in numpy, the algorithms of the reference (Uni10 v1.0.0) for:
   * Network fromfile/construct/launch/merge and the greedy planner
                                     (tensor-network/lib/Network.cpp:63-135, 271-506, 602-739)
   * Block::svd via LAPACK dgesvd     (numeric/lapack/lib/uni10_lapack_cpu.cpp:289-313)
+  * Block::eigh via LAPACK dsyev     (data-structure/lib/BlockReal.cpp:359-391,
+                                     uni10_lapack_cpu.cpp:131-152)
   * the iTEBD truncation + normalisation over U(1) sectors
                                     (examples/iTEBD.cpp:153-171, Matrix::resize
                                      tensor-network/lib/MatrixReal.cpp:289-360)
@@ -792,6 +794,27 @@ def block_svd(mat: np.ndarray):
 
     u, s, vt = scipy.linalg.svd(mat, full_matrices=False, lapack_driver="gesvd")
     return u, s, vt
+
+
+def block_eigh(mat: np.ndarray):
+    """Block::eigh -> (E, V) via LAPACK dsyev ('V', 'U'); BlockReal.cpp:359-391,
+    uni10_lapack_cpu.cpp:131-152.
+
+    The reference hands the row-major N x N buffer to the column-major dsyev,
+    which reads its upper triangle: the LOWER triangle of the row-major matrix
+    (row >= column).  E holds the eigenvalues in ascending order; dsyev leaves
+    eigenvector j in column j of its column-major output, so in the row-major
+    Matrix the reference returns, row j of V is eigenvector j."""
+    import scipy.linalg
+
+    a = np.asarray(mat, dtype=np.float64)
+    n = a.shape[0]
+    if a.ndim != 2 or a.shape[1] != n:
+        raise ValueError("Cannot perform eigenvalue decomposition on a non-square matrix.")
+    low = np.tril(a)
+    sym = low + np.tril(a, -1).T
+    e, v = scipy.linalg.eigh(sym, driver="ev")
+    return e, np.ascontiguousarray(v.T)
 
 
 # --------------------------------------------------------------------------- truncation

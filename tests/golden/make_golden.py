@@ -7,7 +7,8 @@ Run here (where the reference sources exist and oracle/_ref is built):
 
 It writes:
   cases.json / arrays.npz  reference outputs (UniTensor::permute, transpose,
-                           contract, combineBond, Network::launch, Block::svd)
+                           contract, combineBond, Network::launch, Block::svd,
+                           Block::eigh)
                            for seeded inputs: workload 1 at full size, the
                            iTEBD network at full size (chi=512), reduced-size
                            versions of workloads 3-5, and randomized
@@ -360,6 +361,31 @@ def greedy_network(w: Writer, rng):
            "tensors": {n: tensor_meta(specs[n], labels[n]) for n in specs}, "R": out_meta(o["R"])}, arrays)
 
 
+def eigh_cases(w: Writer, rng):
+    """Block::eigh (dsyev) of every block of square-block U(1) tensors, one
+    IN and one OUT bond with equal charges and degeneracies; the inputs are
+    not symmetric, so the fixture also pins which triangle dsyev reads."""
+    specs = [[(-2, 1), (-1, 4), (0, 9), (1, 30), (2, 2)], [(0, 64)], [(-1, 3), (1, 3)]]
+    for i, runs in enumerate(specs):
+        bonds = [(1, [(u, 0, 0, d) for u, d in runs]), (-1, [(u, 0, 0, d) for u, d in runs])]
+        n = sum(d * d for _, d in runs)
+        elem = rng.standard_normal(n)
+        if i == 2:  # symmetric blocks with a repeated eigenvalue
+            elem = np.concatenate([np.eye(3).ravel() * 2.0, np.diag([1.0, 1.0, -1.0]).ravel()])
+        S = refrun.RefSession()
+        S.tensor("T", bonds, [1, 2], elem)
+        for j, (u, _) in enumerate(runs):
+            S.eigh("T", (u, 0, 0), f"e{j}")
+        o = S.run()
+        arrays = {"elem": elem}
+        for j in range(len(runs)):
+            e, v = o[f"e{j}"]
+            arrays[f"E{j}"] = np.atleast_1d(np.asarray(e)).ravel()
+            arrays[f"V{j}"] = np.atleast_2d(v)
+        w.add({"id": f"eigh{i}", "kind": "eigh", "bonds": [[t, [list(r) for r in rr]] for t, rr in bonds],
+               "blocks": [[u, d] for u, d in runs]}, arrays)
+
+
 def legacy(refroot: str):
     ex = os.path.join(refroot, "Swig", "examples")
     out = {}
@@ -392,6 +418,7 @@ def main():
     contract_cases(w, rng, 30)
     # fermionic signs of permute / contract, with a stream of their own
     fermion_cases(w, np.random.default_rng(777), 16, 8)
+    eigh_cases(w, np.random.default_rng(4242))
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(w.cases, f, indent=0)
     np.savez_compressed(os.path.join(HERE, "arrays.npz"), **w.arrays)

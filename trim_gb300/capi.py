@@ -44,6 +44,10 @@ class SvdSector(C.Structure):
                 ("s_off", C.c_int64), ("vt_off", C.c_int64)]
 
 
+class EighSector(C.Structure):
+    _fields_ = [("N", C.c_int64), ("a_off", C.c_int64), ("e_off", C.c_int64), ("v_off", C.c_int64)]
+
+
 _P = C.c_void_p
 _I = C.c_int
 _I64 = C.c_int64
@@ -73,6 +77,7 @@ _PROTOS = {
     "tn_contract_sectors_fp64_noalloc": (_I, [_P, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
     "tn_svd_sectors": (_I, [_P, _I, C.POINTER(SvdSector), _DP, _DP, _DP, _DP, _IP]),
     "tn_svd_plan": (_I, [_I64, _I64, _I, _IP, _IP, _IP, _I64P]),
+    "tn_eigh_sectors": (_I, [_P, _I, C.POINTER(EighSector), _DP, _DP, _DP, _IP]),
     "tn_truncate_sectors": (_I, [_P, _I, _I64P, _I64P, _DP, _I64, _I64P, C.POINTER(C.c_double)]),
     "tn_tensor_svd_truncate": (_I, [_P, _I64, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(C.c_double)]),
     "tn_tensor_create": (_I, [_P, _I, _IP, _IP, _IP, _IP, C.POINTER(_P)]),

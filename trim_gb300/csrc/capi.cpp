@@ -333,6 +333,25 @@ int tn_svd_sectors(tn_ctx_t ctx, int n, const tn_svd_sector* list, const double*
   });
 }
 
+int tn_eigh_sectors(tn_ctx_t ctx, int n, const tn_eigh_sector* list, const double* A, double* E, double* V,
+                    int* sweeps) {
+  return guard([&] {
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative sector count");
+    if (n == 0) return;
+    need(list, "list");
+    tn::Ctx& c = *tn::as_ctx(ctx);
+    std::vector<tn_eigh_sector> l(list, list + n);
+    if (!sweeps) {
+      tn::run_eigh_sectors(c, l, A, E, V, nullptr);
+      return;
+    }
+    tn::DevBuf info((size_t)n * sizeof(int), c);
+    tn::run_eigh_sectors(c, l, A, E, V, (int*)info.ptr);
+    TN_CUDA(cudaMemcpyAsync(sweeps, info.ptr, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c.stream));
+    TN_CUDA(cudaStreamSynchronize(c.stream));
+  });
+}
+
 int tn_svd_plan(int64_t M, int64_t N, int max_cluster, int* P, int* b, int* L, int64_t* smem_bytes) {
   return guard([&] {
     if (max_cluster < 1 || max_cluster > 16 || (max_cluster & (max_cluster - 1)))

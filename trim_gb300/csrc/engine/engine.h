@@ -403,6 +403,21 @@ void launch_transpose(const double* src, double* dst, int rows, int cols, cudaSt
 // sector solved by the cuSOLVER fallback)
 void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const double* A, double* U, double* S,
                      double* VT, int* info);
+// symmetric eigendecomposition of n x n sectors through the SVD of a scaled,
+// shifted positive definite copy (eigh_shift.cu): offsets of A; of the
+// shifted copy M and the scaled copy S (both in the M buffer); of E and V;
+// of the SVD's VT; of W = V S
+struct EighJob {
+  int64_t n, a_off, m_off, sc_off, e_off, v_off, vt_off, w_off;
+};
+void launch_eigh_prep(const EighJob* jobs, int njobs, const double* A, double* M, int* scale_exp, cudaStream_t s);
+void launch_eigh_rows(const EighJob* jobs, int njobs, const double* VT, double* V, cudaStream_t s);
+void launch_eigh_values(const EighJob* jobs, int njobs, const double* W, const double* V, const int* scale_exp,
+                        double* E, cudaStream_t s);
+// all sectors of `list` in one batch: E ascending, row j of V eigenvector j;
+// info as for run_svd_sectors
+void run_eigh_sectors(Ctx& ctx, const std::vector<tn_eigh_sector>& list, const double* A, double* E, double* V,
+                      int* info);
 // global truncation to chi over sectors with sorted singular values; fills
 // kept (host, one count per sector) and returns the norm of the kept values
 double run_truncate(Ctx& ctx, const std::vector<int64_t>& s_off, const std::vector<int64_t>& s_cnt, double* S,

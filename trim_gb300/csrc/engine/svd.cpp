@@ -323,6 +323,65 @@ void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const dou
     if (info) TN_CUDA(cudaMemsetAsync(info + i, 0, sizeof(int), ctx.stream));
 }
 
+void run_eigh_sectors(Ctx& ctx, const std::vector<tn_eigh_sector>& list, const double* A, double* E, double* V,
+                      int* info) {
+  std::vector<EighJob> jobs;
+  std::vector<tn_svd_sector> svd;
+  std::vector<tn_sector_gemm> rq;  // W = V S for the Rayleigh quotients
+  std::vector<int> idx;            // list index of every job
+  int64_t m = 0, sv = 0;
+  for (size_t i = 0; i < list.size(); i++) {
+    const tn_eigh_sector& q = list[i];
+    if (q.N < 0 || q.a_off < 0 || q.e_off < 0 || q.v_off < 0) fail(TN_ERR_ARG, "eigh: negative size or offset");
+    if (q.N == 0) continue;
+    idx.push_back((int)i);
+    m += q.N * q.N;
+    sv += q.N;
+  }
+  if (info) TN_CUDA(cudaMemsetAsync(info, 0, list.size() * sizeof(int), ctx.stream));
+  if (idx.empty()) return;
+  // one workspace: M | S | U (then W) | VT | singular values
+  DevBuf wsb((size_t)(4 * m + sv) * sizeof(double), ctx);
+  double* ws = (double*)wsb.ptr;
+  int64_t o = 0, so = 4 * m;
+  for (int i : idx) {
+    const tn_eigh_sector& q = list[i];
+    const int64_t n2 = q.N * q.N;
+    // M at o, S at m + o, U / W at 2m + o, VT at 3m + o
+    jobs.push_back(EighJob{q.N, q.a_off, o, m + o, q.e_off, q.v_off, 3 * m + o, 2 * m + o});
+    svd.push_back(tn_svd_sector{q.N, q.N, o, 2 * m + o, so, 3 * m + o});
+    rq.push_back(tn_sector_gemm{q.N, q.N, q.N, q.v_off, m + o, 2 * m + o});
+    o += n2;
+    so += q.N;
+  }
+  const int nj = (int)jobs.size();
+  DevBuf jb((size_t)nj * (sizeof(EighJob) + 2 * sizeof(int)), ctx);
+  EighJob* dj = (EighJob*)jb.ptr;
+  int* scale = (int*)(dj + nj);
+  int* sw = scale + nj;
+  TN_CUDA(cudaMemcpyAsync(dj, jobs.data(), (size_t)nj * sizeof(EighJob), cudaMemcpyHostToDevice, ctx.stream));
+  {
+    ProfScope ps(ctx, "eigh_shift");
+    launch_eigh_prep(dj, nj, A, ws, scale, ctx.stream);
+    ctx.launched();
+  }
+  run_svd_sectors(ctx, svd, ws, ws, ws, ws, info ? sw : nullptr);
+  {
+    ProfScope ps(ctx, "eigh_shift");
+    launch_eigh_rows(dj, nj, ws, V, ctx.stream);
+    ctx.launched();
+  }
+  run_sector_gemms(ctx, TN_MODE_FP64, rq, V, ws, ws);
+  {
+    ProfScope ps(ctx, "eigh_shift");
+    launch_eigh_values(dj, nj, ws, V, scale, E, ctx.stream);
+    ctx.launched();
+  }
+  if (info)
+    for (int k = 0; k < nj; k++)
+      TN_CUDA(cudaMemcpyAsync(info + idx[k], sw + k, sizeof(int), cudaMemcpyDeviceToDevice, ctx.stream));
+}
+
 double run_truncate(Ctx& ctx, const std::vector<int64_t>& s_off, const std::vector<int64_t>& s_cnt, double* S,
                     int64_t chi, std::vector<int64_t>& kept) {
   const int n = (int)s_off.size();

@@ -162,4 +162,23 @@ std::vector<Matrix> Block::svd() const {
   return out;
 }
 
+// Block::eigh (data-structure/lib/BlockReal.cpp:359-391): {Eig (diagonal,
+// ascending), EigVec (row j = eigenvector j)}; the lower triangle is read,
+// as the reference's dsyev 'U' on the row-major buffer does.
+std::vector<Matrix> Block::eigh() const {
+  if (Rnum != Cnum) throw std::runtime_error("Cannot perform eigenvalue decomposition on a non-square matrix.");
+  if (diag)
+    throw std::runtime_error("Cannot perform eigenvalue decomposition on a diagonal matrix. Need not to do so.");
+  Matrix E(Rnum, Cnum, true), V(Rnum, Cnum);
+  if (Rnum) {
+    std::vector<tn_eigh_sector> list(1);
+    list[0] = tn_eigh_sector{(int64_t)Rnum, 0, 0, 0};
+    tn::run_eigh_sectors(C(), list, m_elem, E.getElem(), V.getElem(), nullptr);
+  }
+  std::vector<Matrix> out;
+  out.push_back(E);
+  out.push_back(V);
+  return out;
+}
+
 }  // namespace uni10

@@ -82,6 +82,18 @@ def svd_sectors(sectors, a_ptr: int, u_ptr: int, s_ptr: int, vt_ptr: int, sweeps
     return list(sw)[:n] if sweeps else None
 
 
+def eigh_sectors(sectors, a_ptr: int, e_ptr: int, v_ptr: int, sweeps: bool = False):
+    """Batched per-sector symmetric eigendecomposition (Block::eigh); sectors
+    are (N, a_off, e_off, v_off) tuples, the pointers device addresses.
+    Eigenvalues ascending, eigenvectors as rows.  With sweeps=True returns
+    the Jacobi sweep count of every sector (synchronous)."""
+    n = len(sectors)
+    arr = (capi.EighSector * max(1, n))(*[capi.EighSector(*t) for t in sectors])
+    sw = (C.c_int * max(1, n))() if sweeps else None
+    call("tn_eigh_sectors", None, n, arr, a_ptr, e_ptr, v_ptr, sw)
+    return list(sw)[:n] if sweeps else None
+
+
 def svd_plan(M: int, N: int, max_cluster: int = 16) -> dict:
     P, b, L, sm = C.c_int(), C.c_int(), C.c_int(), C.c_int64()
     call("tn_svd_plan", int(M), int(N), int(max_cluster), C.byref(P), C.byref(b), C.byref(L), C.byref(sm))
