@@ -7,12 +7,20 @@
 // value d * 2^-7s, exact.  C = 2^(ea+eb-14) * sum_{s+t<=7} A_s B_t (34 of the
 // 49 digit products).  The products of one level l = s+t are integers times
 // 2^-7l; per k their magnitudes sum to at most 2*129*64 + 3*64*64 = 28800
-// (level 4, the largest), so levels 0..4 accumulate exactly in FP32 over a
-// chunk of 576 k (576 * 28800 < 2^24); they get their own TMEM
-// accumulators and are drained into a double-float (hi, lo) FP32 sum per
-// chunk.  Levels 5..7 share one accumulator (their FP32 rounding is far
-// below 2^-53 of the result).  The dropped levels 8..12 and the operand
-// rounding bound the error near 2^-50 relative to row/column maxima.
+// for levels 0..4, so those accumulate exactly in FP32 over a chunk of 576 k
+// (576 * 28800 < 2^24).  Every level 0..7 has its own 64-column TMEM
+// accumulator (all 512 columns), drained into a double-float (hi, lo) FP32
+// sum per chunk; the FP32 rounding of levels 5..7 is far below 2^-53 of the
+// result.  The dropped levels 8..12 and the operand rounding bound the error
+// near 2^-50 relative to row/column maxima.
+//
+// With level l at columns 64 l, the products of A digit s with B digits
+// t0..t0+n-1 land in the contiguous columns 64 (s+t0) .. 64 (s+t0+n) - 1, and
+// the n B digit tiles lie back to back in shared memory with the same
+// 8-row stride: one MMA with N = 64 n (n <= 4) issues them all and reads the
+// A tile once.  A k-step takes 11 MMAs instead of 34, and runs at the full
+// tensor rate (N = 64 MMAs are bound by their shared-memory operand reads:
+// 48 clocks for 32 of work).
 // Fast BF16 (TN_MODE_FAST_BF16): one slice, the BF16 rounding of each scaled
 // element, FP32 accumulation over the whole K.
 //
@@ -21,7 +29,7 @@
 // GEMM moves each tile with one 1-D bulk copy.  A tile: 128 rows x 64 k
 // (16 KB per slice); B tile: 64 columns x 64 k (8 KB per slice).
 //
-// GEMM CTA (192 threads): warp 0 = loads (bulk copies), warp 1 = MMA issue +
+// GEMM CTA (576 threads): warp 0 = loads (bulk copies), warp 1 = MMA issue +
 // TMEM allocation, warps 2..17 = epilogue: warp w drains TMEM lane quadrant
 // w & 3 and columns 16 * ((w - 2) >> 2) .. +15 of every accumulator, so a
 // chunk's drain -- during which the MMAs wait -- is spread over 16 warps.
@@ -43,7 +51,7 @@ constexpr int kATile = kTM * kTK * 2;  // bytes of one A slice tile
 constexpr int kBTile = kTN * kTK * 2;  // bytes of one B slice tile
 constexpr int kARing = 6, kBRing = 2;
 constexpr int kChunkTiles = 9;  // 576 k per exact-accumulation chunk
-constexpr int kLevels = 6;      // exact levels 0..4 + one shared accumulator for 5..7
+constexpr int kLevels = 8;      // one accumulator per level 0..7
 constexpr int kMaxLevel = 7;    // digit products with s + t <= 7 are kept
 constexpr int kEpiWarps = 16;
 constexpr int kThreadsTc = 64 + 32 * kEpiWarps;
@@ -331,7 +339,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
     // ------------------------------------------------ MMA issue
     // The whole warp runs the loop (every lane waits on the barriers and the
     // outcome is made warp-uniform); one elected lane issues the MMAs and commits.
-    const uint32_t idesc = idesc_bf16_f32(kTM, kTN);
+    // instruction descriptor for N = 64: N = 64 n adds (n - 1) * 8 to its N >> 3 field (bit 17)
+    const uint32_t idesc1 = idesc_bf16_f32(kTM, kTN);
+    static_assert(idesc_bf16_f32(kTM, 4 * kTN) == idesc_bf16_f32(kTM, kTN) + ((3u * (kTN >> 3)) << 17), "N field");
     uint32_t na = 0, nb = 0, nchunk = 0;
     bool ok = true;
     for (int it = blockIdx.x; it < nitems && ok; it += gridDim.x) {
@@ -357,23 +367,34 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
             }
             tc_fence_after();
             const uint64_t adesc = desc_sw128(smem_u32(abuf + sa * kATile));
-            for (int t = 0; t < NS && s + t <= (NS == 1 ? 0 : kMaxLevel); t++) {
-              const int lvl = min(s + t, LV - 1);
-              const uint64_t bdesc = desc_sw128(b_addr + t * kBTile);
-              const uint32_t d = tmem + lvl * kTN;
+            // B digits t = 0 .. T-1 pair with A digit s (s + t <= 7), in
+            // groups of at most 4 (7 -> 4 + 3, 6 -> 3 + 3, 5 -> 3 + 2)
+            const int T = NS == 1 ? 1 : min(NS, kMaxLevel + 1 - s);
+            for (int t0 = 0; t0 < T;) {
+              int tn = T - t0 > 4 ? (T - t0 + 1) >> 1 : T - t0;
+              const int l0 = s + t0;
+              // one accumulate flag per MMA: cut the group where a level is
+              // written for the first time in this chunk (level 7, by s = 1)
+              const uint32_t acc = (touched >> l0) & 1;
+              for (int k = 1; k < tn; k++)
+                if (((touched >> (l0 + k)) & 1) != acc) {
+                  tn = k;
+                  break;
+                }
+              const uint32_t d = tmem + l0 * kTN;
+              const uint64_t bdesc = desc_sw128(b_addr + t0 * kBTile);
+              const uint32_t idesc = idesc1 + ((uint32_t)(tn - 1) * (kTN >> 3) << 17);
               if (nks == kTK / 16) {  // a full 64-k tile: no per-step guard in the issue stream
+                mma_bf16_elect(d, adesc, bdesc, idesc, acc);
 #pragma unroll
-                for (int kk = 0; kk < kTK / 16; kk++) {
+                for (int kk = 1; kk < kTK / 16; kk++)
                   // advancing K by 16 bf16 = 32 bytes inside the swizzle atom: +2 in the address field
-                  mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
-                  touched |= 1u << lvl;
-                }
+                  mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, 1);
               } else {  // the last tile of a ragged K: only the 16-k steps that hold data
-                for (int kk = 0; kk < nks; kk++) {
-                  mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched >> lvl) & 1);
-                  touched |= 1u << lvl;
-                }
+                for (int kk = 0; kk < nks; kk++) mma_bf16_elect(d, adesc + 2 * kk, bdesc + 2 * kk, idesc, kk ? 1 : acc);
               }
+              touched |= ((1u << tn) - 1) << l0;
+              t0 += tn;
             }
             mma_commit_elect(&sh.emptyA[sa]);
             na++;
