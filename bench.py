@@ -486,28 +486,29 @@ def permute_main(args, rank, local, world):
     chi = args.chi
     bonds = [wl.dense_bond(1, chi)] * 3 + [wl.dense_bond(-1, chi)] * 3
     n = chi ** 6
-    x = torch.randn(n, dtype=torch.float64, device="cuda", generator=torch.Generator(device="cuda").manual_seed(5))
-    t = tu.UniTensor(bonds, list(range(6)))
-    torch.cuda.synchronize()
-    tu.capi.call("tn_tensor_set_elem_device", t.h, x.data_ptr(), n)
+    c128 = args.c128  # complex (cflag) elements: 16-byte (re, im) pairs
+    esz = 16 if c128 else 8
+    x = torch.randn(n, dtype=torch.complex128 if c128 else torch.float64, device="cuda",
+                    generator=torch.Generator(device="cuda").manual_seed(5))
     perm = [int(v) for v in args.perm.split(",")]
     rn = args.perm_rownum
     src_map = tu.SectorMap(bonds)
     dst_bonds = [wl.change(bonds[p], 1 if i < rn else -1) for i, p in enumerate(perm)]
     dst_map = tu.SectorMap(dst_bonds)
     y = torch.empty_like(x)
+    run = tu.permute_device_c128 if c128 else tu.permute_device
     for _ in range(args.warmup):
-        tu.permute_device(src_map, dst_map, perm, x.data_ptr(), y.data_ptr())
+        run(src_map, dst_map, perm, x.data_ptr(), y.data_ptr())
     tu.sync()
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with ClockSampler(local) as clk:
         for s_, e_ in ev:
             s_.record(stream)
-            tu.permute_device(src_map, dst_map, perm, x.data_ptr(), y.data_ptr())
+            run(src_map, dst_map, perm, x.data_ptr(), y.data_ptr())
             e_.record(stream)
         torch.cuda.synchronize()
     ms = statistics.median(s_.elapsed_time(e_) for s_, e_ in ev)
-    gbs = 16.0 * n / (ms * 1e-3) / 1e9
+    gbs = 2.0 * esz * n / (ms * 1e-3) / 1e9
     y_keep = y.clone()
     # same-size device-to-device copy on the same stream: the plain-copy ceiling
     cev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -517,7 +518,7 @@ def permute_main(args, rank, local, world):
             y.copy_(x)
             e_.record(stream)
     torch.cuda.synchronize()
-    copy_gbs = 16.0 * n / (statistics.median(s_.elapsed_time(e_) for s_, e_ in cev) * 1e-3) / 1e9
+    copy_gbs = 2.0 * esz * n / (statistics.median(s_.elapsed_time(e_) for s_, e_ in cev) * 1e-3) / 1e9
     exact = bool(torch.equal(y_keep, x.view([chi] * 6).permute(*perm).reshape(-1)))
     peaks = {}
     try:
@@ -527,10 +528,11 @@ def permute_main(args, rank, local, world):
         pass
     peak = peaks.get("hbm_gbs", 6800.0)
     if rank == 0:
-        print(json.dumps({"metric": "permute GB/s (16 B per element)", "value": gbs, "unit": "GB/s", "n_gpus": world,
+        print(json.dumps({"metric": f"permute GB/s ({2 * esz} B per element)", "value": gbs, "unit": "GB/s", "n_gpus": world,
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-                          "bit_exact": exact, "copy_gb_s": copy_gbs, "config": {"workload": f"dense_rank6_chi{chi}_permute", "elements": n,
-                                                         "perm": perm, "l2": "inputs larger than L2"},
+                          "dtype": "c128" if c128 else "f64",
+                          "bit_exact": exact, "copy_gb_s": copy_gbs, "config": {"workload": f"dense_rank6_chi{chi}_permute" + ("_c128" if c128 else ""),
+                                                         "elements": n, "perm": perm, "l2": "inputs larger than L2"},
                           "roofline": {"kernel": "permute", "bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
                                        "frac": gbs / peak, "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
                           "clocks": clk.summary()}))
@@ -775,6 +777,7 @@ def main():
     ap.add_argument("--chi", type=int, default=24)
     ap.add_argument("--perm", default="4,5,0,1,2,3", help="permute workload: the new bond order")
     ap.add_argument("--perm-rownum", type=int, default=2, help="permute workload: incoming bonds after the permute")
+    ap.add_argument("--c128", action="store_true", help="permute workload: complex (cflag) elements, 16 bytes each")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, local, world = dist_env()

@@ -127,6 +127,24 @@ int tn_permute(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, const int* rsp, const
 int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host, double* dst_host,
                           int64_t* written);
 
+/* ---- complex (cflag) permute clients ------------------------------------
+ * Complex FP64 elements (std::complex<double>: (re, im) pairs, 16 bytes, as
+ * the reference's c_elem) in the block layout of the same sector maps.
+ * Replace UniTensor::permute(cflag, ...) (tensor-network/lib/UniTensorComplex.cpp:568-825),
+ * transpose(cflag) (:447-505, conj = 0) and cTranspose(cflag) (:507-566,
+ * conj = 1; the element-wise std::conj of setCTranspose,
+ * numeric/lapack/lib/uni10_lapack_cpu.cpp:822-826).  Bit-exact: a fermionic
+ * sign flips the sign bits of both parts, conj that of the imaginary part.
+ * Buffers are device buffers of elem_num 16-byte elements, 16-byte aligned.
+ * For the transpose, dst is the sector map of the bonds in transposed order
+ * (column bonds as IN, then row bonds as OUT). */
+int tn_permute_c128(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, const int* rsp, const void* src_elem,
+                    void* dst_elem);
+int tn_transpose_c128(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, int conj, const void* src_elem, void* dst_elem);
+/* tn_plan_check_permute for 16-byte elements (host arrays of 2 * elem_num doubles) */
+int tn_plan_check_permute_c128(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host,
+                               double* dst_host, int64_t* written);
+
 /* Host-side check of the operand views a contraction uses instead of this
  * permute when the FP64 kernel can read the source in place (every
  * sub-block of the result a row-major view of the source): builds the

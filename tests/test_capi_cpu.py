@@ -129,3 +129,36 @@ def test_errors_are_statuses():
         tu.SectorMap([(1, [(1000, 0, 0, 2)])])  # U1 out of range
     with pytest.raises(capi.TnError):
         tu.SectorMap([(2, [(0, 0, 0, 2)])])  # bad type
+
+
+@pytest.mark.parametrize("case", PERM, ids=[c["id"] for c in PERM])
+def test_complex_permute_plan_matches_reference(case):
+    """The complex (cflag) permute moves 16-byte (re, im) pairs with the
+    real permute's sector arithmetic (UniTensorComplex.cpp:592-825 is
+    UniTensorReal.cpp:532-768 on Complex elements): with re = T and
+    im = -2 T (exact), the result is (P, -2 P) bit for bit, fermionic signs
+    on both parts, on tiles of half the real tile limits."""
+    bonds = G.bonds_of(case["T"])
+    labels, new = case["T"]["labels"], case["new_labels"]
+    rsp = [labels.index(l) for l in new]
+    out = [wl.change(bonds[rsp[b]], 1 if b < case["rownum"] else -1) for b in range(len(bonds))]
+    x = G.arr(case["id"], "T")
+    z = x + 1j * (-2.0 * x)
+    got, written = tu.plan_check_permute_c128(tu.SectorMap(bonds), tu.SectorMap(out), rsp, z)
+    assert written == x.size
+    p = G.arr(case["id"], "P")
+    assert np.array_equal(got.real, p) and np.array_equal(got.imag, -2.0 * p)
+
+
+def test_complex_permute_plans_of_dense_tensors():
+    """Dense rank-6 complex permutes on all three tile modes (2-D transpose,
+    stacked planes of short bonds, long rows) against numpy."""
+    rng = np.random.default_rng(8)
+    chi = 6
+    bonds = [(1, [(0, 0, 0, chi)])] * 3 + [(-1, [(0, 0, 0, chi)])] * 3
+    x = rng.uniform(-1, 1, chi ** 6) + 1j * rng.uniform(-1, 1, chi ** 6)
+    for perm, rn in (((4, 5, 0, 1, 2, 3), 2), ((0, 3, 5, 1, 2, 4), 3), ((1, 2, 0, 3, 4, 5), 3), ((5, 4, 3, 2, 1, 0), 3)):
+        out = [wl.change(bonds[perm[b]], 1 if b < rn else -1) for b in range(6)]
+        got, written = tu.plan_check_permute_c128(tu.SectorMap(bonds), tu.SectorMap(out), list(perm), x)
+        assert written == x.size
+        assert np.array_equal(got, x.reshape([chi] * 6).transpose(perm).reshape(-1))

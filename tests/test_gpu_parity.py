@@ -53,6 +53,54 @@ def test_permute_transpose_bit_exact(tu, case):
     assert np.array_equal(t.get_elem(), G.arr(case["id"], "PT"))
 
 
+@pytest.mark.parametrize("case", PERM, ids=[c["id"] for c in PERM])
+def test_complex_permute_transpose_ctranspose_bit_exact(tu, case):
+    """Complex (cflag) permute, transpose and cTranspose on the GPU
+    (UniTensorComplex.cpp:447-825): re = T, im = -2 T (exact) give
+    (P, -2 P), then (PT, -2 PT), and conjugated (PT, 2 PT), bit for bit."""
+    import torch
+
+    bonds = G.bonds_of(case["T"])
+    labels, new = case["T"]["labels"], case["new_labels"]
+    rsp = [labels.index(l) for l in new]
+    out = [wl.change(bonds[rsp[b]], 1 if b < case["rownum"] else -1) for b in range(len(bonds))]
+    x = G.arr(case["id"], "T")
+    z = torch.from_numpy(x + 1j * (-2.0 * x)).cuda()
+    y = torch.full_like(z, complex(np.nan, np.nan))
+    src, dst = tu.SectorMap(bonds), tu.SectorMap(out)
+    tu.permute_device_c128(src, dst, rsp, z.data_ptr(), y.data_ptr())
+    tu.sync()
+    p, pt = G.arr(case["id"], "P"), G.arr(case["id"], "PT")
+    got = y.cpu().numpy()
+    assert np.array_equal(got.real, p) and np.array_equal(got.imag, -2.0 * p)
+    tmap = tu.SectorMap(G.bonds_of(case["out_transpose"]))
+    for conj in (False, True):
+        w = torch.full_like(z, complex(np.nan, np.nan))
+        tu.transpose_device_c128(dst, tmap, conj, y.data_ptr(), w.data_ptr())
+        tu.sync()
+        got = w.cpu().numpy()
+        assert np.array_equal(got.real, pt)
+        assert np.array_equal(got.imag, (2.0 if conj else -2.0) * pt)
+
+
+@pytest.mark.parametrize("perm,rn", [((4, 5, 0, 1, 2, 3), 2), ((0, 3, 5, 1, 2, 4), 3), ((1, 2, 0, 3, 4, 5), 3),
+                                     ((5, 4, 3, 2, 1, 0), 3), ((0, 1, 2, 3, 5, 4), 3)])
+def test_complex_dense_permutes_bit_exact(tu, perm, rn):
+    """Dense rank-6 chi=12 complex permutes (2-D transpose, stacked planes,
+    long rows) against torch's permute."""
+    import torch
+
+    chi = 12
+    bonds = [wl.dense_bond(1, chi)] * 3 + [wl.dense_bond(-1, chi)] * 3
+    g = torch.Generator(device="cuda").manual_seed(11)
+    x = torch.randn(chi ** 6, dtype=torch.complex128, device="cuda", generator=g)
+    y = torch.empty_like(x)
+    out = [wl.change(bonds[perm[b]], 1 if b < rn else -1) for b in range(6)]
+    tu.permute_device_c128(tu.SectorMap(bonds), tu.SectorMap(out), list(perm), x.data_ptr(), y.data_ptr())
+    tu.sync()
+    assert torch.equal(y, x.view([chi] * 6).permute(*perm).reshape(-1))
+
+
 @pytest.mark.parametrize("case", CON, ids=[c["id"] for c in CON])
 def test_contract_fp64(tu, case):
     a = tu.UniTensor(G.bonds_of(case["A"]), case["A"]["labels"], G.arr(case["id"], "A"))

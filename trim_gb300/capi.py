@@ -71,6 +71,9 @@ _PROTOS = {
     "tn_sectormap_destroy": (_I, [_P]),
     "tn_permute": (_I, [_P, _P, _P, _IP, _DP, _DP]),
     "tn_plan_check_permute": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
+    "tn_permute_c128": (_I, [_P, _P, _P, _IP, _DP, _DP]),
+    "tn_transpose_c128": (_I, [_P, _P, _P, _I, _DP, _DP]),
+    "tn_plan_check_permute_c128": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
     "tn_plan_check_views": (_I, [_P, _P, _IP, _DP, _DP, _IP]),
     "tn_contract_sectors": (_I, [_P, _I, _I, C.POINTER(SectorGemm), _DP, _DP, _DP]),
     "tn_autotune": (_I, [_P, _I, _I64P]),

@@ -244,6 +244,53 @@ int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const do
   });
 }
 
+int tn_permute_c128(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, const int* rsp, const void* src_elem,
+                    void* dst_elem) {
+  return guard([&] {
+    need(src, "src");
+    need(dst, "dst");
+    need(rsp, "rsp");
+    tn::Ctx* c = tn::as_ctx(ctx);
+    std::vector<int> r(rsp, rsp + src->m->bonds.size());
+    auto plan = tn::get_perm_plan(*c, *src->m, *dst->m, r, 16);
+    if (plan->elem_num > 0) {
+      need(src_elem, "src_elem");
+      need(dst_elem, "dst_elem");
+      if (((uintptr_t)src_elem | (uintptr_t)dst_elem) & 15) tn::fail(TN_ERR_ARG, "complex buffers must be 16-byte aligned");
+    }
+    tn::run_permute(*c, *plan, src_elem, dst_elem);
+  });
+}
+
+int tn_transpose_c128(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, int conj, const void* src_elem, void* dst_elem) {
+  return guard([&] {
+    need(src, "src");
+    need(dst, "dst");
+    tn::Ctx* c = tn::as_ctx(ctx);
+    if (src->m->elem_num != dst->m->elem_num) tn::fail(TN_ERR_SHAPE, "transpose: element counts differ");
+    auto plan = tn::get_transpose_plan(*c, *src->m, *dst->m, 16, conj != 0);
+    if (plan->elem_num > 0) {
+      need(src_elem, "src_elem");
+      need(dst_elem, "dst_elem");
+      if (((uintptr_t)src_elem | (uintptr_t)dst_elem) & 15) tn::fail(TN_ERR_ARG, "complex buffers must be 16-byte aligned");
+    }
+    tn::run_permute(*c, *plan, src_elem, dst_elem);
+  });
+}
+
+int tn_plan_check_permute_c128(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host,
+                               double* dst_host, int64_t* written) {
+  return guard([&] {
+    need(src, "src");
+    need(dst, "dst");
+    need(rsp, "rsp");
+    std::vector<int> r(rsp, rsp + src->m->bonds.size());
+    auto plan = tn::host_plan(tn::build_perm_subs(*src->m, *dst->m, r, 16), src->m->elem_num, 16);
+    int64_t w = tn::check_permute_plan_host(*plan, src_host, dst_host);
+    if (written) *written = w;
+  });
+}
+
 int tn_plan_check_views(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host, double* dst_host,
                         int* applies) {
   return guard([&] {

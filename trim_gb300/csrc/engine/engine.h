@@ -134,6 +134,8 @@ struct PermPlan {
   int nsub = 0;
   int64_t ntiles = 0;
   int64_t elem_num = 0;
+  int esz = 8;        // element size in bytes: 8 (real) or 16 (complex pairs)
+  bool conj = false;  // 16-byte elements: conjugate on the way (cTranspose)
 };
 using PermPlanP = std::shared_ptr<PermPlan>;
 
@@ -306,16 +308,21 @@ void release_solver(Ctx* c);  // destroys the cuSOLVER handle, if any
 Ctx* as_ctx(tn_ctx_t c);
 
 // ---------------------------------------------------------------- operations
-PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
-PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst);
-std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp);
-PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num);  // tiles assigned, no device copy
+// esz: element size in bytes, 8 (real FP64) or 16 (complex FP64 pairs: tile
+// limits halved); conj: the 16-byte transpose also conjugates (cTranspose)
+PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp,
+                        int esz = 8);
+PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, int esz = 8, bool conj = false);
+std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp,
+                                     int esz = 8);
+PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num, int esz = 8);  // tiles assigned, no device copy
 // Runs a plan's tile walk on the host (the kernel's index arithmetic, decoded
 // with the same helper): every source and destination offset is checked
 // against [0, elem_num) and the copy is done into dst.  Returns the number
 // of elements written, or throws on an out-of-range offset.
 int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double* dst);
-void run_permute(Ctx& ctx, const PermPlan& plan, const double* src, double* dst);
+// src / dst hold plan.elem_num elements of plan.esz bytes
+void run_permute(Ctx& ctx, const PermPlan& plan, const void* src, void* dst);
 
 uint64_t hash_list(const std::vector<tn_sector_gemm>& list, int tag);
 // sector GEMMs: C_i = A_i . B_i for every item, all in one grouped launch
@@ -346,8 +353,8 @@ std::vector<GemmTile> plan_fp64(const std::vector<tn_sector_gemm>& list, int num
                                 int64_t* ws_elems, const Fp64Policy& pol = Fp64Policy());
 
 // kernel launchers (defined in the .cu files)
-void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles,
-                           const double* src, double* dst, int grid, cudaStream_t s);
+void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles, int esz,
+                           bool conj, const void* src, void* dst, int grid, cudaStream_t s);
 // counters (one int per split group, zero between launches) may be null: then
 // split tiles need launch_splitk_reduce afterwards; otherwise the last CTA of
 // each split group sums its partial tiles in split order and resets the counter

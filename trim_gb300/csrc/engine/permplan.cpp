@@ -25,7 +25,12 @@ struct Dim {
 //         that each tile still moves thousands of elements; z is the dim
 //         with the smallest source or destination stride (it extends a
 //         contiguous run on one side).
-void choose_tile(PermSub& ps) {
+//
+// Limits are in elements for 8-byte elements (a tile <= 4096 elements, a
+// transpose tile within 64 x 65, rows of <= 64); es = 2 (16-byte elements)
+// halves them, so a tile fills the same shared memory.
+void choose_tile(PermSub& ps, int es) {
+  const int64_t kTile = 4096 / es, kStage = (64 * 65) / es, kRow = 64 / es;
   const int n = ps.ndim;
   ps.ydim = -1;
   ps.zdim = -1;
@@ -44,24 +49,24 @@ void choose_tile(PermSub& ps) {
       if (y < 0 || ps.sstride[i] < ps.sstride[y]) y = i;
     if (y >= 0 && ps.sstride[y] > ps.sstride[x]) y = -1;
   }
-  // tiles hold at most 4096 elements (16 per thread of a 256-thread CTA);
-  // transpose tiles also fit a 64 x 65 shared-memory array
+  // tiles hold at most kTile elements (16 per thread of a 256-thread CTA for
+  // 8-byte elements); transpose tiles also fit kStage elements with a pitch of tx + 1
   if (y >= 0) {
     ps.mode = 1;
     ps.ydim = y;
-    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 64);
-    int64_t ty = std::min<int64_t>(4096 / ps.tx, (64 * 65) / (ps.tx + 1));
+    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], kRow);
+    int64_t ty = std::min<int64_t>(kTile / ps.tx, kStage / (ps.tx + 1));
     ps.ty = (int32_t)std::min<int64_t>(ps.dims[y], std::min<int64_t>(ty, 1024));
   } else {
-    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], 4096);
+    ps.tx = (int32_t)std::min<int64_t>(ps.dims[x], kTile);
     if (n >= 2) {
       ps.ydim = n - 2;
-      ps.ty = (int32_t)std::min<int64_t>(ps.dims[n - 2], std::max<int64_t>(1, 4096 / ps.tx));
+      ps.ty = (int32_t)std::min<int64_t>(ps.dims[n - 2], std::max<int64_t>(1, kTile / ps.tx));
     } else {
       ps.ty = 1;
     }
   }
-  if (ps.mode == 1 && (int64_t)ps.tx * ps.ty <= 2048 && n >= 3) {
+  if (ps.mode == 1 && (int64_t)ps.tx * ps.ty <= kTile / 2 && n >= 3) {
     int z = -1;
     int64_t best = 0;
     for (int i = 0; i < n; i++) {
@@ -72,8 +77,8 @@ void choose_tile(PermSub& ps) {
         best = c;
       }
     }
-    const int64_t tz = std::min<int64_t>({(int64_t)ps.dims[z], (int64_t)(64 * 65) / ((int64_t)ps.ty * (ps.tx + 1)),
-                                         (int64_t)4096 / ((int64_t)ps.tx * ps.ty)});
+    const int64_t tz = std::min<int64_t>({(int64_t)ps.dims[z], kStage / ((int64_t)ps.ty * (ps.tx + 1)),
+                                         kTile / ((int64_t)ps.tx * ps.ty)});
     if (tz > 1) {
       ps.mode = 2;
       ps.zdim = z;
@@ -91,10 +96,12 @@ void choose_tile(PermSub& ps) {
 
 }  // namespace
 
-static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermSub>& subs, int64_t elem_num);
+static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermSub>& subs, int64_t elem_num, int esz,
+                             bool conj);
 
-PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp) {
-  std::string key = src.key + "#" + dst.key + "#";
+PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp, int esz) {
+  if (esz != 8 && esz != 16) fail(TN_ERR_ARG, "permute: element size must be 8 or 16 bytes");
+  std::string key = src.key + "#" + dst.key + "#" + (esz == 16 ? "c#" : "");
   for (int r : rsp) key += std::to_string(r) + ",";
   {
     std::lock_guard<std::mutex> lk(ctx.mu);
@@ -104,8 +111,8 @@ PermPlanP get_perm_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, co
       return it->second;
     }
   }
-  std::vector<PermSub> subs = build_perm_subs(src, dst, rsp);
-  return finish_plan(ctx, key, subs, src.elem_num);
+  std::vector<PermSub> subs = build_perm_subs(src, dst, rsp, esz);
+  return finish_plan(ctx, key, subs, src.elem_num, esz, false);
 }
 
 // The bond swaps that carry fermionic signs (UniTensorReal.cpp:656-681 with
@@ -130,7 +137,7 @@ static std::vector<std::pair<int, int>> fermion_swaps(int n, int rbn_in, int rbn
   return swaps;
 }
 
-std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp) {
+std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst, const std::vector<int>& rsp, int esz) {
   const int n = (int)src.bonds.size();
   if ((int)dst.bonds.size() != n || (int)rsp.size() != n) fail(TN_ERR_ARG, "permute: bond counts differ");
   // the destination must be the permuted source (bond b <- source bond rsp[b])
@@ -221,7 +228,7 @@ std::vector<PermSub> build_perm_subs(const SectorMap& src, const SectorMap& dst,
       ps.sstride[i] = dims[i].s;
       ps.dstride[i] = dims[i].d;
     }
-    choose_tile(ps);
+    choose_tile(ps, esz / 8);
     subs.push_back(ps);
   }
   return subs;
@@ -356,8 +363,10 @@ OpViewsP get_op_views(Ctx& ctx, const SectorMap& src, const SectorMap& dst, cons
 // Block-wise transpose of UniTensor::transpose (UniTensorReal.cpp:448-506):
 // block q of the source (R x C, row-major) becomes block q of the destination
 // (C x R).  One 2-D copy per block.
-PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst) {
-  std::string key = "T#" + src.key + "#" + dst.key;
+PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& dst, int esz, bool conj) {
+  if (esz != 8 && esz != 16) fail(TN_ERR_ARG, "transpose: element size must be 8 or 16 bytes");
+  if (conj && esz != 16) fail(TN_ERR_ARG, "transpose: conjugation needs complex (16-byte) elements");
+  std::string key = std::string(esz == 16 ? (conj ? "CT#" : "cT#") : "T#") + src.key + "#" + dst.key;
   {
     std::lock_guard<std::mutex> lk(ctx.mu);
     auto it = ctx.perm_cache.find(key);
@@ -394,14 +403,15 @@ PermPlanP get_transpose_plan(Ctx& ctx, const SectorMap& src, const SectorMap& ds
       ps.sstride[i] = dims[i].s;
       ps.dstride[i] = dims[i].d;
     }
-    choose_tile(ps);
+    choose_tile(ps, esz / 8);
     subs.push_back(ps);
   }
-  return finish_plan(ctx, key, subs, src.elem_num);
+  return finish_plan(ctx, key, subs, src.elem_num, esz, conj);
 }
 
-PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num) {
+PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num, int esz) {
   auto plan = std::make_shared<PermPlan>();
+  plan->esz = esz;
   std::vector<int64_t>& tile_start = plan->host_tile_start;
   tile_start.reserve(subs.size() + 1);
   int64_t tiles = 0;
@@ -418,8 +428,10 @@ PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num) {
   return plan;
 }
 
-static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermSub>& subs_in, int64_t elem_num) {
-  PermPlanP plan = host_plan(std::move(subs_in), elem_num);
+static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermSub>& subs_in, int64_t elem_num, int esz,
+                             bool conj) {
+  PermPlanP plan = host_plan(std::move(subs_in), elem_num, esz);
+  plan->conj = conj;
   const std::vector<PermSub>& subs = plan->host_subs;
   const std::vector<int64_t>& tile_start = plan->host_tile_start;
   if (!subs.empty()) {
@@ -439,13 +451,13 @@ static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermS
   return plan;
 }
 
-void run_permute(Ctx& ctx, const PermPlan& plan, const double* src, double* dst) {
+void run_permute(Ctx& ctx, const PermPlan& plan, const void* src, void* dst) {
   if (plan.ntiles == 0) return;
   // persistent: two resident CTAs per SM (100 KB of staging shared memory each)
   int64_t grid = std::min<int64_t>(plan.ntiles, (int64_t)ctx.num_sms * 2);
-  ProfScope ps(ctx, "permute", 16.0 * plan.elem_num, 0);
+  ProfScope ps(ctx, "permute", 2.0 * plan.esz * plan.elem_num, 0);
   launch_permute_kernel((const PermSub*)plan.subs->ptr, (const int64_t*)plan.tile_start->ptr, plan.nsub, plan.ntiles,
-                        src, dst, (int)grid, ctx.stream);
+                        plan.esz, plan.conj, src, dst, (int)grid, ctx.stream);
   ctx.launched();
 }
 

@@ -7,6 +7,13 @@
 // source-contiguous dim and the tile is transposed through shared memory so
 // loads are coalesced too; mode 2 stacks tz planes of a third dim z into a
 // small transpose tile.  Remaining dims are decoded once per tile.
+//
+// Elements are 8 bytes (real FP64) or 16 bytes (complex FP64 as (re, im)
+// pairs, the cflag twins UniTensorComplex.cpp:447-825): the kernel is the same
+// with the element type as a template parameter; the plan halves its tile
+// limits for 16-byte elements so a tile takes the same shared memory.  A
+// sub-block's sign flips both parts; conj (cTranspose) also flips the
+// imaginary part.
 #include <vector>
 
 #include "../engine/engine.h"
@@ -127,9 +134,19 @@ __device__ __forceinline__ double flip_sign(double x, uint64_t flip) {
   return __longlong_as_double((long long)((uint64_t)__double_as_longlong(x) ^ flip));
 }
 
-__device__ __forceinline__ void cp_async8(double* smem, const double* gmem) {
+// sign-bit masks of the real and imaginary parts
+struct Flip {
+  uint64_t re, im;
+};
+__device__ __forceinline__ double apply_flip(double x, Flip f) { return flip_sign(x, f.re); }
+__device__ __forceinline__ double2 apply_flip(double2 x, Flip f) {
+  return make_double2(flip_sign(x.x, f.re), flip_sign(x.y, f.im));
+}
+
+template <typename T>
+__device__ __forceinline__ void cp_async_el(T* smem, const T* gmem) {
   unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gmem) : "memory");
+  asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gmem), "n"((int)sizeof(T)) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
@@ -155,7 +172,8 @@ __device__ __forceinline__ TileInfo decode_at(const PermSub* __restrict__ subs, 
 // Mode 0 keeps the tile as [y][x] (pitch tx), mode 1 as [y][x] with pitch
 // tx + 1; loads run with lanes along x (mode 0) or along y, the
 // source-contiguous dim (mode 1).
-__device__ __forceinline__ void issue_tile(const TileInfo& w, const double* __restrict__ src, double* buf) {
+template <typename T>
+__device__ __forceinline__ void issue_tile(const TileInfo& w, const T* __restrict__ src, T* buf) {
   if (w.mode >= 0) {
     if (w.mode == 2) {
       // [z][y][x] with pitch tx + 1.  A thread takes (y, x) pairs with lanes
@@ -165,33 +183,33 @@ __device__ __forceinline__ void issue_tile(const TileInfo& w, const double* __re
       for (int p = threadIdx.x; p < pairs; p += kThreads) {
         const int xx = p / w.ty, yy = p - xx * w.ty;
         if (xx >= w.nx || yy >= w.ny) continue;
-        const double* g = src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx;
-        double* sp = buf + yy * pitch + xx;
-        for (int zz = 0; zz < w.nz; zz++, g += w.sz, sp += plane) cp_async8(sp, g);
+        const T* g = src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx;
+        T* sp = buf + yy * pitch + xx;
+        for (int zz = 0; zz < w.nz; zz++, g += w.sz, sp += plane) cp_async_el(sp, g);
       }
     } else if (w.mode == 0 && w.tx >= kThreads) {  // long rows: lanes stride along each row
       for (int yy = 0; yy < w.ny; yy++) {
-        const double* g = src + w.bs + (int64_t)yy * w.sy + (int64_t)threadIdx.x * w.sx;
+        const T* g = src + w.bs + (int64_t)yy * w.sy + (int64_t)threadIdx.x * w.sx;
         const int64_t gstep = (int64_t)kThreads * w.sx;
-        double* sp = buf + yy * w.tx + threadIdx.x;
-        for (int xx = threadIdx.x; xx < w.nx; xx += kThreads, g += gstep, sp += kThreads) cp_async8(sp, g);
+        T* sp = buf + yy * w.tx + threadIdx.x;
+        for (int xx = threadIdx.x; xx < w.nx; xx += kThreads, g += gstep, sp += kThreads) cp_async_el(sp, g);
       }
     } else if (w.mode == 0) {
       const int q = kThreads / w.tx, r = kThreads - q * w.tx;
       const int y0 = threadIdx.x / w.tx, x0 = threadIdx.x - y0 * w.tx;
       if (r == 0) {  // constant step: q whole rows
         if (x0 < w.nx) {
-          const double* g = src + w.bs + (int64_t)y0 * w.sy + (int64_t)x0 * w.sx;
+          const T* g = src + w.bs + (int64_t)y0 * w.sy + (int64_t)x0 * w.sx;
           const int64_t gstep = (int64_t)q * w.sy;
-          double* sp = buf + y0 * w.tx + x0;
+          T* sp = buf + y0 * w.tx + x0;
           const int sstep = q * w.tx;
-          for (int y = y0; y < w.ny; y += q, g += gstep, sp += sstep) cp_async8(sp, g);
+          for (int y = y0; y < w.ny; y += q, g += gstep, sp += sstep) cp_async_el(sp, g);
         }
       } else {
         int yy = y0, xx = x0;
 #pragma unroll 4
         for (int k = 0; k < kPerThread; k++) {
-          if (yy < w.ny && xx < w.nx) cp_async8(buf + yy * w.tx + xx, src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx);
+          if (yy < w.ny && xx < w.nx) cp_async_el(buf + yy * w.tx + xx, src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx);
           xx += r;
           yy += q;
           if (xx >= w.tx) { xx -= w.tx; yy++; }
@@ -203,16 +221,16 @@ __device__ __forceinline__ void issue_tile(const TileInfo& w, const double* __re
       const int x0 = threadIdx.x / w.ty, y0 = threadIdx.x - x0 * w.ty;
       if (r == 0) {  // constant step: q whole columns
         if (y0 < w.ny) {
-          const double* g = src + w.bs + (int64_t)y0 * w.sy + (int64_t)x0 * w.sx;
+          const T* g = src + w.bs + (int64_t)y0 * w.sy + (int64_t)x0 * w.sx;
           const int64_t gstep = (int64_t)q * w.sx;
-          double* sp = buf + y0 * pitch + x0;
-          for (int x = x0; x < w.nx; x += q, g += gstep, sp += q) cp_async8(sp, g);
+          T* sp = buf + y0 * pitch + x0;
+          for (int x = x0; x < w.nx; x += q, g += gstep, sp += q) cp_async_el(sp, g);
         }
       } else {
         int xx = x0, yy = y0;
 #pragma unroll 4
         for (int k = 0; k < kPerThread; k++) {
-          if (xx < w.nx && yy < w.ny) cp_async8(buf + yy * pitch + xx, src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx);
+          if (xx < w.nx && yy < w.ny) cp_async_el(buf + yy * pitch + xx, src + w.bs + (int64_t)yy * w.sy + (int64_t)xx * w.sx);
           yy += r;
           xx += q;
           if (yy >= w.ty) { yy -= w.ty; xx++; }
@@ -224,25 +242,27 @@ __device__ __forceinline__ void issue_tile(const TileInfo& w, const double* __re
 }
 
 // Store a landed tile from shared memory with lanes along x (destination-contiguous).
-__device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf, double* __restrict__ dst) {
+template <typename T>
+__device__ __forceinline__ void store_tile(const TileInfo& w, const T* buf, T* __restrict__ dst, uint64_t conj) {
   const uint64_t flip = w.neg ? 0x8000000000000000ull : 0ull;
+  const Flip f{flip, flip ^ conj};
   if (w.mode == 2) {  // (x, y) pairs with lanes along x; the z planes with a constant step
     const int pitch = w.tx + 1, plane = w.ty * pitch, pairs = w.ty * w.tx;
     for (int p = threadIdx.x; p < pairs; p += kThreads) {
       const int yy = p / w.tx, xx = p - yy * w.tx;
       if (xx >= w.nx || yy >= w.ny) continue;
-      const double* sp = buf + yy * pitch + xx;
-      double* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx;
-      for (int zz = 0; zz < w.nz; zz++, sp += plane, g += w.dz) *g = flip_sign(*sp, flip);
+      const T* sp = buf + yy * pitch + xx;
+      T* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx;
+      for (int zz = 0; zz < w.nz; zz++, sp += plane, g += w.dz) *g = apply_flip(*sp, f);
     }
     return;
   }
   if (w.mode == 0 && w.tx >= kThreads) {  // long rows, as loaded
     for (int yy = 0; yy < w.ny; yy++) {
-      const double* sp = buf + yy * w.tx + threadIdx.x;
-      double* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)threadIdx.x * w.dx;
+      const T* sp = buf + yy * w.tx + threadIdx.x;
+      T* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)threadIdx.x * w.dx;
       const int64_t gstep = (int64_t)kThreads * w.dx;
-      for (int xx = threadIdx.x; xx < w.nx; xx += kThreads, sp += kThreads, g += gstep) *g = flip_sign(*sp, flip);
+      for (int xx = threadIdx.x; xx < w.nx; xx += kThreads, sp += kThreads, g += gstep) *g = apply_flip(*sp, f);
     }
     return;
   }
@@ -251,12 +271,12 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf,
   const int y0 = threadIdx.x / w.tx, x0 = threadIdx.x - y0 * w.tx;
   if (r == 0) {  // constant step: q whole rows
     if (x0 < w.nx) {
-      const double* sp = buf + y0 * pitch + x0;
+      const T* sp = buf + y0 * pitch + x0;
       const int sstep = q * pitch;
-      double* g = dst + w.bd + (int64_t)y0 * w.dy + (int64_t)x0 * w.dx;
+      T* g = dst + w.bd + (int64_t)y0 * w.dy + (int64_t)x0 * w.dx;
       const int64_t gstep = (int64_t)q * w.dy;
-      if (w.neg) {
-        for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = flip_sign(*sp, flip);
+      if (f.re | f.im) {
+        for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = apply_flip(*sp, f);
       } else {
         for (int y = y0; y < w.ny; y += q, sp += sstep, g += gstep) *g = *sp;
       }
@@ -267,8 +287,8 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const double* buf,
 #pragma unroll 4
   for (int k = 0; k < kPerThread; k++) {
     if (yy < w.ny && xx < w.nx) {
-      double v = buf[yy * pitch + xx];
-      dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx] = flip_sign(v, flip);
+      const T v = buf[yy * pitch + xx];
+      dst[w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx] = apply_flip(v, f);
     }
     xx += r;
     yy += q;
@@ -296,11 +316,14 @@ __device__ __forceinline__ void decode_batch(TileInfo* ring, const PermSub* __re
   ring[k % kRing] = decode_at(subs, tile_start, nsub, ntiles, blockIdx.x + k * (int64_t)gridDim.x);
 }
 
+template <typename T>
 __global__ void __launch_bounds__(kThreads, 2) permute_kernel(const PermSub* __restrict__ subs,
                                                               const int64_t* __restrict__ tile_start, int nsub,
-                                                              int64_t ntiles, const double* __restrict__ src,
-                                                              double* __restrict__ dst) {
-  extern __shared__ double smem[];  // kStages * kSmem doubles
+                                                              int64_t ntiles, const T* __restrict__ src,
+                                                              T* __restrict__ dst, uint64_t conj) {
+  constexpr int kSmemT = kSmem * (int)sizeof(double) / (int)sizeof(T);  // one stage, in elements
+  extern __shared__ double smem_d[];  // kStages * kSmem doubles
+  T* smem = (T*)smem_d;
   __shared__ TileInfo ring[kRing];
   const int64_t G = gridDim.x;
   if (threadIdx.x < 32) decode_batch(ring, subs, tile_start, nsub, ntiles, 0);
@@ -308,7 +331,7 @@ __global__ void __launch_bounds__(kThreads, 2) permute_kernel(const PermSub* __r
 #pragma unroll
   for (int s = 0; s < kStages - 1; s++) {
     const TileInfo w = ring[s];
-    issue_tile(w, src, smem + s * kSmem);
+    issue_tile(w, src, smem + s * kSmemT);
   }
   int stage = 0;
   int64_t i = 0;
@@ -316,14 +339,14 @@ __global__ void __launch_bounds__(kThreads, 2) permute_kernel(const PermSub* __r
     const int ns = (stage + kStages - 1) % kStages;  // stored in the previous iteration
     {
       const TileInfo w = ring[(i + kStages - 1) % kRing];
-      issue_tile(w, src, smem + ns * kSmem);
+      issue_tile(w, src, smem + ns * kSmemT);
     }
     if (threadIdx.x < 32 && (i & 31) == 0) decode_batch(ring, subs, tile_start, nsub, ntiles, i + 32);
     cp_async_wait<kStages - 1>();  // this thread's loads of tile t have landed
     __syncthreads();               // ... and every other thread's
     {
       const TileInfo w = ring[i % kRing];
-      store_tile(w, smem + stage * kSmem, dst);
+      store_tile(w, smem + stage * kSmemT, dst, conj);
     }
     __syncthreads();  // the stage is reloaded in the next iteration
     stage = (stage + 1) % kStages;
@@ -342,8 +365,12 @@ __global__ void scale_kernel(double* __restrict__ p, int64_t n, double a) {
 
 }  // namespace
 
+// src / dst: host arrays of plan.elem_num elements of plan.esz bytes (one or
+// two doubles each).
 int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double* dst) {
   const int64_t n = plan.elem_num;
+  const int es = plan.esz / 8;
+  if (es != 1 && es != 2) fail(TN_ERR_ARG, "plan check: element size must be 8 or 16 bytes");
   std::vector<unsigned char> hit(n, 0);
   int64_t written = 0;
   for (int64_t t = 0; t < plan.ntiles; t++) {
@@ -352,7 +379,8 @@ int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double*
     if (w.nx > w.tx || w.ny > w.ty || w.nz > w.tz || w.nx <= 0 || w.ny <= 0 || w.nz <= 0)
       fail(TN_ERR_ARG, "plan check: bad tile extents");
     if (w.mode != 2 && w.tz != 1) fail(TN_ERR_ARG, "plan check: stacked planes outside mode 2");
-    if (w.mode >= 1 && (int64_t)w.tz * w.ty * (w.tx + 1) > kSmem) fail(TN_ERR_ARG, "plan check: tile exceeds shared memory");
+    const int64_t stage = w.mode >= 1 ? (int64_t)w.tz * w.ty * (w.tx + 1) : (int64_t)w.tx * w.ty;
+    if (stage > kSmem / es) fail(TN_ERR_ARG, "plan check: tile exceeds shared memory");
     if ((int64_t)w.tx * w.ty * w.tz > (int64_t)kThreads * kPerThread)
       fail(TN_ERR_ARG, "plan check: tile exceeds thread walk");
     if (w.mode == 2 && ((int64_t)w.tx * w.ty * w.tz >= (1 << 16) || w.tx > 4096 || w.ty > 4096))
@@ -364,23 +392,39 @@ int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double*
           int64_t d = w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx + (int64_t)zz * w.dz;
           if (so < 0 || so >= n || d < 0 || d >= n) fail(TN_ERR_ARG, "plan check: offset out of range");
           if (hit[d]++) fail(TN_ERR_ARG, "plan check: destination written twice");
-          dst[d] = w.neg ? -src[so] : src[so];
+          for (int c = 0; c < es; c++) {
+            const bool neg = w.neg != (c == 1 && plan.conj);
+            const double v = src[so * es + c];
+            dst[d * es + c] = neg ? -v : v;
+          }
           written++;
         }
   }
   return written;
 }
 
-void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles,
-                           const double* src, double* dst, int grid, cudaStream_t s) {
+template <typename T>
+static void launch_permute_t(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles, const T* src,
+                             T* dst, uint64_t conj, int grid, cudaStream_t s) {
   const size_t smem = (size_t)kStages * kSmem * sizeof(double);
-  static bool attr = false;  // once per process; the attribute is per function
+  static bool attr = false;  // once per process and instantiation; the attribute is per function
   if (!attr) {
-    TN_CUDA(cudaFuncSetAttribute(permute_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    TN_CUDA(cudaFuncSetAttribute(permute_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  permute_kernel<<<grid, kThreads, smem, s>>>(subs, tile_start, nsub, ntiles, src, dst);
+  permute_kernel<T><<<grid, kThreads, smem, s>>>(subs, tile_start, nsub, ntiles, src, dst, conj);
   TN_CUDA(cudaGetLastError());
+}
+
+void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles, int esz,
+                           bool conj, const void* src, void* dst, int grid, cudaStream_t s) {
+  if (esz == 8)
+    launch_permute_t<double>(subs, tile_start, nsub, ntiles, (const double*)src, (double*)dst, 0, grid, s);
+  else if (esz == 16)
+    launch_permute_t<double2>(subs, tile_start, nsub, ntiles, (const double2*)src, (double2*)dst,
+                              conj ? 0x8000000000000000ull : 0ull, grid, s);
+  else
+    fail(TN_ERR_ARG, "permute: element size must be 8 or 16 bytes");
 }
 
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s) {

@@ -66,6 +66,26 @@ def permute_device(src: SectorMap, dst: SectorMap, rsp, src_ptr: int, dst_ptr: i
     call("tn_permute", None, src.h, dst.h, int_array(rsp), src_ptr, dst_ptr)
 
 
+def permute_device_c128(src: SectorMap, dst: SectorMap, rsp, src_ptr: int, dst_ptr: int) -> None:
+    """Complex (cflag) permute: elements are 16-byte (re, im) FP64 pairs."""
+    call("tn_permute_c128", None, src.h, dst.h, int_array(rsp), src_ptr, dst_ptr)
+
+
+def transpose_device_c128(src: SectorMap, dst: SectorMap, conj: bool, src_ptr: int, dst_ptr: int) -> None:
+    """Complex transpose (conj=False) or cTranspose (conj=True) of every block;
+    dst is the sector map of the bonds in transposed order."""
+    call("tn_transpose_c128", None, src.h, dst.h, int(bool(conj)), src_ptr, dst_ptr)
+
+
+def plan_check_permute_c128(src: SectorMap, dst: SectorMap, rsp, src_host: np.ndarray) -> tuple[np.ndarray, int]:
+    """The complex permute's tile walk on the CPU (no GPU)."""
+    s = np.ascontiguousarray(src_host, dtype=np.complex128)
+    d = np.full(dst.elem_num, np.nan, dtype=np.complex128)
+    w = C.c_int64()
+    call("tn_plan_check_permute_c128", src.h, dst.h, int_array(rsp), s.ctypes.data, d.ctypes.data, C.byref(w))
+    return d, w.value
+
+
 def contract_sectors(mode, gemms, a_ptr: int, b_ptr: int, c_ptr: int) -> None:
     arr = (capi.SectorGemm * max(1, len(gemms)))(*[capi.SectorGemm(*g) for g in gemms])
     call("tn_contract_sectors", None, _mode(mode), len(gemms), arr, a_ptr, b_ptr, c_ptr)
