@@ -273,6 +273,10 @@ int tn_tensor_sectormap(tn_tensor_t t, tn_smap_t* m);
 int tn_tensor_permute(tn_tensor_t t, int n, const int* new_labels, int in_bond_num);
 /* transpose() (UniTensor.h:576) */
 int tn_tensor_transpose(tn_tensor_t t);
+/* addGate(swaps) (UniTensor.h:665, UniTensorReal.cpp:868-921): swaps holds
+ * nswaps bond pairs (b1, b2); every sub-block whose pairs carry an odd
+ * number of (odd, odd) fermionic parities is negated in place, bit-exact. */
+int tn_tensor_add_gate(tn_tensor_t t, int nswaps, const int* swaps);
 /* combineBond(const std::vector<int>&) (UniTensor.h:619) */
 int tn_tensor_combine_bond(tn_tensor_t t, int n, const int* labels);
 /* contract(Ta, Tb, fast) (UniTensor.h:605; UniTensorTools.cpp:124-244);

@@ -69,7 +69,8 @@ class Network {
   Network() = default;
   void fromtext(const std::string& text, const std::string& fname);
   void construct();
-  void destruct();
+  void destruct(bool undo_gates = true);
+  void addSwap();
   void clean(Node* nd);
   void matching(Node* sbj, Node* tar);
   void branch(Node* sbj, Node* tar);
@@ -84,6 +85,10 @@ class Network {
   std::vector<int> brakets;
   Node* root = nullptr;
   bool load = false;
+  // fermionic swap gates per tensor (Network::addSwap) and whether they are
+  // on the tensor now (Network.cpp:697-717)
+  std::vector<std::vector<_Swap> > swaps_arr;
+  std::vector<char> swapflags;
   void* graph_exec = nullptr;  // cudaGraphExec_t
   void* graph = nullptr;       // cudaGraph_t
   UniTensor graph_out;

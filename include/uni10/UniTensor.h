@@ -23,6 +23,12 @@ struct DevBuf;
 
 namespace uni10 {
 
+// a fermionic swap gate on bonds b1, b2 of a tensor (data-structure/uni10_struct.h:38-41)
+typedef struct {
+  int b1;
+  int b2;
+} _Swap;
+
 // Precision of contract()'s sector GEMMs (process-wide default, per thread).
 // TN_MODE_* values of trim_gb300.h: 0 FP64 (the drop-in), 1 split precision
 // on the tensor cores, 2 BF16 fast, 3 TF32 fast.
@@ -88,6 +94,13 @@ class UniTensor {
   UniTensor& permute(int inBondNum);
   UniTensor& transpose();
   UniTensor& combineBond(const std::vector<int>& combined_labels);
+  // UniTensor::addGate (UniTensorReal.cpp:868-921): negates, in place, every
+  // sub-block whose swapped bond pairs carry an odd number of (odd, odd)
+  // fermionic parities
+  void addGate(const std::vector<_Swap>& swaps);
+  // UniTensor::exSwap (UniTensor.cpp:1237-1268): (bond shared with Tb, bond
+  // not shared) for every such pair of this tensor's bonds
+  std::vector<_Swap> exSwap(const UniTensor& Tb) const;
   friend UniTensor contract(UniTensor& Ta, UniTensor& Tb, bool fast);
   // contraction that leaves both operands untouched (permuted operands are
   // temporaries); Network::launch uses it so its leaves keep their buffers

@@ -19,6 +19,7 @@
 //   save NAME PATH                 UniTensor::save (current binary layout)
 //   svd NAME U1 PRT PRTF PREFIX    Block::svd of one block -> PREFIX.{U,S,VT}
 //   eigh NAME U1 PRT PRTF PREFIX   Block::eigh of one block -> PREFIX.{E,V}
+//   addgate NAME B1 B2 [B1 B2 ...]  UniTensor::addGate with these bond swaps
 //   blocks NAME PATH               writes "U1 PRT PRTF ROWS COLS" per block
 //   time ITERS <command...>        runs the command ITERS times (on copies
 //                                  for in-place ones) and prints seconds/iter
@@ -131,6 +132,15 @@ static void run(const std::vector<std::string>& w) {
       std::fwrite(r[k].getElem(), sizeof(double), r[k].elemNum(), fp);
       std::fclose(fp);
     }
+  } else if (op == "addgate") {
+    std::vector<_Swap> sw;
+    for (size_t i = 2; i + 1 < w.size(); i += 2) {
+      _Swap s;
+      s.b1 = std::atoi(w[i].c_str());
+      s.b2 = std::atoi(w[i + 1].c_str());
+      sw.push_back(s);
+    }
+    get(w[1]).addGate(sw);
   } else if (op == "eigh") {
     Qnum q(parityFType(std::atoi(w[4].c_str())), std::atoi(w[2].c_str()), parityType(std::atoi(w[3].c_str())));
     std::vector<Matrix> r = get(w[1]).getBlock(q).eigh();

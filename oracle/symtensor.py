@@ -17,6 +17,9 @@ It restates, in numpy, the algorithms of the reference (Uni10 v1.0.0) for:
   * otimes                           (UniTensorTools.cpp:246-273)
   * Network fromfile/construct/launch/merge and the greedy planner
                                     (tensor-network/lib/Network.cpp:63-135, 271-506, 602-739)
+  * fermionic swap gates: UniTensor::addGate (UniTensorReal.cpp:868-921),
+    exSwap (UniTensor.cpp:1237-1268), recSwap (tools/lib/uni10_tools.cpp:44-69)
+    and Network::addSwap / launch (Network.cpp:697-717, 923-993)
   * Block::svd via LAPACK dgesvd     (numeric/lapack/lib/uni10_lapack_cpu.cpp:289-313)
   * Block::eigh via LAPACK dsyev     (data-structure/lib/BlockReal.cpp:359-391,
                                      uni10_lapack_cpu.cpp:131-152)
@@ -455,6 +458,86 @@ def permute_elems(src: UniTensor, dst: UniTensor, rsp) -> None:
         dview[...] = -sub if parity else sub
 
 
+# --------------------------------------------------------------------------- swap gates
+def add_gate(t: UniTensor, swaps) -> None:
+    """UniTensor::addGate (UniTensorReal.cpp:868-921): the sign of a sub-block
+    is the XOR over the swaps (b1, b2) of prtF(b1's charge) & prtF(b2's
+    charge); sub-blocks of sign -1 are negated in place."""
+    if not t.bonds:
+        raise ValueError("Adding swap gates to a tensor without bonds(scalar).")
+    sm = t.smap
+    for qin in sm.qidx_enc:
+        qi = _subblock_dims(t, qin)
+        parity = 0
+        for b1, b2 in swaps:
+            parity ^= t.bonds[b1].qnums[qi[b1]].prtf & t.bonds[b2].qnums[qi[b2]].prtf
+        if parity:
+            rin, cin = divmod(qin, sm.cqdim)
+            _, _, bc, boff = sm.blocks[sm.rq2blk[rin]]
+            s0 = boff + sm.rq2off[rin] * bc + sm.cq2off[cin]
+            v = np.lib.stride_tricks.as_strided(t.elem[s0:], shape=(sm.rq2dim[rin], sm.cq2dim[cin]), strides=(bc * 8, 8))
+            v[...] = -v
+
+
+def ex_swap(ta: UniTensor, tb: UniTensor):
+    """UniTensor::exSwap (UniTensor.cpp:1237-1268): (bond of ta whose label is
+    in tb, bond of ta whose label is not) for every such pair."""
+    inter = [a for a, l in enumerate(ta.labels) if l in tb.labels]
+    left = [a for a, l in enumerate(ta.labels) if l not in tb.labels]
+    return [(i, j) for i in inter for j in left]
+
+
+def rec_swap(order):
+    """recSwap(ord) (tools/lib/uni10_tools.cpp:44-69, ordF = identity): the
+    adjacent exchanges of a bubble sort of ord, as (smaller, larger) values."""
+    ord_ = list(order)
+    out = []
+    n = len(ord_)
+    for i in range(n - 1):
+        for j in range(n - i - 1):
+            if ord_[j] > ord_[j + 1]:
+                out.append((ord_[j + 1], ord_[j]))
+                ord_[j], ord_[j + 1] = ord_[j + 1], ord_[j]
+    return out
+
+
+def network_swaps(root, tensors):
+    """Network::addSwap (Network.cpp:923-993): the contraction order of the
+    leaves (pre-order walk of the tree), its bubble-sort exchanges, each
+    giving exSwap(T_b1, T_b2) to tensor b1; per tensor the pairs are kept when
+    they occur an odd number of times, ordered by min * bondNum + max."""
+    con = []
+
+    def walk(nd):
+        if nd is None or len(con) == len(tensors):
+            return
+        if nd.t is not None:
+            con.append(nd.t)
+        walk(nd.left)
+        walk(nd.right)
+
+    walk(root)
+    arr = [[] for _ in tensors]
+    for b1, b2 in rec_swap(con):
+        arr[b1] += ex_swap(tensors[b1], tensors[b2])
+    out = []
+    for t, sw in zip(tensors, arr):
+        nb = len(t.bonds)
+        recs = {}
+        for a, b in sw:
+            h = min(a, b) * nb + max(a, b)
+            recs[h] = not recs.get(h, False)
+        out.append([(h // nb, h % nb) for h in sorted(recs) if recs[h]])
+    return out
+
+
+def is_fermionic(tensors) -> bool:
+    """Whether any bond carries an odd fermionic parity (the reference keys
+    the swap gates on Qnum::isFermionic, set by any PRTF_ODD charge; without
+    one every gate sign is +1)."""
+    return any(q.prtf for t in tensors for b in t.bonds for q in b.qnums)
+
+
 # --------------------------------------------------------------------------- contract
 def contract(ta: UniTensor, tb: UniTensor, fast: bool = False, gemm=None) -> UniTensor:
     """contract(rflag, Ta, Tb, fast) -- UniTensorTools.cpp:124-244.
@@ -621,6 +704,8 @@ class Network:
         self.names, self.label_arr, self.rnums, self.order, self.brakets = [], [], [], [], []
         self._parse(text)
         self.tensors: list[UniTensor | None] = [None] * (len(self.names) - 1)
+        self.swapflags = [False] * (len(self.names) - 1)
+        self.swaps = None  # per tensor, from the first construct (Network::addSwap)
 
     def _parse(self, text: str) -> None:  # Network.cpp:271-427
         ord_names = []
@@ -685,6 +770,7 @@ class Network:
         c.set_label(self.label_arr[idx])
         c.name = self.names[idx]
         self.tensors[idx] = c
+        self.swapflags[idx] = False  # Network.cpp:524-528
 
     # -- construct: Network.cpp:428-506 and the greedy planner :602-670
     def construct(self):
@@ -774,6 +860,13 @@ class Network:
 
     def launch(self, gemm=None) -> UniTensor:  # Network.cpp:697-717
         root = self.construct()
+        if self.swaps is None:
+            self.swaps = network_swaps(root, self.tensors) if is_fermionic(self.tensors) else [[] for _ in self.tensors]
+        for t, sw in enumerate(self.swaps):
+            if not self.swapflags[t]:
+                if sw:
+                    add_gate(self.tensors[t], sw)
+                self.swapflags[t] = True
         out = self._merge(root, gemm)
         tout = self.label_arr[-1]
         if len(tout) > 1:

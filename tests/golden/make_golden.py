@@ -8,7 +8,8 @@ Run here (where the reference sources exist and oracle/_ref is built):
 It writes:
   cases.json / arrays.npz  reference outputs (UniTensor::permute, transpose,
                            contract, combineBond, Network::launch, Block::svd,
-                           Block::eigh)
+                           Block::eigh, UniTensor::addGate, fermionic
+                           Network::launch with swap gates)
                            for seeded inputs: workload 1 at full size, the
                            iTEBD network at full size (chi=512), reduced-size
                            versions of workloads 3-5, and randomized
@@ -77,6 +78,12 @@ def rand_bond(rng, btype, sym):
         nq = int(rng.integers(1, 4))
         pick = sorted(rng.choice(len(pool), size=nq, replace=False))
         return (btype, [(pool[k][0], 0, pool[k][1], int(rng.integers(1, 4))) for k in pick])
+    if sym == "fermion_rich":  # 2-4 charges, at least one of odd fermionic parity
+        pool = [(-1, 0), (-1, 1), (0, 0), (0, 1), (1, 0), (1, 1)]
+        while True:
+            pick = sorted(rng.choice(len(pool), size=int(rng.integers(2, 5)), replace=False))
+            if any(pool[k][1] for k in pick):
+                return (btype, [(pool[k][0], 0, pool[k][1], int(rng.integers(1, 4))) for k in pick])
     return (btype, [(0, 0, 0, int(rng.integers(1, 5)))])
 
 
@@ -386,6 +393,79 @@ def eigh_cases(w: Writer, rng):
                "blocks": [[u, d] for u, d in runs]}, arrays)
 
 
+FNETS = [
+    # (net text, [(name, [(label, type)])]): a label's second tensor gets Bond::change of the first's bond
+    ("A: 1 2; 3\nB: 3 4; 5\nC: 5 1; 6\nTOUT: 2 4; 6\nORDER: ((B C) A)\n",
+     [("A", [(1, 1), (2, 1), (3, -1)]), ("B", [(3, 1), (4, 1), (5, -1)]), ("C", [(5, 1), (1, 1), (6, -1)])]),
+    ("A: 1 2; 3\nB: 3 4; 5\nC: 5 1; 6\nTOUT: 2 4; 6\n",
+     [("A", [(1, 1), (2, 1), (3, -1)]), ("B", [(3, 1), (4, 1), (5, -1)]), ("C", [(5, 1), (1, 1), (6, -1)])]),
+    ("A: 1; 2 3\nB: 2 4; 5\nC: 3 5; 6\nD: 6; 1 7\nTOUT: 4; 7\nORDER: ((C D) (B A))\n",
+     [("A", [(1, 1), (2, -1), (3, -1)]), ("B", [(2, 1), (4, 1), (5, -1)]), ("C", [(3, 1), (5, 1), (6, -1)]),
+      ("D", [(6, 1), (1, -1), (7, -1)])]),
+]
+
+
+def fermion_gates(w: Writer, rng, ngate: int, nnet: int):
+    """UniTensor::addGate on random fermionic tensors, and fermionic networks
+    whose contraction order differs from the file order, so Network::launch
+    puts swap gates (addSwap, Network.cpp:944-993) on the tensors."""
+    made = 0
+    while made < ngate:
+        rank = int(rng.integers(2, 6))
+        bonds = rand_tensor(rng, rank, "fermion")
+        if all(len(runs) == 1 for _, runs in bonds):
+            continue
+        pairs = []
+        for _ in range(int(rng.integers(1, 5))):
+            b1, b2 = (int(v) for v in rng.choice(rank, size=2, replace=False))
+            pairs.append((b1, b2))
+        labels = list(range(10, 10 + rank))
+        el = rng.uniform(-1, 1, wl.elem_count(bonds))
+        S = refrun.RefSession()
+        S.tensor("T", bonds, labels, el)
+        S.cmd("addgate T " + " ".join(f"{a} {b}" for a, b in pairs))
+        S.save("T", "G")
+        o = S.run()
+        w.add({"id": f"fgate{made}", "kind": "addgate", "T": tensor_meta(bonds, labels), "swaps": pairs,
+               "out": out_meta(o["G"])}, {"T": el, "G": o["G"]["elem"]})
+        made += 1
+    made = 0
+    tries = 0
+    while made < nnet:
+        tries += 1
+        net, spec = FNETS[made % len(FNETS)]
+        first = {}
+        tens = []
+        for name, legs in spec:
+            bonds = []
+            for lab, t in legs:
+                if lab not in first:
+                    first[lab] = rand_bond(rng, t, "fermion_rich")
+                    bonds.append(first[lab])
+                else:
+                    bonds.append(wl.change(first[lab], t))
+            tens.append((name, bonds, [lab for lab, _ in legs]))
+        if any(wl.elem_count(b) == 0 for _, b, _ in tens):
+            continue
+        S = refrun.RefSession()
+        els = {}
+        for name, bonds, labels in tens:
+            els[name] = rng.uniform(-1, 1, wl.elem_count(bonds))
+            S.tensor(name, bonds, labels, els[name])
+        S.network("R", net, {name: name for name, _, _ in tens})
+        S.save("R")
+        try:
+            o = S.run()
+        except RuntimeError:
+            continue
+        if "R" not in o or o["R"]["elem"].size == 0 or not np.any(o["R"]["elem"]):
+            continue  # no sector survives the contraction: the gates could not show
+        w.add({"id": f"fnet{made}", "kind": "fnet", "net": net,
+               "tensors": {name: tensor_meta(bonds, labels) for name, bonds, labels in tens}, "R": out_meta(o["R"])},
+              {**els, "R": o["R"]["elem"]})
+        made += 1
+
+
 def legacy(refroot: str):
     ex = os.path.join(refroot, "Swig", "examples")
     out = {}
@@ -419,6 +499,7 @@ def main():
     # fermionic signs of permute / contract, with a stream of their own
     fermion_cases(w, np.random.default_rng(777), 16, 8)
     eigh_cases(w, np.random.default_rng(4242))
+    fermion_gates(w, np.random.default_rng(909), 12, 15)
     with open(os.path.join(HERE, "cases.json"), "w") as f:
         json.dump(w.cases, f, indent=0)
     np.savez_compressed(os.path.join(HERE, "arrays.npz"), **w.arrays)

@@ -101,6 +101,61 @@ def test_complex_dense_permutes_bit_exact(tu, perm, rn):
     assert torch.equal(y, x.view([chi] * 6).permute(*perm).reshape(-1))
 
 
+FGATE = [c for c in G.cases().values() if c["kind"] == "addgate"]
+FNET = [c for c in G.cases().values() if c["kind"] == "fnet"]
+
+
+@pytest.mark.parametrize("case", FGATE, ids=[c["id"] for c in FGATE])
+def test_add_gate_bit_exact(tu, case):
+    t = tu.UniTensor(G.bonds_of(case["T"]), case["T"]["labels"], G.arr(case["id"], "T"))
+    t.add_gate([tuple(p) for p in case["swaps"]])
+    assert np.array_equal(t.get_elem(), G.arr(case["id"], "G"))
+
+
+def _fnet(tu, case):
+    net = tu.Network(case["net"])
+    ts = {}
+    for name, meta in case["tensors"].items():
+        ts[name] = tu.UniTensor(G.bonds_of(meta), meta["labels"], G.arr(case["id"], name))
+        net.put_tensor(name, ts[name])
+    return net, ts
+
+
+@pytest.mark.parametrize("case", FNET, ids=[c["id"] for c in FNET])
+def test_fermionic_network_swap_gates(tu, case):
+    """Network::launch on fermionic tensors puts the swap gates of its
+    contraction order on the tensors once (Network.cpp:697-717, 944-993):
+    the result matches the reference, a second launch does not apply them
+    again, and a tensor put anew gets them again."""
+    ref = G.arr(case["id"], "R")
+    net, ts = _fnet(tu, case)
+    for _ in range(2):
+        r = net.launch("fp64")
+        assert [[b[0], [list(x) for x in b[1]]] for b in r.bonds()] == case["R"]["bonds"]
+        assert r.labels() == case["R"]["labels"]
+        assert rel(r.get_elem(), ref) <= FP64_TOL
+    for name in case["tensors"]:
+        net.put_tensor(name, ts[name])
+        assert rel(net.launch("fp64").get_elem(), ref) <= FP64_TOL
+
+
+def test_fermionic_network_with_gates_refuses_capture(tu):
+    from trim_gb300 import capi
+
+    for case in FNET:
+        net, _ = _fnet(tu, case)
+        ref = net.launch("fp64").get_elem()
+        try:
+            net.capture("fp64")
+        except capi.TnError as e:
+            assert e.code == 7  # TN_ERR_UNSUPPORTED
+            assert "swap gates" in str(e)
+            return
+        net.replay()  # no gate on any tensor: capture is allowed
+        assert rel(net.output().get_elem(), ref) <= FP64_TOL
+    pytest.fail("no fixture carries a swap gate")
+
+
 @pytest.mark.parametrize("case", CON, ids=[c["id"] for c in CON])
 def test_contract_fp64(tu, case):
     a = tu.UniTensor(G.bonds_of(case["A"]), case["A"]["labels"], G.arr(case["id"], "A"))

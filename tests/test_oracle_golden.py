@@ -194,3 +194,41 @@ def test_eigh_oracle_matches_reference(case_id):
         if not np.array_equal(a, a.T):
             e_up = np.linalg.eigvalsh(np.triu(a) + np.triu(a, 1).T)
             assert np.max(np.abs(e_up - e_ref)) > 1e-6
+
+
+FGATE = [c for c in G.cases().values() if c["kind"] == "addgate"]
+FNET = [c for c in G.cases().values() if c["kind"] == "fnet"]
+
+
+@pytest.mark.parametrize("case", FGATE, ids=[c["id"] for c in FGATE])
+def test_add_gate_bit_exact(case):
+    t = st.UniTensor(to_bonds(G.bonds_of(case["T"])), case["T"]["labels"], G.arr(case["id"], "T").copy())
+    st.add_gate(t, [tuple(p) for p in case["swaps"]])
+    assert np.array_equal(t.elem, G.arr(case["id"], "G"))
+
+
+@pytest.mark.parametrize("case", FNET, ids=[c["id"] for c in FNET])
+def test_fermionic_network_swap_gates(case):
+    """Network::launch with swap gates on fermionic tensors: the restated
+    addSwap/addGate reproduce the reference within 1e-13 (identical BLAS)."""
+    net = st.Network(text=case["net"])
+    for name, meta in case["tensors"].items():
+        net.put_tensor(name, st.UniTensor(to_bonds(G.bonds_of(meta)), meta["labels"], G.arr(case["id"], name)))
+    r = net.launch()
+    ref = G.arr(case["id"], "R")
+    assert bonds_meta(r) == case["R"]["bonds"] and r.labels == case["R"]["labels"]
+    assert np.linalg.norm(r.elem - ref) <= 1e-13 * max(np.linalg.norm(ref), 1e-300)
+
+
+def test_fermionic_networks_depend_on_the_gates():
+    """Dropping the swap gates changes the result of some fixtures, so the
+    fixtures pin the gates."""
+    changed = 0
+    for case in FNET:
+        net = st.Network(text=case["net"])
+        for name, meta in case["tensors"].items():
+            net.put_tensor(name, st.UniTensor(to_bonds(G.bonds_of(meta)), meta["labels"], G.arr(case["id"], name)))
+        net.swaps = [[] for _ in net.tensors]
+        r = net.launch()
+        changed += not np.allclose(r.elem, G.arr(case["id"], "R"), rtol=1e-12, atol=1e-14)
+    assert changed >= 3

@@ -551,6 +551,17 @@ int tn_tensor_permute(tn_tensor_t t, int n, const int* new_labels, int in_bond_n
   });
 }
 
+int tn_tensor_add_gate(tn_tensor_t t, int nswaps, const int* swaps) {
+  return guard([&] {
+    need(t, "t");
+    if (nswaps < 0) tn::fail(TN_ERR_ARG, "negative swap count");
+    if (nswaps) need(swaps, "swaps");
+    std::vector<uni10::_Swap> sw;
+    for (int i = 0; i < nswaps; i++) sw.push_back(uni10::_Swap{swaps[2 * i], swaps[2 * i + 1]});
+    t->t.addGate(sw);
+  });
+}
+
 int tn_tensor_transpose(tn_tensor_t t) {
   return guard([&] {
     need(t, "tensor");

@@ -323,6 +323,14 @@ PermPlanP host_plan(std::vector<PermSub> subs, int64_t elem_num, int esz = 8);  
 int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double* dst);
 // src / dst hold plan.elem_num elements of plan.esz bytes
 void run_permute(Ctx& ctx, const PermPlan& plan, const void* src, void* dst);
+// UniTensor::addGate (UniTensorReal.cpp:868-921): sub-blocks whose swapped
+// bond pairs carry an odd number of (odd, odd) fermionic parities are negated
+// in place; elem holds elem_num elements of esz (8 or 16) bytes.  Returns
+// the number of sub-blocks negated.
+int64_t run_add_gate(Ctx& ctx, const SectorMap& m, const std::vector<std::pair<int, int>>& swaps, void* elem,
+                     int esz = 8);
+// the (offset, rows, cols, ld) entries in doubles that run_add_gate negates
+std::vector<int64_t> add_gate_table(const SectorMap& m, const std::vector<std::pair<int, int>>& swaps, int esz);
 
 uint64_t hash_list(const std::vector<tn_sector_gemm>& list, int tag);
 // sector GEMMs: C_i = A_i . B_i for every item, all in one grouped launch
@@ -363,6 +371,7 @@ void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const 
                       cudaStream_t s);
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
                           cudaStream_t s);
+void launch_negate_blocks(const int64_t* tab, int n, double* elem, cudaStream_t s);
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s);
 void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
                     int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,

@@ -451,6 +451,45 @@ static PermPlanP finish_plan(Ctx& ctx, const std::string& key, std::vector<PermS
   return plan;
 }
 
+std::vector<int64_t> add_gate_table(const SectorMap& m, const std::vector<std::pair<int, int>>& swaps, int esz) {
+  const int n = (int)m.bonds.size();
+  if (esz != 8 && esz != 16) fail(TN_ERR_ARG, "addGate: element size must be 8 or 16 bytes");
+  for (const auto& sw : swaps)
+    if (sw.first < 0 || sw.first >= n || sw.second < 0 || sw.second >= n)
+      fail(TN_ERR_ARG, "addGate: swap names a bond the tensor does not have");
+  const int64_t es = esz / 8;
+  std::vector<int64_t> tab;
+  std::vector<int> qin(n);
+  for (int64_t qidx : m.qidx_enc) {
+    int64_t tmp = qidx;
+    for (int b = n - 1; b >= 0; b--) {
+      const int64_t qd = (int64_t)m.bonds[b].q.size();
+      qin[b] = (int)(tmp % qd);
+      tmp /= qd;
+    }
+    int parity = 0;
+    for (const auto& sw : swaps) parity ^= m.bonds[sw.first].q[qin[sw.first]].prtf & m.bonds[sw.second].q[qin[sw.second]].prtf;
+    if (!parity) continue;
+    const int64_t r = qidx / m.cqdim, c = qidx % m.cqdim;
+    const auto& B = m.blocks[m.rq2blk[r]];
+    tab.insert(tab.end(), {(B.off + m.rq2off[r] * B.cols + m.cq2off[c]) * es, m.rq2dim[r], m.cq2dim[c] * es, B.cols * es});
+  }
+  return tab;
+}
+
+int64_t run_add_gate(Ctx& ctx, const SectorMap& m, const std::vector<std::pair<int, int>>& swaps, void* elem, int esz) {
+  if (m.bonds.empty()) fail(TN_ERR_ARG, "Adding swap gates to a tensor without bonds(scalar).");
+  const std::vector<int64_t> tab = add_gate_table(m, swaps, esz);
+  const int64_t n = (int64_t)tab.size() / 4;
+  if (n == 0) return 0;
+  if (n > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "addGate: too many sub-blocks");
+  DevBuf d(tab.size() * sizeof(int64_t), ctx);
+  TN_CUDA(cudaMemcpyAsync(d.ptr, tab.data(), tab.size() * sizeof(int64_t), cudaMemcpyHostToDevice, ctx.stream));
+  launch_negate_blocks((const int64_t*)d.ptr, (int)n, (double*)elem, ctx.stream);
+  ctx.launched();
+  return n;
+}
+
 void run_permute(Ctx& ctx, const PermPlan& plan, const void* src, void* dst) {
   if (plan.ntiles == 0) return;
   // persistent: two resident CTAs per SM (100 KB of staging shared memory each)

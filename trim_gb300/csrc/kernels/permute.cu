@@ -354,6 +354,19 @@ __global__ void __launch_bounds__(kThreads, 2) permute_kernel(const PermSub* __r
   cp_async_wait<0>();
 }
 
+// Negation of listed sub-blocks in place (UniTensor::addGate's sign -1,
+// UniTensorReal.cpp:868-921): one CTA per entry (offset, rows, cols, ld),
+// the sign bit flipped as an integer XOR (bit-identical to a product by -1).
+__global__ void __launch_bounds__(256) negate_blocks_kernel(const int64_t* __restrict__ tab, double* __restrict__ p) {
+  const int64_t* e = tab + 4 * (int64_t)blockIdx.x;
+  const int64_t off = e[0], rows = e[1], cols = e[2], ld = e[3];
+  for (int64_t i = threadIdx.x; i < rows * cols; i += blockDim.x) {
+    const int64_t r = i / cols, c = i - r * cols;
+    double* q = p + off + r * ld + c;
+    *q = flip_sign(*q, 0x8000000000000000ull);
+  }
+}
+
 __global__ void fill_kernel(double* __restrict__ p, int64_t n, double v) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -425,6 +438,12 @@ void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int n
                               conj ? 0x8000000000000000ull : 0ull, grid, s);
   else
     fail(TN_ERR_ARG, "permute: element size must be 8 or 16 bytes");
+}
+
+void launch_negate_blocks(const int64_t* tab, int n, double* elem, cudaStream_t s) {
+  if (n <= 0) return;
+  negate_blocks_kernel<<<n, 256, 0, s>>>(tab, elem);
+  TN_CUDA(cudaGetLastError());
 }
 
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s) {

@@ -245,7 +245,8 @@ Network Network::fromText(const std::string& text) {
 Network::Network(Network&& o) noexcept
     : names(std::move(o.names)), name2pos(std::move(o.name2pos)), label_arr(std::move(o.label_arr)),
       Rnums(std::move(o.Rnums)), leafs(std::move(o.leafs)), tensors(std::move(o.tensors)), order(std::move(o.order)),
-      brakets(std::move(o.brakets)), root(o.root), load(o.load), graph_exec(o.graph_exec), graph(o.graph),
+      brakets(std::move(o.brakets)), root(o.root), load(o.load), swaps_arr(std::move(o.swaps_arr)),
+      swapflags(std::move(o.swapflags)), graph_exec(o.graph_exec), graph(o.graph),
       graph_out(std::move(o.graph_out)), graph_sigs(std::move(o.graph_sigs)) {
   o.root = nullptr;
   o.load = false;
@@ -255,7 +256,7 @@ Network::Network(Network&& o) noexcept
 
 Network::~Network() {
   drop_graph();
-  if (load) destruct();
+  if (load) destruct(false);  // the tensors die with the network: no gate to undo
   for (Node* l : leafs) delete l;
   for (UniTensor* t : tensors) delete t;
 }
@@ -271,6 +272,7 @@ void Network::putTensor(size_t idx, const UniTensor* UniT, bool force) {
     *(tensors[idx]) = *UniT;
     tensors[idx]->setLabel(label_arr[idx]);
     tensors[idx]->setName(names[idx]);
+    if (idx < swapflags.size()) swapflags[idx] = 0;  // the new tensor has no gate yet
   } else {
     UniTensor* t = new UniTensor(*UniT);
     t->setName(names[idx]);
@@ -351,7 +353,64 @@ void Network::construct() {
   } else {
     throw std::runtime_error("Error when constructing the network. The bond number of the resulting tensor is different from the bond number of 'TOUT'");
   }
+  addSwap();
   load = true;
+}
+
+// Network::addSwap (Network.cpp:923-993): the leaves' contraction order (a
+// pre-order walk of the tree), the adjacent exchanges of its bubble sort
+// (recSwap, tools/lib/uni10_tools.cpp:44-69), exSwap(T_b1, T_b2) for each
+// exchange given to tensor b1, and per tensor the pairs that occur an odd
+// number of times, in order of min * bondNum + max.  Only with fermionic
+// charges: otherwise every gate sign is +1 (the reference keys this on
+// Qnum::isFermionic, set by any PRTF_ODD charge).
+void Network::addSwap() {
+  const size_t n = tensors.size();
+  swaps_arr.assign(n, std::vector<_Swap>());
+  if (swapflags.size() != n) swapflags.assign(n, 0);
+  bool odd = false;
+  for (UniTensor* t : tensors)
+    if (t && t->sectorMap())
+      for (const auto& b : t->sectorMap()->bonds)
+        for (const auto& q : b.q) odd |= q.prtf != 0;
+  if (!odd) return;
+  std::vector<int> con;
+  std::function<void(Node*)> walk = [&](Node* nd) {
+    if (nd == nullptr || con.size() == n) return;
+    if (nd->T)
+      for (size_t i = 0; i < n; i++)
+        if (tensors[i] == nd->T) {
+          con.push_back((int)i);
+          break;
+        }
+    walk(nd->left);
+    walk(nd->right);
+  };
+  walk(root);
+  if (con.size() != n) throw std::runtime_error("Fatal error(code = N3). Please contact the developer of the uni10 library.");
+  for (size_t i = 0; i + 1 < n; i++)
+    for (size_t j = 0; j + 1 < n - i; j++)
+      if (con[j] > con[j + 1]) {
+        const int b1 = con[j + 1], b2 = con[j];
+        std::swap(con[j], con[j + 1]);
+        std::vector<_Swap> sw = tensors[b1]->exSwap(*tensors[b2]);
+        swaps_arr[b1].insert(swaps_arr[b1].end(), sw.begin(), sw.end());
+      }
+  for (size_t t = 0; t < n; t++) {
+    const int nb = (int)tensors[t]->bondNum();
+    std::map<int, bool> recs;
+    for (const _Swap& s : swaps_arr[t]) {
+      const int h = std::min(s.b1, s.b2) * nb + std::max(s.b1, s.b2);
+      auto it = recs.find(h);
+      if (it != recs.end())
+        it->second = !it->second;
+      else
+        recs[h] = true;
+    }
+    swaps_arr[t].clear();
+    for (const auto& kv : recs)
+      if (kv.second) swaps_arr[t].push_back(_Swap{kv.first / nb, kv.first % nb});
+  }
 }
 
 void Network::branch(Node* sbj, Node* tar) {
@@ -423,9 +482,15 @@ void Network::clean(Node* nd) {
   delete nd;
 }
 
-void Network::destruct() {
+void Network::destruct(bool undo_gates) {
   clean(root);
   root = nullptr;
+  // the gates come off again (a second sign flip), as Network.cpp:684-692 does
+  for (size_t t = 0; t < swaps_arr.size(); t++) {
+    if (undo_gates && t < swapflags.size() && swapflags[t] && !swaps_arr[t].empty()) tensors[t]->addGate(swaps_arr[t]);
+    if (t < swapflags.size()) swapflags[t] = 0;
+    swaps_arr[t].clear();
+  }
   for (Node* l : leafs)
     if (l) {
       l->parent = l->left = l->right = nullptr;
@@ -455,6 +520,11 @@ UniTensor Network::merge(Node* nd) {
 
 UniTensor Network::launch(const std::string& _name) {
   if (!load) construct();
+  for (size_t t = 0; t < swaps_arr.size(); t++)
+    if (!swapflags[t]) {
+      if (!swaps_arr[t].empty()) tensors[t]->addGate(swaps_arr[t]);
+      swapflags[t] = 1;
+    }
   UniTensor UniT = merge(root);
   size_t idx = label_arr.size() - 1;
   if (!label_arr.empty() && label_arr[idx].size() > 1) UniT.permute(label_arr[idx], Rnums[idx]);
@@ -474,6 +544,10 @@ void Network::drop_graph() {
 void Network::capture() {
   drop_graph();
   UniTensor warm = launch();  // plans, workspace and tree in place
+  // swap gates go on a tensor once, at the launch after it is put; a replay on
+  // new elements would skip them
+  for (const auto& sw : swaps_arr)
+    if (!sw.empty()) tn::fail(TN_ERR_UNSUPPORTED, "capture: a network with fermionic swap gates cannot be replayed");
   graph_out = warm;           // persistent output buffer, allocated outside the graph
   graph_sigs.clear();
   for (UniTensor* t : tensors) graph_sigs.push_back(t->sectorMap() ? t->sectorMap()->key : std::string());

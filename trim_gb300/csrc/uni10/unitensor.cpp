@@ -5,6 +5,7 @@
 // UniTensorReal.cpp, UniTensorTools.cpp) including in-place permutes of
 // contract()'s operands.
 #include <cstdio>
+#include <algorithm>
 #include <cstring>
 #include <sstream>
 #include <stdexcept>
@@ -839,6 +840,25 @@ std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, c
 }
 
 // ---------------------------------------------------------------- SVD + truncation
+void UniTensor::addGate(const std::vector<_Swap>& swaps) {
+  if (!(status & HAVEBOND)) throw std::runtime_error("Adding swap gates to a tensor without bonds(scalar).");
+  if (!(status & HAVEELEM)) throw std::runtime_error("Cannot add swap gates to a tensor before setting its elements.");
+  std::vector<std::pair<int, int>> sw;
+  for (const _Swap& s : swaps) sw.emplace_back(s.b1, s.b2);
+  tn::run_add_gate(C(), *smap, sw, dptr(elem));
+}
+
+std::vector<_Swap> UniTensor::exSwap(const UniTensor& Tb) const {
+  std::vector<_Swap> swaps;
+  if (!(status & Tb.status & HAVEBOND)) return swaps;
+  std::vector<int> inter, left;
+  for (size_t a = 0; a < labels.size(); a++)
+    (std::find(Tb.labels.begin(), Tb.labels.end(), labels[a]) != Tb.labels.end() ? inter : left).push_back((int)a);
+  for (int i : inter)
+    for (int j : left) swaps.push_back(_Swap{i, j});
+  return swaps;
+}
+
 // The U(1) form of the iTEBD update (examples/iTEBD.cpp:153-171): Block::svd of
 // every block (BlockReal.cpp:226-250), the chi largest singular values over
 // all blocks kept (Matrix::resize, MatrixReal.cpp:289-360) and divided by

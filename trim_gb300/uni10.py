@@ -256,6 +256,13 @@ class UniTensor:
         call("tn_tensor_permute", self.h, len(new_labels), int_array(new_labels), in_bond_num)
         return self
 
+    def add_gate(self, swaps) -> "UniTensor":
+        """UniTensor::addGate: negate the sub-blocks whose swapped bond pairs
+        carry an odd number of (odd, odd) fermionic parities (in place)."""
+        flat = [int(v) for p in swaps for v in p]
+        call("tn_tensor_add_gate", self.h, len(swaps), int_array(flat) if flat else None)
+        return self
+
     def transpose(self) -> "UniTensor":
         call("tn_tensor_transpose", self.h)
         return self
