@@ -141,6 +141,10 @@ int tn_plan_check_permute(tn_smap_t src, tn_smap_t dst, const int* rsp, const do
 int tn_permute_c128(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, const int* rsp, const void* src_elem,
                     void* dst_elem);
 int tn_transpose_c128(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, int conj, const void* src_elem, void* dst_elem);
+/* addGate(cflag, swaps) (UniTensorComplex.cpp:927-980) on a complex element
+ * buffer of the sector map m: swaps holds nswaps bond pairs (b1, b2); the
+ * sub-blocks of sign -1 are negated in place (both parts), bit-exact. */
+int tn_add_gate_c128(tn_ctx_t ctx, tn_smap_t m, int nswaps, const int* swaps, void* elem);
 /* tn_plan_check_permute for 16-byte elements (host arrays of 2 * elem_num doubles) */
 int tn_plan_check_permute_c128(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host,
                                double* dst_host, int64_t* written);

@@ -112,6 +112,20 @@ def test_add_gate_bit_exact(tu, case):
     assert np.array_equal(t.get_elem(), G.arr(case["id"], "G"))
 
 
+@pytest.mark.parametrize("case", FGATE, ids=[c["id"] for c in FGATE])
+def test_add_gate_c128_bit_exact(tu, case):
+    """Complex addGate (UniTensorComplex.cpp:927-980): re = T, im = -2 T
+    give (G, -2 G) bit for bit."""
+    import torch
+
+    x = G.arr(case["id"], "T")
+    z = torch.from_numpy(x + 1j * (-2.0 * x)).cuda()
+    tu.add_gate_c128(tu.SectorMap(G.bonds_of(case["T"])), [tuple(p) for p in case["swaps"]], z.data_ptr())
+    tu.sync()
+    g, got = G.arr(case["id"], "G"), z.cpu().numpy()
+    assert np.array_equal(got.real, g) and np.array_equal(got.imag, -2.0 * g)
+
+
 def _fnet(tu, case):
     net = tu.Network(case["net"])
     ts = {}

@@ -73,6 +73,7 @@ _PROTOS = {
     "tn_plan_check_permute": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
     "tn_permute_c128": (_I, [_P, _P, _P, _IP, _DP, _DP]),
     "tn_tensor_add_gate": (_I, [_P, _I, _IP]),
+    "tn_add_gate_c128": (_I, [_P, _P, _I, _IP, _DP]),
     "tn_transpose_c128": (_I, [_P, _P, _P, _I, _DP, _DP]),
     "tn_plan_check_permute_c128": (_I, [_P, _P, _IP, _DP, _DP, _I64P]),
     "tn_plan_check_views": (_I, [_P, _P, _IP, _DP, _DP, _IP]),

@@ -278,6 +278,22 @@ int tn_transpose_c128(tn_ctx_t ctx, tn_smap_t src, tn_smap_t dst, int conj, cons
   });
 }
 
+int tn_add_gate_c128(tn_ctx_t ctx, tn_smap_t m, int nswaps, const int* swaps, void* elem) {
+  return guard([&] {
+    need(m, "m");
+    if (nswaps < 0) tn::fail(TN_ERR_ARG, "negative swap count");
+    if (nswaps) need(swaps, "swaps");
+    tn::Ctx* c = tn::as_ctx(ctx);
+    std::vector<std::pair<int, int>> sw;
+    for (int i = 0; i < nswaps; i++) sw.emplace_back(swaps[2 * i], swaps[2 * i + 1]);
+    if (m->m->elem_num > 0) {
+      need(elem, "elem");
+      if ((uintptr_t)elem & 15) tn::fail(TN_ERR_ARG, "complex buffers must be 16-byte aligned");
+    }
+    tn::run_add_gate(*c, *m->m, sw, elem, 16);
+  });
+}
+
 int tn_plan_check_permute_c128(tn_smap_t src, tn_smap_t dst, const int* rsp, const double* src_host,
                                double* dst_host, int64_t* written) {
   return guard([&] {

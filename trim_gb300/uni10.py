@@ -77,6 +77,12 @@ def transpose_device_c128(src: SectorMap, dst: SectorMap, conj: bool, src_ptr: i
     call("tn_transpose_c128", None, src.h, dst.h, int(bool(conj)), src_ptr, dst_ptr)
 
 
+def add_gate_c128(m: SectorMap, swaps, elem_ptr: int) -> None:
+    """Complex addGate on a device buffer of 16-byte elements (in place)."""
+    flat = [int(v) for p in swaps for v in p]
+    call("tn_add_gate_c128", None, m.h, len(swaps), int_array(flat) if flat else None, elem_ptr)
+
+
 def plan_check_permute_c128(src: SectorMap, dst: SectorMap, rsp, src_host: np.ndarray) -> tuple[np.ndarray, int]:
     """The complex permute's tile walk on the CPU (no GPU)."""
     s = np.ascontiguousarray(src_host, dtype=np.complex128)
