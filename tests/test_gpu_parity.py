@@ -23,6 +23,7 @@ def tu():
         pytest.skip("no CUDA device")
     from trim_gb300 import uni10 as tu
 
+    tu.set_stream(torch.cuda.current_stream().cuda_stream)  # ordered with torch's work on the tensors
     return tu
 
 
@@ -67,6 +68,7 @@ def test_complex_permute_transpose_ctranspose_bit_exact(tu, case):
     x = G.arr(case["id"], "T")
     z = torch.from_numpy(x + 1j * (-2.0 * x)).cuda()
     y = torch.full_like(z, complex(np.nan, np.nan))
+    torch.cuda.synchronize()  # the library runs on its own stream
     src, dst = tu.SectorMap(bonds), tu.SectorMap(out)
     tu.permute_device_c128(src, dst, rsp, z.data_ptr(), y.data_ptr())
     tu.sync()
@@ -76,6 +78,7 @@ def test_complex_permute_transpose_ctranspose_bit_exact(tu, case):
     tmap = tu.SectorMap(G.bonds_of(case["out_transpose"]))
     for conj in (False, True):
         w = torch.full_like(z, complex(np.nan, np.nan))
+        torch.cuda.synchronize()
         tu.transpose_device_c128(dst, tmap, conj, y.data_ptr(), w.data_ptr())
         tu.sync()
         got = w.cpu().numpy()
@@ -96,6 +99,7 @@ def test_complex_dense_permutes_bit_exact(tu, perm, rn):
     x = torch.randn(chi ** 6, dtype=torch.complex128, device="cuda", generator=g)
     y = torch.empty_like(x)
     out = [wl.change(bonds[perm[b]], 1 if b < rn else -1) for b in range(6)]
+    torch.cuda.synchronize()  # the library runs on its own stream
     tu.permute_device_c128(tu.SectorMap(bonds), tu.SectorMap(out), list(perm), x.data_ptr(), y.data_ptr())
     tu.sync()
     assert torch.equal(y, x.view([chi] * 6).permute(*perm).reshape(-1))
@@ -120,6 +124,7 @@ def test_add_gate_c128_bit_exact(tu, case):
 
     x = G.arr(case["id"], "T")
     z = torch.from_numpy(x + 1j * (-2.0 * x)).cuda()
+    torch.cuda.synchronize()
     tu.add_gate_c128(tu.SectorMap(G.bonds_of(case["T"])), [tuple(p) for p in case["swaps"]], z.data_ptr())
     tu.sync()
     g, got = G.arr(case["id"], "G"), z.cpu().numpy()

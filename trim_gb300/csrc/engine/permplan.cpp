@@ -26,11 +26,13 @@ struct Dim {
 //         with the smallest source or destination stride (it extends a
 //         contiguous run on one side).
 //
-// Limits are in elements for 8-byte elements (a tile <= 4096 elements, a
-// transpose tile within 64 x 65, rows of <= 64); es = 2 (16-byte elements)
-// halves them, so a tile fills the same shared memory.
+// Limits are in elements: a tile <= 4096 elements and a transpose tile within
+// 64 x 65 for 8-byte elements; es = 2 (16-byte elements) halves both, so a
+// tile fills the same shared memory.  Transpose rows stay up to 64 elements
+// wide either way (64 x 32 complex tiles: 86% of the copy rate against 69%
+// for 32 x 63 ones).
 void choose_tile(PermSub& ps, int es) {
-  const int64_t kTile = 4096 / es, kStage = (64 * 65) / es, kRow = 64 / es;
+  const int64_t kTile = 4096 / es, kStage = (64 * 65) / es, kRow = 64;
   const int n = ps.ndim;
   ps.ydim = -1;
   ps.zdim = -1;
