@@ -380,6 +380,7 @@ def itebd_eigh_section(args, torch, tu, stream, flush, spec, els, theta64, rank,
         eo += r
     E = torch.empty(max(eo, 1), dtype=torch.float64, device="cuda")
     V = torch.empty(max(th.elem_num(), 1), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
     run = lambda: tu.eigh_sectors(secs, th.device_ptr(), E.data_ptr(), V.data_ptr())
     for _ in range(args.warmup):
         run()
@@ -496,6 +497,7 @@ def permute_main(args, rank, local, world):
     dst_bonds = [wl.change(bonds[p], 1 if i < rn else -1) for i, p in enumerate(perm)]
     dst_map = tu.SectorMap(dst_bonds)
     y = torch.empty_like(x)
+    torch.cuda.synchronize()  # x is written on torch's stream, read on the library's
     run = tu.permute_device_c128 if c128 else tu.permute_device
     for _ in range(args.warmup):
         run(src_map, dst_map, perm, x.data_ptr(), y.data_ptr())
