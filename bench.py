@@ -398,6 +398,7 @@ def itebd_eigh_section(args, torch, tu, stream, flush, spec, els, theta64, rank,
     run()
     prof = tu.prof_read()
     tu.prof_enable(False)
+    tu.sync()
     e = E.cpu().numpy()
     out = {"sectors": len(secs), "ms_gpu": statistics.median(wall), "kernels_ms": {k_: v["ms"] for k_, v in prof.items()}}
     cpu_ms = None
