@@ -257,6 +257,16 @@ void Ctx::check_device_error() {
   }
 }
 
+const double* mapped_host(const void* host) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, host) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr) return nullptr;
+  return (const double*)a.devicePointer;
+}
+
 cudaStream_t Ctx::side_stream(int i) {
   if (i == 0) return stream;
   while ((int)side.size() < i) {

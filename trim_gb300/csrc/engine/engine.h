@@ -372,6 +372,18 @@ void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const 
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
                           cudaStream_t s);
 void launch_negate_blocks(const int64_t* tab, int n, double* elem, cudaStream_t s);
+// up to kMaxCopies element copies (device or device-mapped host addresses) in one launch
+constexpr int kMaxCopies = 16;
+struct CopyList {
+  double* dst[kMaxCopies];
+  const double* src[kMaxCopies];
+  int64_t n[kMaxCopies];
+  int count;
+};
+void launch_copy_list(const CopyList& L, int grid, cudaStream_t s);
+// the device address of a pinned, mapped host buffer, or null when the device
+// cannot address it (pageable memory: then it takes a copy engine)
+const double* mapped_host(const void* host);
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s);
 void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
                     int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,

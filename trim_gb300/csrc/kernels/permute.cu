@@ -367,6 +367,20 @@ __global__ void __launch_bounds__(256) negate_blocks_kernel(const int64_t* __res
   }
 }
 
+// Several copies in one launch, the list passed by value.  Used for copies
+// between device memory and pinned host memory that the device reads and
+// writes directly (the caller has checked each host buffer is mapped), so a
+// graph step moves its inputs and its result in one kernel node each instead
+// of one copy node per buffer.
+__global__ void __launch_bounds__(256) copy_list_kernel(CopyList L) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int j = 0; j < L.count; j++) {
+    double* __restrict__ d = L.dst[j];
+    const double* __restrict__ s = L.src[j];
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.n[j]; i += stride) d[i] = s[i];
+  }
+}
+
 __global__ void fill_kernel(double* __restrict__ p, int64_t n, double v) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) p[i] = v;
 }
@@ -443,6 +457,13 @@ void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int n
 void launch_negate_blocks(const int64_t* tab, int n, double* elem, cudaStream_t s) {
   if (n <= 0) return;
   negate_blocks_kernel<<<n, 256, 0, s>>>(tab, elem);
+  TN_CUDA(cudaGetLastError());
+}
+
+void launch_copy_list(const CopyList& L, int grid, cudaStream_t s) {
+  if (L.count <= 0) return;
+  if (L.count > kMaxCopies) fail(TN_ERR_ARG, "copy list: too many copies");
+  copy_list_kernel<<<grid, 256, 0, s>>>(L);
   TN_CUDA(cudaGetLastError());
 }
 

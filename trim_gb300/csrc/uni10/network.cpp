@@ -569,20 +569,52 @@ void Network::capture() {
   }
   c.keep = &graph_keep;  // plans and workspace the recorded kernels read
   try {
-    for (size_t i = 0; i < host_in.size(); i++) {  // bound host inputs into the put tensors
+    // bound host inputs into the put tensors.  Pinned host buffers are mapped
+    // into the device's address space: then one kernel reads them all
+    // directly (one graph node, the reads of all inputs in flight at once);
+    // otherwise one copy per input.
+    tn::CopyList in{};
+    bool direct = !host_in.empty() && host_in.size() <= (size_t)tn::kMaxCopies;
+    for (size_t i = 0; i < host_in.size(); i++) {
       UniTensor* t = tensors[host_in[i].first];
       if (host_in_n[i] != t->elemNum())
         throw std::runtime_error("Network::capture: a bound host input does not match its tensor's element count");
-      TN_CUDA(cudaMemcpyAsync(t->getElem(), host_in[i].second, host_in_n[i] * sizeof(double), cudaMemcpyHostToDevice,
-                              cap));
+      const double* hp = direct ? tn::mapped_host(host_in[i].second) : nullptr;
+      if (!hp) {
+        direct = false;
+        continue;
+      }
+      in.dst[in.count] = t->getElem();
+      in.src[in.count] = hp;
+      in.n[in.count] = (int64_t)host_in_n[i];
+      in.count++;
+    }
+    if (direct) {
+      tn::launch_copy_list(in, c.num_sms * 4, cap);
+      c.launched();
+    } else {
+      for (size_t i = 0; i < host_in.size(); i++)
+        TN_CUDA(cudaMemcpyAsync(tensors[host_in[i].first]->getElem(), host_in[i].second, host_in_n[i] * sizeof(double),
+                                cudaMemcpyHostToDevice, cap));
     }
     UniTensor r = launch();
-    TN_CUDA(cudaMemcpyAsync(graph_out.getElem(), r.getElem(), r.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
-                            cap));
-    if (host_out) {
-      if (host_out_n != r.elemNum())
-        throw std::runtime_error("Network::capture: the bound host output does not match the result's element count");
-      TN_CUDA(cudaMemcpyAsync(host_out, graph_out.getElem(), host_out_n * sizeof(double), cudaMemcpyDeviceToHost, cap));
+    if (host_out && host_out_n != r.elemNum())
+      throw std::runtime_error("Network::capture: the bound host output does not match the result's element count");
+    const double* hout = host_out ? tn::mapped_host(host_out) : nullptr;
+    if (hout) {  // the result into the persistent output and the mapped host buffer, one kernel
+      tn::CopyList out{};
+      out.dst[0] = graph_out.getElem();
+      out.dst[1] = const_cast<double*>(hout);
+      out.src[0] = out.src[1] = r.getElem();
+      out.n[0] = out.n[1] = (int64_t)r.elemNum();
+      out.count = 2;
+      tn::launch_copy_list(out, c.num_sms * 4, cap);
+      c.launched();
+    } else {
+      TN_CUDA(cudaMemcpyAsync(graph_out.getElem(), r.getElem(), r.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
+                              cap));
+      if (host_out)
+        TN_CUDA(cudaMemcpyAsync(host_out, graph_out.getElem(), host_out_n * sizeof(double), cudaMemcpyDeviceToHost, cap));
     }
   } catch (...) {
     c.keep = nullptr;
