@@ -374,10 +374,17 @@ __global__ void __launch_bounds__(256) negate_blocks_kernel(const int64_t* __res
 // of one copy node per buffer.
 __global__ void __launch_bounds__(256) copy_list_kernel(CopyList L) {
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   for (int j = 0; j < L.count; j++) {
     double* __restrict__ d = L.dst[j];
     const double* __restrict__ s = L.src[j];
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < L.n[j]; i += stride) d[i] = s[i];
+    int64_t done = 0;
+    if ((((uintptr_t)d | (uintptr_t)s) & 15) == 0) {  // 16-byte requests: half as many round trips
+      const int64_t n2 = L.n[j] >> 1;
+      for (int64_t i = tid; i < n2; i += stride) ((double2*)d)[i] = ((const double2*)s)[i];
+      done = n2 << 1;
+    }
+    for (int64_t i = done + tid; i < L.n[j]; i += stride) d[i] = s[i];
   }
 }
 
