@@ -162,3 +162,27 @@ def test_complex_permute_plans_of_dense_tensors():
         got, written = tu.plan_check_permute_c128(tu.SectorMap(bonds), tu.SectorMap(out), list(perm), x)
         assert written == x.size
         assert np.array_equal(got, x.reshape([chi] * 6).transpose(perm).reshape(-1))
+
+
+def test_permute_plan_of_the_ipeps_operand_short_rows():
+    """The iPEPS quadrant's big operand permute X[10,3|4,20] -> [3,4|10,20]:
+    the combined double-layer bonds carry charge runs of 4, so each
+    sub-block row is 4 elements on both sides; the plan stacks them into 3-D
+    tiles (mode 3).  Bit-exact against the oracle."""
+    rng = np.random.default_rng(9)
+    spec = wl.ipeps_ctm(chi=16, D=4)
+    _, C, T1, _ = spec["tensors"]
+    c_in, dd, c_out = T1.bonds
+    bonds = [dd, wl.change(c_in, 1), wl.change(c_out, -1), wl.change(dd, -1)]  # X[10, 3 | 4, 20]
+    labels, new, rn = [10, 3, 4, 20], [3, 4, 10, 20], 2
+    x = rng.uniform(-1, 1, wl.elem_count(bonds))
+    t = st.UniTensor(to_bonds(bonds), labels, x)
+    t.permute(new, rn)
+    rsp = [labels.index(l) for l in new]
+    out = [wl.change(bonds[rsp[b]], 1 if b < rn else -1) for b in range(4)]
+    got, written = tu.plan_check_permute(tu.SectorMap(bonds), tu.SectorMap(out), rsp, x)
+    assert written == x.size
+    assert np.array_equal(got, t.elem)
+    z = x + 1j * (0.5 * x)
+    gotc, _ = tu.plan_check_permute_c128(tu.SectorMap(bonds), tu.SectorMap(out), rsp, z)
+    assert np.array_equal(gotc.real, t.elem) and np.array_equal(gotc.imag, 0.5 * t.elem)

@@ -20,6 +20,9 @@ struct Dim {
 //         best source dim); y = the next destination dim, several rows/tile.
 // mode 1: 2-D transpose through shared memory: loads run along y (the
 //         source-contiguous dim), stores along x.
+// mode 3: mode-0 rows that are short on both sides (a few elements): tz
+//         row-sets of a third dim stacked into a dense [z][y][x] tile, loaded
+//         in source-stride order and stored in destination-stride order.
 // mode 2: when a transpose tile of x and y is small (short bonds, e.g. 24 x
 //         24), a third dim z is stacked into it (tz planes of x by y) so
 //         that each tile still moves thousands of elements; z is the dim
@@ -66,6 +69,26 @@ void choose_tile(PermSub& ps, int es) {
       ps.ty = (int32_t)std::min<int64_t>(ps.dims[n - 2], std::max<int64_t>(1, kTile / ps.tx));
     } else {
       ps.ty = 1;
+    }
+  }
+  // mode 3: rows contiguous on both sides but short (e.g. the charge runs of
+  // a combined bond, 4 elements): a third dim, the one with the smallest
+  // source or destination stride, stacks tz row-sets into one dense tile
+  if (ps.mode == 0 && n >= 3 && (int64_t)ps.tx * ps.ty <= kTile / 16) {
+    int z = -1;
+    int64_t best = 0;
+    for (int i = 0; i < n - 2; i++) {
+      const int64_t c = std::min(ps.sstride[i], ps.dstride[i]);
+      if (z < 0 || c < best) {
+        z = i;
+        best = c;
+      }
+    }
+    const int64_t tz = std::min<int64_t>((int64_t)ps.dims[z], kTile / ((int64_t)ps.tx * ps.ty));
+    if (tz > 1) {
+      ps.mode = 3;
+      ps.zdim = z;
+      ps.tz = (int32_t)tz;
     }
   }
   if (ps.mode == 1 && (int64_t)ps.tx * ps.ty <= kTile / 2 && n >= 3) {

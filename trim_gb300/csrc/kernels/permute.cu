@@ -6,7 +6,10 @@
 // destination-contiguous dim, so stores are coalesced; in mode 1 y is the
 // source-contiguous dim and the tile is transposed through shared memory so
 // loads are coalesced too; mode 2 stacks tz planes of a third dim z into a
-// small transpose tile.  Remaining dims are decoded once per tile.
+// small transpose tile; mode 3 stacks short rows (x contiguous on both sides
+// but only a few elements long) into a dense [z][y][x] tile that is loaded in
+// source-stride order and stored in destination-stride order.  Remaining dims
+// are decoded once per tile.
 //
 // Elements are 8 bytes (real FP64) or 16 bytes (complex FP64 as (re, im)
 // pairs, the cflag twins UniTensorComplex.cpp:447-825): the kernel is the same
@@ -156,6 +159,38 @@ __device__ __forceinline__ void cp_async_wait() {
 
 constexpr int kStages = 3;  // tiles in flight per CTA: 2 loading while 1 is stored
 
+// Mode 3 (short rows stacked in 3-D): one axis of the [z][y][x] tile -- its
+// full and valid extents, its stride in global memory and in the dense
+// shared-memory tile.
+struct Ax {
+  int t, n, m;
+  int64_t g;
+};
+__device__ __forceinline__ void sort3(Ax& a, Ax& b, Ax& c) {  // ascending global stride
+  Ax t;
+  if (b.g < a.g) { t = a; a = b; b = t; }
+  if (c.g < b.g) { t = b; b = c; c = t; }
+  if (b.g < a.g) { t = a; a = b; b = t; }
+}
+// Every element of the tile, a fastest, by flat index e = tid + k * kThreads
+// (consecutive threads on consecutive addresses along the fastest axis);
+// digits by multiply-high division, exact for e, t < 2^16.
+template <class F>
+__device__ __forceinline__ void walk3(const Ax& a, const Ax& b, const Ax& c, F f) {
+  const uint32_t ma = a.t > 1 ? 0xFFFFFFFFu / (uint32_t)a.t + 1u : 0u;
+  const uint32_t mb = b.t > 1 ? 0xFFFFFFFFu / (uint32_t)b.t + 1u : 0u;
+  const int tot = a.t * b.t * c.t;
+  for (int e = threadIdx.x; e < tot; e += kThreads) {
+    const uint32_t qa = a.t > 1 ? __umulhi((uint32_t)e, ma) : (uint32_t)e;
+    const int ia = e - (int)qa * a.t;
+    const uint32_t qb = b.t > 1 ? __umulhi(qa, mb) : qa;
+    const int ib = (int)qa - (int)qb * b.t;
+    const int ic = (int)qb;
+    if (ia < a.n && ib < b.n && ic < c.n)
+      f(ia * a.m + ib * b.m + ic * c.m, (int64_t)ia * a.g + (int64_t)ib * b.g + (int64_t)ic * c.g);
+  }
+}
+
 // Decode of tile t, or an empty tile (mode -1) past the end of the list.
 __device__ __forceinline__ TileInfo decode_at(const PermSub* __restrict__ subs, const int64_t* __restrict__ tile_start,
                                               int nsub, int64_t ntiles, int64_t t) {
@@ -187,6 +222,12 @@ __device__ __forceinline__ void issue_tile(const TileInfo& w, const T* __restric
         T* sp = buf + yy * pitch + xx;
         for (int zz = 0; zz < w.nz; zz++, g += w.sz, sp += plane) cp_async_el(sp, g);
       }
+    } else if (w.mode == 3) {
+      // [z][y][x] dense; elements in source-stride order
+      Ax a{w.tx, w.nx, 1, w.sx}, b{w.ty, w.ny, w.tx, w.sy}, c{w.tz, w.nz, w.tx * w.ty, w.sz};
+      sort3(a, b, c);
+      const T* s0 = src + w.bs;
+      walk3(a, b, c, [&](int m, int64_t g) { cp_async_el(buf + m, s0 + g); });
     } else if (w.mode == 0 && w.tx >= kThreads) {  // long rows: lanes stride along each row
       for (int yy = 0; yy < w.ny; yy++) {
         const T* g = src + w.bs + (int64_t)yy * w.sy + (int64_t)threadIdx.x * w.sx;
@@ -255,6 +296,13 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const T* buf, T* _
       T* g = dst + w.bd + (int64_t)yy * w.dy + (int64_t)xx * w.dx;
       for (int zz = 0; zz < w.nz; zz++, sp += plane, g += w.dz) *g = apply_flip(*sp, f);
     }
+    return;
+  }
+  if (w.mode == 3) {  // elements in destination-stride order
+    Ax a{w.tx, w.nx, 1, w.dx}, b{w.ty, w.ny, w.tx, w.dy}, c{w.tz, w.nz, w.tx * w.ty, w.dz};
+    sort3(a, b, c);
+    T* d0 = dst + w.bd;
+    walk3(a, b, c, [&](int m, int64_t g) { d0[g] = apply_flip(buf[m], f); });
     return;
   }
   if (w.mode == 0 && w.tx >= kThreads) {  // long rows, as loaded
@@ -412,12 +460,12 @@ int64_t check_permute_plan_host(const PermPlan& plan, const double* src, double*
     TileInfo w = decode_tile(P, t - P.tile_begin);
     if (w.nx > w.tx || w.ny > w.ty || w.nz > w.tz || w.nx <= 0 || w.ny <= 0 || w.nz <= 0)
       fail(TN_ERR_ARG, "plan check: bad tile extents");
-    if (w.mode != 2 && w.tz != 1) fail(TN_ERR_ARG, "plan check: stacked planes outside mode 2");
-    const int64_t stage = w.mode >= 1 ? (int64_t)w.tz * w.ty * (w.tx + 1) : (int64_t)w.tx * w.ty;
+    if (w.mode < 2 && w.tz != 1) fail(TN_ERR_ARG, "plan check: stacked planes outside modes 2 and 3");
+    const int64_t stage = (w.mode == 1 || w.mode == 2) ? (int64_t)w.tz * w.ty * (w.tx + 1) : (int64_t)w.tz * w.tx * w.ty;
     if (stage > kSmem / es) fail(TN_ERR_ARG, "plan check: tile exceeds shared memory");
     if ((int64_t)w.tx * w.ty * w.tz > (int64_t)kThreads * kPerThread)
       fail(TN_ERR_ARG, "plan check: tile exceeds thread walk");
-    if (w.mode == 2 && ((int64_t)w.tx * w.ty * w.tz >= (1 << 16) || w.tx > 4096 || w.ty > 4096))
+    if (w.mode >= 2 && ((int64_t)w.tx * w.ty * w.tz >= (1 << 16) || w.tx > 4096 || w.ty > 4096))
       fail(TN_ERR_ARG, "plan check: tile index exceeds the multiply-high division range");
     for (int zz = 0; zz < w.nz; zz++)
       for (int yy = 0; yy < w.ny; yy++)
