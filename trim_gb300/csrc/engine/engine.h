@@ -139,6 +139,9 @@ struct PermPlan {
 };
 using PermPlanP = std::shared_ptr<PermPlan>;
 
+// rows of a narrow sector (N <= kRowDotMaxN, GemmTile::tn == 1) per work item
+constexpr int kRowDotRows = 16, kRowDotMaxN = 8, kRowDotMaxK = 8192;
+
 // FP64 grouped GEMM work item: one output tile (split along K) of a sector.
 struct GemmTile {
   int64_t a_off, b_off, c_off;  // sector base offsets (elements)
@@ -147,7 +150,7 @@ struct GemmTile {
   int32_t k0, k1;               // K range of this item
   int32_t split;                // index of this K split (0..nsplit-1)
   int32_t nsplit;
-  int32_t tn;                   // tile columns: 32, 16, 8 or 4 (512/tn rows)
+  int32_t tn;                   // tile columns: 32, 16, 8 or 4 (512/tn rows); 1: kRowDotRows rows of a narrow sector
   int32_t grp;                  // split group (one per split output tile), -1 if nsplit==1
   int32_t a_vw, b_vw;           // operand views (ViewHdr index), -1: contiguous row-major
   int64_t ws_off;               // partial-tile slot in the workspace (elements), -1 if nsplit==1

@@ -27,10 +27,17 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
                                       const std::vector<std::pair<int, int>>* vw = nullptr) {
   // K is split so that no work item (one tile over a K range) carries much
   // more than total / (SMs x items_per_sm), with at least ~4 items per SM
+  // narrow sectors read contiguously (no operand view) take warp-per-row items
+  auto rowdot = [&](size_t gi) {
+    const auto& g = list[gi];
+    const bool plain = !vw || ((*vw)[gi].first < 0 && (*vw)[gi].second < 0);
+    return plain && pol.tn_rule == 0 && g.N <= kRowDotMaxN && g.K <= kRowDotMaxK;
+  };
   int64_t tiles = 0;
   double work = 0;
-  for (const auto& g : list) {
-    if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
+  for (size_t gi = 0; gi < list.size(); gi++) {
+    const auto& g = list[gi];
+    if (g.M <= 0 || g.N <= 0 || g.K <= 0 || rowdot(gi)) continue;
     const int tn = tile_width(g.N, pol), tm = kTileElems / tn;
     int64_t t = ((g.M + tm - 1) / tm) * ((g.N + tn - 1) / tn);
     tiles += t;
@@ -44,6 +51,29 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
     const auto& g = list[gi];
     if (g.M <= 0 || g.N <= 0 || g.K <= 0) continue;
     if (g.M > INT32_MAX || g.N > INT32_MAX || g.K > INT32_MAX) fail(TN_ERR_UNSUPPORTED, "sector GEMM dimension too large");
+    if (rowdot(gi)) {
+      for (int64_t m0 = 0; m0 < g.M; m0 += kRowDotRows) {
+        GemmTile t;
+        t.a_off = g.a_off;
+        t.b_off = g.b_off;
+        t.c_off = g.c_off;
+        t.M = (int32_t)g.M;
+        t.N = (int32_t)g.N;
+        t.K = (int32_t)g.K;
+        t.m0 = (int32_t)m0;
+        t.n0 = 0;
+        t.k0 = 0;
+        t.k1 = (int32_t)g.K;
+        t.split = 0;
+        t.nsplit = 1;
+        t.tn = 1;
+        t.grp = -1;
+        t.a_vw = t.b_vw = -1;
+        t.ws_off = -1;
+        out.push_back(t);
+      }
+      continue;
+    }
     const int tn = tile_width(g.N, pol), tm = kTileElems / tn;
     int nsplit = 1;
     if (allow_split) {

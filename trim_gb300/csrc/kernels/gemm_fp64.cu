@@ -21,6 +21,7 @@ namespace tn {
 namespace {
 
 constexpr int kTileElems = 512, kRowsPerLane = 4;
+static_assert(kRowDotRows % 4 == 0, "row-dot items are walked by the 4 warps of a CTA");
 
 __device__ __forceinline__ int find_start(const int64_t* __restrict__ st, int n, int64_t v) {
   int lo = 0, hi = n - 1;  // largest i with st[i] <= v
@@ -118,6 +119,53 @@ __device__ __forceinline__ void fp64_tile(const GemmTile& t, const double* __res
   }
 }
 
+// Narrow sectors (N <= 8, GemmTile::tn == 1): a warp per output row, lanes
+// along K (A's row read coalesced, B's rows k..k+31 -- 32 N contiguous
+// doubles -- read once), N accumulators per lane reduced by a butterfly of
+// shuffles in a fixed order.  An item covers kRowDotRows rows of one sector,
+// the whole K.  A 512-entry tile of at least 4 columns would leave 4 - N of
+// every 4 lanes idle on such sectors.
+template <int NN>
+__device__ __forceinline__ void rowdot_tile(const GemmTile& t, const double* __restrict__ A,
+                                            const double* __restrict__ B, double* __restrict__ C) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double* __restrict__ b = B + t.b_off;
+  for (int r = warp; r < kRowDotRows; r += 4) {
+    const int m = t.m0 + r;
+    if (m >= t.M) break;  // warp-uniform
+    const double* __restrict__ a = A + t.a_off + (int64_t)m * t.K;
+    double acc[NN];
+#pragma unroll
+    for (int n = 0; n < NN; n++) acc[n] = 0.0;
+#pragma unroll 2
+    for (int k = lane; k < t.K; k += 32) {
+      const double av = __ldg(a + k);
+#pragma unroll
+      for (int n = 0; n < NN; n++) acc[n] = fma(av, __ldg(b + (int64_t)k * NN + n), acc[n]);
+    }
+#pragma unroll
+    for (int n = 0; n < NN; n++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) acc[n] += __shfl_xor_sync(0xffffffffu, acc[n], o);
+      if (lane == n) C[t.c_off + (int64_t)m * NN + n] = acc[n];
+    }
+  }
+}
+
+__device__ __forceinline__ void rowdot_dispatch(const GemmTile& t, const double* __restrict__ A,
+                                                const double* __restrict__ B, double* __restrict__ C) {
+  switch (t.N) {
+    case 1: rowdot_tile<1>(t, A, B, C); break;
+    case 2: rowdot_tile<2>(t, A, B, C); break;
+    case 3: rowdot_tile<3>(t, A, B, C); break;
+    case 4: rowdot_tile<4>(t, A, B, C); break;
+    case 5: rowdot_tile<5>(t, A, B, C); break;
+    case 6: rowdot_tile<6>(t, A, B, C); break;
+    case 7: rowdot_tile<7>(t, A, B, C); break;
+    default: rowdot_tile<8>(t, A, B, C); break;
+  }
+}
+
 // The last CTA to finish a split tile sums the group's partial tiles in split
 // order (deterministic) and resets the group's counter for the next launch.
 __device__ __forceinline__ void finish_split(const GemmTile& t, const double* __restrict__ ws, double* __restrict__ C,
@@ -152,6 +200,7 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(const GemmTile* __restri
   for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
     const GemmTile t = tiles[it];
     switch (t.tn) {
+      case 1: rowdot_dispatch(t, A, B, C); break;
       case 4: fp64_tile<4>(t, A, B, C, ws, views, pool); break;
       case 8: fp64_tile<8>(t, A, B, C, ws, views, pool); break;
       case 16: fp64_tile<16>(t, A, B, C, ws, views, pool); break;
