@@ -360,3 +360,31 @@ def test_errors_on_device_path(tu):
     with pytest.raises(capi.TnError) as e:
         a.permute([1, 9], 1)
     assert "do not 1-1 correspond" in str(e.value)
+
+
+def test_ipeps_short_row_permute_bit_exact(tu):
+    """The iPEPS quadrant's operand permute X[10,3|4,20] -> [3,4|10,20] at
+    chi=32, D=4 (rows of 2-4 elements stacked into 3-D tiles): bit-exact
+    against the oracle, real and complex."""
+    import torch
+
+    rng = np.random.default_rng(19)
+    spec = wl.ipeps_ctm(chi=32, D=4)
+    c_in, dd, c_out = spec["tensors"][2].bonds
+    bonds = [dd, wl.change(c_in, 1), wl.change(c_out, -1), wl.change(dd, -1)]
+    labels, new, rn = [10, 3, 4, 20], [3, 4, 10, 20], 2
+    x = rng.uniform(-1, 1, wl.elem_count(bonds))
+    t = tu.UniTensor(bonds, labels, x)
+    t.permute(new, rn)
+    o = st.UniTensor(to_obonds(bonds), labels, x)
+    o.permute(new, rn)
+    assert np.array_equal(t.get_elem(), o.elem)
+    rsp = [labels.index(l) for l in new]
+    out = [wl.change(bonds[rsp[b]], 1 if b < rn else -1) for b in range(4)]
+    z = torch.from_numpy(x + 1j * (0.25 * x)).cuda()
+    y = torch.empty_like(z)
+    torch.cuda.synchronize()
+    tu.permute_device_c128(tu.SectorMap(bonds), tu.SectorMap(out), rsp, z.data_ptr(), y.data_ptr())
+    tu.sync()
+    got = y.cpu().numpy()
+    assert np.array_equal(got.real, o.elem) and np.array_equal(got.imag, 0.25 * o.elem)
