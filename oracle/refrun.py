@@ -1,8 +1,9 @@
 """Drive the compiled reference (oracle/_ref/ref_driver) from Python -- TEST ORACLE.
 
-Used here, where /root/reference exists, to pin the numpy restatement and to
-write golden fixtures.  ``available()`` is False on machines without the
-built reference; callers skip then.
+Used on the machine where the reference sources are present (oracle/_ref
+is built from them by oracle/refbuild/Makefile) to pin the numpy
+restatement and to write golden fixtures.  ``available()`` is False on
+machines without the built reference; callers skip then.
 """
 from __future__ import annotations
 
