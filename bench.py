@@ -42,6 +42,16 @@ def dist_env():
     return int(os.environ.get("RANK", 0)), int(os.environ.get("LOCAL_RANK", 0)), int(os.environ.get("WORLD_SIZE", 1))
 
 
+def max_over_ranks(torch, vals, device):
+    """Element-wise maximum of a list of floats over all ranks (a no-op on
+    one process): the step times every rank reports are the slowest rank's."""
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return [float(v) for v in vals]
+    t = torch.tensor([float(v) for v in vals], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def itebd_inputs():
     spec = wl.itebd()
     rng = np.random.default_rng(spec["seed"])
@@ -275,9 +285,7 @@ def gpu_main(args, rank, local, world):
                      "h2d": sum(8 * els[n].size for n in names), "d2h": 8 * vals.size}
     if world > 1:
         for m in res:
-            t = torch.tensor([res[m]["ms_graph"], res[m]["e2e_ms"]], device="cuda")
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            res[m]["ms_graph"], res[m]["e2e_ms"] = float(t[0]), float(t[1])
+            res[m]["ms_graph"], res[m]["e2e_ms"] = max_over_ranks(torch, [res[m]["ms_graph"], res[m]["e2e_ms"]], "cuda")
 
     svd = itebd_svd_section(args, torch, tu, stream, flush, spec, els, ref64, rank, world)
     eigh = itebd_eigh_section(args, torch, tu, stream, flush, spec, els, ref64, rank, world)
