@@ -31,7 +31,7 @@ std::vector<GemmTile> plan_fp64_split(const std::vector<tn_sector_gemm>& list, i
   auto rowdot = [&](size_t gi) {
     const auto& g = list[gi];
     const bool plain = !vw || ((*vw)[gi].first < 0 && (*vw)[gi].second < 0);
-    return plain && pol.tn_rule == 0 && g.N <= kRowDotMaxN && g.K <= kRowDotMaxK;
+    return plain && pol.tn_rule == 0 && g.N <= kRowDotMaxN && g.K >= 32 && g.K <= kRowDotMaxK;  // lanes along K
   };
   int64_t tiles = 0;
   double work = 0;
