@@ -368,10 +368,13 @@ void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int n
                            bool conj, const void* src, void* dst, int grid, cudaStream_t s);
 // counters (one int per split group, zero between launches) may be null: then
 // split tiles need launch_splitk_reduce afterwards; otherwise the last CTA of
-// each split group sums its partial tiles in split order and resets the counter
+// each split group sums its partial tiles in split order and resets the counter.
+// dependent_launch: launch with programmatic stream serialisation, so the
+// launch overlaps the previous kernel's tail (the kernel waits for that
+// kernel's completion before its first global access)
 void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const double* B, double* C,
                       double* ws, int* counters, const ViewHdr* views, const int64_t* pool, int grid,
-                      cudaStream_t s);
+                      cudaStream_t s, bool dependent_launch = true);
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid,
                           cudaStream_t s);
 void launch_negate_blocks(const int64_t* tab, int n, double* elem, cudaStream_t s);

@@ -13,8 +13,15 @@
 // 512/tn rows (GemmTile::tn, chosen by the planner).  Lane l of a warp owns
 // column l % tn and rows (l / tn) + i * (32 / tn), i < 4, of the warp's
 // 4 * 32/tn rows; A is broadcast across the lanes of a row, B rows are
-// coalesced.  Items split along K write partial tiles to a workspace and a
-// second kernel sums them in split order, so the result is deterministic.
+// coalesced.  Items split along K write partial tiles to a workspace; the
+// last CTA of each split tile (or, without counters, a second kernel) sums
+// them in split order, so the result is deterministic.
+//
+// Consecutive launches on a stream (the chain of contractions of a network)
+// use programmatic dependent launch: a CTA first lets the next grid launch,
+// then waits (griddepcontrol.wait) for the previous grid to complete and its
+// writes to be visible before it touches global memory, so the next launch's
+// set-up overlaps this one's tail while every access stays ordered.
 #include "../engine/engine.h"
 
 namespace tn {
@@ -197,6 +204,9 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(const GemmTile* __restri
                                                         double* __restrict__ ws, int* __restrict__ counters,
                                                         const ViewHdr* __restrict__ views,
                                                         const int64_t* __restrict__ pool) {
+  // no global access before the wait: the previous grid may still be running
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
   for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
     const GemmTile t = tiles[it];
     switch (t.tn) {
@@ -231,10 +241,20 @@ __global__ void __launch_bounds__(kTileElems) splitk_reduce_kernel(const GemmTil
 }  // namespace
 
 void launch_gemm_fp64(const GemmTile* tiles, int ntiles, const double* A, const double* B, double* C, double* ws,
-                      int* counters, const ViewHdr* views, const int64_t* pool, int grid, cudaStream_t s) {
+                      int* counters, const ViewHdr* views, const int64_t* pool, int grid, cudaStream_t s,
+                      bool dependent_launch) {
   if (ntiles <= 0) return;
-  gemm_fp64_kernel<<<grid, 128, 0, s>>>(tiles, ntiles, A, B, C, ws, counters, views, pool);
-  TN_CUDA(cudaGetLastError());
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(128);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = dependent_launch ? 1 : 0;
+  TN_CUDA(cudaLaunchKernelEx(&cfg, gemm_fp64_kernel, tiles, ntiles, A, B, C, ws, counters, views, pool));
 }
 
 void launch_splitk_reduce(const GemmTile* tiles, int ntiles, const double* ws, double* C, int grid, cudaStream_t s) {

@@ -76,7 +76,7 @@ void contract_sectors_fp64_noalloc(cudaStream_t stream, const std::vector<tn_sec
   double* ws = (double*)(base + kTileRegion);
   TN_CUDA(cudaMemcpyAsync(dtiles, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice, stream));
   int grid = (int)std::min<int64_t>((int64_t)tiles.size(), (int64_t)sms * 16);
-  launch_gemm_fp64(dtiles, (int)tiles.size(), A, B, C, ws, nullptr, nullptr, nullptr, grid, stream);
+  launch_gemm_fp64(dtiles, (int)tiles.size(), A, B, C, ws, nullptr, nullptr, nullptr, grid, stream, false);
   if (ws_elems > 0) launch_splitk_reduce(dtiles, (int)tiles.size(), ws, C, grid, stream);
 }
 
