@@ -181,6 +181,26 @@ def _itebd_device(tu, spec, els):
     return names, dev, net
 
 
+def measured_fp64_peak(torch, n=4096, reps=5):
+    """FP64 denominator measured in this run: cuBLAS DGEMM (torch.matmul on
+    float64) of n x n x n, best of `reps` after two warm-ups, CUDA events."""
+    a = torch.rand(n, n, dtype=torch.float64, device="cuda")
+    b = torch.rand(n, n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        c = a @ b
+    best = float("inf")
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        c = a @ b
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    del a, b, c
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 def _time_steps(torch, stream, flush, steps, fn):
     """CUDA-event time per step on the library stream, L2 flushed between steps."""
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
@@ -311,8 +331,9 @@ def gpu_main(args, rank, local, world):
                 "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"}
     elif dname == "gemm_fp64":
         ach = d["flops"] / d["launches"] / (avg_ms * 1e-3) / 1e12
-        roof = {"bound": "fp64", "achieved": ach, "peak": 1.25, "unit": "TFLOP/s",
-                "peak_source": "nominal FP64 rate (no measured FP64 figure)"}
+        roof = {"bound": "fp64", "achieved": ach, "peak": measured_fp64_peak(torch), "unit": "TFLOP/s",
+                "peak_source": "measured in this run: cuBLAS DGEMM 4096^3 (torch.matmul float64), best of 5",
+                "peak_nominal": 1.25}
     elif dname == "tc_slice":
         ach = d["bytes"] / d["launches"] / (avg_ms * 1e-3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
@@ -326,6 +347,14 @@ def gpu_main(args, rank, local, world):
                 "peak_source": "measured (burst)" if "bf16_tflops" in peaks else "fallback",
                 "work": "BF16 tensor flops (34 digit products per FP64-equivalent flop)" if pairs > 1 else "BF16 flops"}
     roof.update({"kernel": dname, "frac": roof["achieved"] / roof["peak"], "avg_launch_ms": avg_ms, "traffic": None})
+    if dname == "gemm_fp64":
+        # dram__bytes_read.sum + dram__bytes_write.sum per launch, mean over the
+        # network's five gemm_fp64 launches (grids 545/593/667/762/543), from one
+        # ncu capture of `bench.py --no-cpu --steps 3 --warmup 3 --clock-seconds 0`
+        roof.update({"traffic": 880589.0, "traffic_unit": "bytes per launch",
+                     "traffic_source": "ncu, mean over the 5 network launches (reads 0.73-1.12 MB, writes 0: "
+                                       "outputs stay in L2)",
+                     "algorithmic_bytes_per_launch": d["bytes"] / d["launches"]})
     kernels = {k_: {"ms_per_step": v["ms"] / args.steps, "launches_per_step": v["launches"] / args.steps}
                for k_, v in prof.items()}
     pbytes = prof.get("permute", {}).get("bytes", 0.0)
