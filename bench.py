@@ -241,6 +241,8 @@ def gpu_main(args, rank, local, world):
 
     stream = torch.cuda.Stream()
     tu.set_stream(stream.cuda_stream)
+    if args.autotune:  # FP64 GEMM policies timed per sector histogram on the first eager launch
+        tu.autotune(True)
     spec, els = itebd_inputs()
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     modes = ["fp64"] + ([args.mode] if args.mode != "fp64" else [])
@@ -379,6 +381,7 @@ def gpu_main(args, rank, local, world):
             "data": "synthetic (seeded)",
             "config": {"workload": WORKLOAD, "chi": 512, "sectors": 17, "mode": head, "flops_per_step": flops,
                        "execution": "Network::launch captured as one CUDA graph, replayed per step",
+                       "fp64_policy": "autotuned per sector histogram" if args.autotune else "default",
                        "l2": "flushed between timed steps (512 MB write)", "parallelism": f"replicas x{world}"},
             "error_vs_fp64": R["err_vs_fp64"],
             "speedup_vs_fp64_gpu": res["fp64"]["ms_graph"] / R["ms_graph"],
@@ -814,6 +817,8 @@ def main():
     ap.add_argument("--D", type=int, default=8)
     ap.add_argument("--batch", type=int, default=1024)
     ap.add_argument("--modes", default="split,bf16")
+    ap.add_argument("--autotune", action="store_true",
+                    help="iTEBD workload: FP64 GEMM tile/split policies from the autotuner")
     ap.add_argument("--chi", type=int, default=24)
     ap.add_argument("--perm", default="4,5,0,1,2,3", help="permute workload: the new bond order")
     ap.add_argument("--perm-rownum", type=int, default=2, help="permute workload: incoming bonds after the permute")

@@ -281,6 +281,48 @@ def test_fused_form_reads_permuted_operands_in_place(env):
     assert seen_views > 0
 
 
+def test_graph_host_io_odd_counts_and_8_byte_offsets(env):
+    """Host-bound graph I/O where the one-launch copy list takes its 8-byte
+    path (a host buffer 8 bytes past a 16-byte boundary) and its odd-count
+    tail (15, 35 and 21 elements): the replayed result is the product of the
+    current host inputs, bit-identical to an eager launch."""
+    torch, capi, tu = env
+    net = tu.Network("X: 1; 2\nY: 2; 3\nTOUT: 1; 3\n")
+    dims = {"X": (3, 5), "Y": (5, 7)}
+    bond = lambda t, d: wl.u1_bond(t, (0,), (d,))
+    rng = np.random.default_rng(7)
+    els = {n: rng.uniform(-1, 1, m * k) for n, (m, k) in dims.items()}
+    ts = {"X": tu.UniTensor([bond(wl.IN, 3), bond(wl.OUT, 5)], [1, 2], els["X"]),
+          "Y": tu.UniTensor([bond(wl.IN, 5), bond(wl.OUT, 7)], [2, 3], els["Y"])}
+    for n, t in ts.items():
+        net.put_tensor(n, t)
+    eager = net.launch("fp64").get_elem()
+    want = els["X"].reshape(3, 5) @ els["Y"].reshape(5, 7)
+    assert np.abs(eager - want.ravel()).max() <= 1e-13 * np.abs(want).max()
+    # X one element into its pinned buffer (8-byte aligned only), Y at the start
+    xbuf = torch.zeros(16 + 1, dtype=torch.float64).pin_memory()
+    xbuf[1:16].copy_(torch.from_numpy(els["X"]))
+    ybuf = torch.from_numpy(els["Y"].copy()).pin_memory()
+    obuf = torch.full((22,), np.nan, dtype=torch.float64).pin_memory()
+    net.bind_host_input("X", xbuf.data_ptr() + 8, 15)
+    net.bind_host_input("Y", ybuf.data_ptr(), 35)
+    net.bind_host_output(obuf.data_ptr() + 8, 21)
+    net.capture("fp64")
+    net.replay()
+    tu.sync()
+    assert np.array_equal(obuf[1:].numpy(), eager)
+    assert np.isnan(obuf[0].item())  # nothing written before the bound output
+    xbuf[1:16].mul_(-2.0)
+    ybuf.add_(0.5)
+    net.replay()
+    tu.sync()
+    ts["X"].set_elem(xbuf[1:16].numpy().copy())
+    ts["Y"].set_elem(ybuf.numpy().copy())
+    for n, t in ts.items():
+        net.put_tensor(n, t)
+    assert np.array_equal(obuf[1:].numpy(), net.launch("fp64").get_elem())
+
+
 def test_graph_with_host_bound_inputs_and_output(env):
     """Network capture with pinned host buffers bound: every replay copies the
     current host inputs in and theta out; bit-identical to eager launches on
