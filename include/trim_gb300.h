@@ -53,7 +53,7 @@ enum {
   TN_MODE_FP64 = 0,      /* plain FP64 GEMM per sector: the drop-in form */
   TN_MODE_SPLIT = 1,     /* split-precision: BF16 slices on tcgen05, FP64-level error */
   TN_MODE_FAST_BF16 = 2, /* one BF16 slice, FP32 accumulation */
-  TN_MODE_FAST_TF32 = 3, /* TF32 operands, FP32 accumulation */
+  TN_MODE_FAST_TF32 = 3, /* TF32 operands (tcgen05 kind::tf32, tiled form), FP32 accumulation */
   /* flag: in the tensor-core modes, send every sector to the tensor cores
    * (by default a sector with K < 16 or N < 16 runs on the exact FP64
    * kernel instead) */
@@ -73,6 +73,7 @@ typedef struct tn_ctx_s* tn_ctx_t;
 typedef struct tn_smap_s* tn_smap_t;
 typedef struct tn_tensor_s* tn_tensor_t;
 typedef struct tn_network_s* tn_network_t;
+typedef struct tn_batch_s* tn_batch_t;
 
 /* One sector GEMM of a contraction: C[M x N] = A[M x K] . B[K x N], all
  * row-major and dense (ld = K, N, N), at element offsets into the A, B, C
@@ -162,6 +163,15 @@ int tn_plan_check_views(tn_smap_t src, tn_smap_t dst, const int* rsp, const doub
 int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A,
                         const double* B, double* C);
 
+/* The n sector GEMMs one launch each, in list order: the reference's
+ * per-sector matrixMul loop (tensor-network/lib/UniTensorTools.cpp:191-203,
+ * one cublasDgemm per sector on its GPU build, numeric/lapack/lib/uni10_lapack_gpu.cu:42-50)
+ * kept as the baseline the grouped launch is measured against.  Same
+ * arguments and results as tn_contract_sectors (A, B, C may be NULL when
+ * the offsets are absolute element addresses, device address / 8). */
+int tn_contract_sectors_loop(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A,
+                             const double* B, double* C);
+
 /* Autotuner of the FP64 grouped GEMM (no counterpart in the reference): when
  * on, the first contraction with a new sector-size histogram (the number of
  * sectors per (log2 M, log2 N, log2 K) bucket) times each candidate plan --
@@ -178,15 +188,19 @@ int tn_autotune(tn_ctx_t ctx, int on, int64_t* entries);
  * GPU for its own allocator under a hard cap, a latency-critical loop that
  * must not enter the allocator, a plugin host that forbids device allocation
  * after start-up).  It has no counterpart in the reference.
- * Its tile list and split-K partial tiles live in one file-scope device array
+ * Its work list and split-K partial tiles live in one file-scope device array
  * of TN_NOALLOC_SCRATCH_BYTES, held by every GPU that loads the library until
  * the process exits; it calls no cudaMalloc/cudaFree or allocating library
  * routine.  The caller passes A, B, C (device) and the stream (NULL: legacy
  * default stream).  The first call on a device looks up the array's device
- * address (cudaGetSymbolAddress, that device current): make it before any
- * stream capture.  Work that needs more output tiles than the array holds is
- * rejected with TN_ERR_ARG.  All calls share the array: calls that overlap on
- * the GPU race, so order them (one stream). */
+ * address (cudaGetSymbolAddress, that device current).  The work list holds
+ * 11 915 items (an output tile over a K range, or 16 rows of a sector with
+ * N <= 8); when the K-split plan needs more, K is left unsplit, and work that
+ * still needs more items is rejected with TN_ERR_ARG.  The work list is copied
+ * from pageable host memory, so a call returns only after the stream's
+ * earlier work has completed, and a call on a stream that is being captured
+ * returns TN_ERR_UNSUPPORTED without issuing anything.  All calls share the
+ * array: calls that overlap on the GPU race, so order them (one stream). */
 #define TN_NOALLOC_SCRATCH_BYTES (8u << 20)
 int tn_contract_sectors_fp64_noalloc(void* cuda_stream, int n, const tn_sector_gemm* list, const double* A,
                                      const double* B, double* C);
@@ -268,6 +282,29 @@ int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n);
 /* device-resident element buffer (getElem() on a device build) */
 int tn_tensor_device_elem(tn_tensor_t t, double** dev, int64_t* n);
 int tn_tensor_set_elem_device(tn_tensor_t t, const double* dev, int64_t n);
+/* UniTensor(const std::string& fname) (UniTensor.cpp:486-583) and
+ * UniTensor::save (UniTensor.cpp:922-986): the reference's binary layout
+ * (r_flag, c_flag, name, status, bonds, labels, elements), read and written
+ * byte for byte.  load also reads the reference's older layout without the
+ * flags and name (its own fixtures, e.g. Swig/examples/egU3_W, use it).
+ * Real tensors only; a malformed file gives TN_ERR_FILE. */
+int tn_tensor_load(tn_ctx_t ctx, const char* path, tn_tensor_t* out);
+int tn_tensor_save(tn_tensor_t t, const char* path);
+/* putBlock(const Qnum&, const Block&) (UniTensor.h:633, UniTensorReal.cpp:208-239)
+ * from host memory: the block of charge (qnum[0], qnum[1], qnum[2]) =
+ * (U1, parity, fermionic parity) becomes a rows x cols matrix (row-major,
+ * n = rows * cols values) or, with diag != 0, a diagonal one (n = min(rows,
+ * cols) values; the rest of the block is zeroed, as the reference does). */
+int tn_tensor_put_block(tn_tensor_t t, const int* qnum, int64_t rows, int64_t cols, int diag, const double* host,
+                        int64_t n);
+/* No reference counterpart: *diag = 1 when the tensor has one row and one
+ * column bond and every block is known to be diagonal (filled only by
+ * diagonal putBlock calls after creation, or S of tn_tensor_svd_truncate).
+ * A contraction with such a tensor over one bond runs as a row or column
+ * scale of the other operand -- the diagonal paths of RDotR (diagRowMul /
+ * diagColMul, data-structure/lib/BlockTools.cpp:45-60) -- instead of sector
+ * GEMMs; a dense write (setElem) clears the flag. */
+int tn_tensor_is_diagonal(tn_tensor_t t, int* diag);
 int tn_tensor_set_label(tn_tensor_t t, int n, const int* labels);
 int tn_tensor_get_labels(tn_tensor_t t, int* labels, int* n);
 /* bond signature of the tensor (same packing as tn_tensor_create); sizes in/out */
@@ -291,6 +328,27 @@ int tn_contract(tn_tensor_t a, tn_tensor_t b, int fast, int mode, tn_tensor_t* o
  * pair (UniTensorTools.cpp:124-244, one matrixMul per sector); out[i] is
  * what contract(a[i], b[i]) returns. */
 int tn_contract_batch(int n, const tn_tensor_t* a, const tn_tensor_t* b, int mode, tn_tensor_t* out);
+/* ---- batches of independent contractions (no reference counterpart: the
+ * reference contracts pair by pair, UniTensorTools.cpp:124-244) ----------
+ * A batch keeps copies of the n operand pairs, their permuted forms and the
+ * n outputs in device memory for its lifetime, so tn_batch_launch runs every
+ * operand permute and then all sector GEMMs of all pairs as one grouped
+ * launch on a work list planned at the first launch (no host planning per
+ * call).  tn_batch_capture records a launch as one CUDA graph that
+ * tn_batch_replay reruns on the elements last put (tn_batch_put copies a
+ * pair's new elements into the batch; the bonds must stay the same).
+ * tn_batch_output returns a handle sharing output i's buffer; it is what
+ * contract(a[i], b[i]) returns.  Outer products (no contracted bond) are
+ * refused.  tn_batch_sectors gives the grouped work list (absolute element
+ * addresses), e.g. for tn_contract_sectors_loop. */
+int tn_batch_create(int n, const tn_tensor_t* a, const tn_tensor_t* b, tn_batch_t* out);
+int tn_batch_destroy(tn_batch_t b);
+int tn_batch_put(tn_batch_t b, int i, tn_tensor_t a, tn_tensor_t bt);
+int tn_batch_launch(tn_batch_t b, int mode);
+int tn_batch_capture(tn_batch_t b, int mode);
+int tn_batch_replay(tn_batch_t b);
+int tn_batch_output(tn_batch_t b, int i, tn_tensor_t* out);
+int tn_batch_sectors(tn_batch_t b, int cap, tn_sector_gemm* list, int* n);
 /* otimes(Ta, Tb) (UniTensorTools.cpp:246-273) */
 int tn_otimes(tn_tensor_t a, tn_tensor_t b, int mode, tn_tensor_t* out);
 /* multiply every element by a (operator*=(Real), UniTensor.h:262) */

@@ -6,4 +6,5 @@
 #include "uni10/Matrix.h"
 #include "uni10/UniTensor.h"
 #include "uni10/Network.h"
+#include "uni10/Batch.h"
 #endif

@@ -35,6 +35,8 @@ typedef struct {
 void setContractMode(int mode);
 int contractMode();
 
+class Batch;
+
 class UniTensor {
  public:
   UniTensor();
@@ -59,7 +61,9 @@ class UniTensor {
   // stream has passed it (any synchronising call, e.g. getElem to the host).
   // With pinned host memory the copy overlaps the caller's next calls.
   void setElemAsync(const double* host);
-  double* getElem();               // device pointer
+  double* getElem();               // device pointer (a writable escape: clears isDiagonal())
+  // Not in the reference: the device element buffer for reading
+  const double* elemPtr() const;
   std::vector<double> hostElem() const;
   double at(size_t idx) const;
   double operator[](size_t idx) const { return at(idx); }
@@ -87,6 +91,14 @@ class UniTensor {
   Matrix getBlock(const Qnum& qnum, bool diag = false) const;
   void putBlock(const Block& mat);
   void putBlock(const Qnum& qnum, const Block& mat);
+  // Not in the reference: true for a tensor with one row and one column bond
+  // whose blocks are all diagonal -- filled only through putBlock with
+  // diagonal matrices after creation or set_zero (as the reference's
+  // singular-value and Lambda tensors are), or S of svdTruncate.  A
+  // contraction of such a tensor over one bond is a row or column scale of
+  // the other operand (the diagonal paths of RDotR), not a sector GEMM.
+  // setElem and any other dense write clear it.
+  bool isDiagonal() const { return diag_; }
 
   // the hot path
   UniTensor& permute(const std::vector<int>& newLabels, int inBondNum);
@@ -130,6 +142,7 @@ class UniTensor {
   const tn::SectorMap* sectorMap() const { return smap.get(); }
 
   friend class Network;
+  friend class Batch;
   friend class Node;
 
  private:
@@ -137,6 +150,8 @@ class UniTensor {
   UniTensor(const std::vector<Bond>& _bonds, const std::string& _name, NoFill);
   static UniTensor permuted(const UniTensor& src, const std::vector<int>& newLabels, int rowBondNum);
   static UniTensor contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool mutate);
+  struct DiagCall;
+  static bool contract_diag(const DiagCall& d);
   struct ContractWork;
   static void prepare_contract(const UniTensor& Ta, const UniTensor& Tb, ContractWork& w);
   static void finish_contract(ContractWork& w);
@@ -149,6 +164,7 @@ class UniTensor {
   int status = 0;
   std::shared_ptr<const tn::SectorMap> smap;
   std::shared_ptr<tn::DevBuf> elem;
+  bool diag_ = false;  // see isDiagonal()
   static const int HAVEBOND = 1;
   static const int HAVEELEM = 2;
 };

@@ -17,6 +17,7 @@
 //   network OUT NETFILE N1 T1 N2 T2 ...   Network::putTensor(Ni, Ti); launch()
 //   copy OUT SRC                   deep copy
 //   save NAME PATH                 UniTensor::save (current binary layout)
+//   name NAME STR                  UniTensor::setName
 //   svd NAME U1 PRT PRTF PREFIX    Block::svd of one block -> PREFIX.{U,S,VT}
 //   eigh NAME U1 PRT PRTF PREFIX   Block::eigh of one block -> PREFIX.{E,V}
 //   addgate NAME B1 B2 [B1 B2 ...]  UniTensor::addGate with these bond swaps
@@ -119,6 +120,8 @@ static void run(const std::vector<std::string>& w) {
     T[w[1]] = get(w[2]);
   } else if (op == "save") {
     get(w[1]).save(w[2]);
+  } else if (op == "name") {
+    get(w[1]).setName(w[2]);
   } else if (op == "labels") {
     get(w[1]).setLabel(ints(w, 2));
   } else if (op == "svd") {

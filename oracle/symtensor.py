@@ -257,7 +257,14 @@ def grouping(bonds: list[Bond]) -> SectorMap:
 class UniTensor:
     """Real (FP64) symmetric tensor: bonds, labels and the contiguous elem
     buffer whose blocks lie back to back in Qnum order, each row-major
-    (UniTensorReal.cpp:1365-1374)."""
+    (UniTensorReal.cpp:1365-1374).
+
+    ``diag`` marks a tensor with one row and one column bond whose blocks were
+    all put as diagonal matrices (the reference's Lambda / singular-value
+    matrices); contract() then applies it as a row or column scale, the
+    diagonal paths of RDotR (BlockTools.cpp:45-60)."""
+
+    diag = False
 
     def __init__(self, bonds: list[Bond], labels=None, elem=None, name: str = ""):
         self.bonds = [b.copy() for b in bonds]
@@ -290,13 +297,27 @@ class UniTensor:
         _, r, c, off = self.smap.blocks[self.smap.block_index[q]]
         return self.elem[off : off + r * c].reshape(r, c)
 
-    def put_block(self, q: Qnum, mat) -> None:
-        self.get_block(q)[...] = mat
+    def put_block(self, q: Qnum, mat, diag: bool = False, fresh: bool = False) -> None:
+        """putBlock (UniTensorReal.cpp:208-239); with diag, ``mat`` is the
+        diagonal and the rest of the block is zeroed.  ``fresh``: no element
+        has been set since creation, so all-diagonal puts make a diagonal
+        tensor."""
+        blk = self.get_block(q)
+        if diag:
+            blk[...] = 0.0
+            n = min(blk.shape)
+            blk[np.arange(n), np.arange(n)] = np.asarray(mat, dtype=np.float64)[:n]
+            if fresh or self.diag:
+                self.diag = len(self.bonds) == 2 and self.in_bond_num() == 1
+        else:
+            blk[...] = mat
+            self.diag = False
 
     def copy(self) -> "UniTensor":
         t = UniTensor.__new__(UniTensor)
         t.bonds = [b.copy() for b in self.bonds]
         t.name, t.smap, t.labels, t.elem = self.name, self.smap, list(self.labels), self.elem.copy()
+        t.diag = self.diag
         return t
 
     def set_label(self, labels) -> None:
@@ -329,6 +350,7 @@ class UniTensor:
         out = UniTensor(out_bonds, labels=list(new_labels), name=self.name)
         permute_elems(self, out, rsp)
         self.bonds, self.smap, self.labels, self.elem = out.bonds, out.smap, out.labels, out.elem
+        self.diag = self.diag and n == 2 and row_bond_num == 1  # a block-wise transpose
         return self
 
     def permute_rows(self, row_bond_num: int) -> "UniTensor":  # UniTensorReal.cpp:508-518
@@ -585,13 +607,28 @@ def contract(ta: UniTensor, tb: UniTensor, fast: bool = False, gemm=None) -> Uni
     tc = UniTensor(c_bonds)
     if c_bonds:
         tc.set_label(new_lc)
+    # a diagonal operand contracted over one bond: RDotR's diagRowMul /
+    # diagColMul (BlockTools.cpp:45-60), no GEMM; rows (columns) beyond the
+    # diagonal's length are zero, as the reference's resize leaves them
+    da = ta.diag and an == 2 and con == 1
+    db = not da and tb.diag and bn == 2 and con == 1
     for q, r, k, off in ta.smap.blocks:
         if q in tb.smap.block_index:
             bb = tb.get_block(q)
             cb = tc.get_block(q)
             if not (r == cb.shape[0] and bb.shape[1] == cb.shape[1] and k == bb.shape[0]):
                 raise ValueError("The dimensions the bonds to be contracted out are different.")
-            cb[...] = gemm(ta.elem[off : off + r * k].reshape(r, k), bb)
+            ab = ta.elem[off : off + r * k].reshape(r, k)
+            if da:
+                n = min(r, k)
+                cb[:n] = np.diagonal(ab)[:n, None] * bb[:n]
+                cb[n:] = 0.0
+            elif db:
+                n = min(bb.shape)
+                cb[:, :n] = ab[:, :n] * np.diagonal(bb)[None, :n]
+                cb[:, n:] = 0.0
+            else:
+                cb[...] = gemm(ab, bb)
     if con == 0:  # outer product, UniTensorTools.cpp:206-225
         lc = old_la[:old_ra] + old_lb[:old_rb] + old_la[old_ra:] + old_lb[old_rb:]
         tc.permute(lc, old_ra + old_rb)

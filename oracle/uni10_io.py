@@ -85,3 +85,20 @@ def write_tensor(path: str, bonds, labels, elem, name: str = "") -> None:
     out += struct.pack("<Q", e.size) + e.tobytes()
     with open(path, "wb") as f:
         f.write(out)
+
+
+def legacy_bytes(bonds, labels, elem, status: int = HAVEBOND | HAVEELEM) -> bytes:
+    """The older layout (no r_flag, c_flag, name): the bytes of the reference's
+    own fixtures (Swig/examples/egU3_W ...)."""
+    out = bytearray(struct.pack("<iiQ", status, len(bonds), 12))
+    for btype, runs in bonds:
+        out += struct.pack("<ii", btype, len(runs))
+        for (u, p, f, _) in runs:
+            out += struct.pack("<iii", u, p, f)
+        for (_, _, _, d) in runs:
+            out += struct.pack("<i", d)
+    out += struct.pack("<i", len(labels)) + struct.pack(f"<{len(labels)}i", *labels)
+    if status & HAVEELEM:
+        e = np.ascontiguousarray(elem, dtype="<f8")
+        out += struct.pack("<Q", e.size) + e.tobytes()
+    return bytes(out)

@@ -2,8 +2,8 @@
 
 Run here (where the reference sources exist and oracle/_ref is built):
 
-    make -C oracle/refbuild REFSRC=/root/reference/uni10/src
-    python tests/golden/make_golden.py --refroot /root/reference/uni10
+    make -C oracle/refbuild REFSRC=<reference project root>/uni10/src
+    python tests/golden/make_golden.py --refroot <reference project root>/uni10
 
 It writes:
   cases.json / arrays.npz  reference outputs (UniTensor::permute, transpose,
@@ -18,7 +18,15 @@ It writes:
                            inputs so a test can tell an RNG drift from a bug.
   legacy.npz               the reference's own fixtures Swig/examples/egU3_W,
                            egU3_WT, egU1_H_U1 and mat_U/mat_Sigma/mat_VT,
-                           decoded from their legacy binary layout.
+                           decoded from their legacy binary layout (with the
+                           SHA-256 of each file's bytes, which pins the
+                           legacy writer of oracle/uni10_io.py).
+  saved/*.uni10, saved.json  tensors written by the reference's
+                           UniTensor::save (current layout) from seeded
+                           inputs, for the product's file reader.
+
+    python tests/golden/make_golden.py --refroot ... --only saved,legacy
+regenerates only the last two.
 """
 from __future__ import annotations
 
@@ -471,21 +479,72 @@ def legacy(refroot: str):
     out = {}
     meta = {}
     for f in ("egU3_W", "egU3_WT", "egU1_H_U1"):
-        d = uni10_io.read_legacy(os.path.join(ex, f))
+        path = os.path.join(ex, f)
+        d = uni10_io.read_legacy(path)
+        with open(path, "rb") as fh:
+            raw = fh.read()
+        if uni10_io.legacy_bytes(d["bonds"], d["labels"], d["elem"], d["status"]) != raw:
+            raise SystemExit(f"legacy writer does not reproduce {f}")
         out[f] = d["elem"]
-        meta[f] = {"bonds": [[t, [list(r) for r in runs]] for t, runs in d["bonds"]], "labels": d["labels"]}
+        meta[f] = {"bonds": [[t, [list(r) for r in runs]] for t, runs in d["bonds"]], "labels": d["labels"],
+                   "status": d["status"], "sha256": hashlib.sha256(raw).hexdigest()}
     for f in ("mat_U", "mat_Sigma", "mat_VT"):
         out[f] = np.fromfile(os.path.join(ex, f), dtype="<f8")
     out["_meta"] = np.frombuffer(json.dumps(meta).encode(), dtype=np.uint8)
     np.savez(os.path.join(HERE, "legacy.npz"), **out)
 
 
+# tensors saved by UniTensor::save: (file, bond signature, labels, name, with elements)
+SAVED = [
+    ("u1_rank3", [wl.u1_bond(1, (-1, 0, 1), (2, 3, 1)), wl.u1_bond(1, (1, -1), (1, 1)),
+                  wl.u1_bond(-1, (-2, -1, 0, 1, 2), (1, 2, 3, 2, 1))], [4, -2, 7], "ALa", True),
+    ("z2_fermion_rank4", [(1, [(0, 0, 0, 2), (0, 1, 1, 3)]), (1, [(0, 0, 0, 1), (0, 1, 1, 2)]),
+                          (-1, [(0, 0, 0, 2), (0, 1, 1, 2)]), (-1, [(0, 1, 1, 1), (0, 0, 0, 3)])], [0, 1, 2, 3], "", True),
+    ("dense_rank2", [wl.dense_bond(1, 5), wl.dense_bond(-1, 7)], [10, 11], "M", True),
+    ("u1_no_elements", [wl.u1_bond(1, (0, 1), (2, 2)), wl.u1_bond(-1, (0, 1), (3, 1))], [0, 1], "empty", False),
+]
+
+
+def saved_files():
+    """UniTensor::save of seeded tensors by the compiled reference."""
+    d = os.path.join(HERE, "saved")
+    os.makedirs(d, exist_ok=True)
+    rng = np.random.default_rng(6006)
+    index = []
+    S = refrun.RefSession()
+    for fname, bonds, labels, name, with_elem in SAVED:
+        el = rng.uniform(-1, 1, wl.elem_count(bonds))
+        if with_elem:
+            S.tensor(fname, bonds, labels, el)
+        else:
+            S.lines.append(f"tensor {fname} {len(bonds)}")
+            S.lines += [refrun.bond_line(b) for b in bonds]
+            S.lines.append("labels " + fname + " " + " ".join(map(str, labels)))
+        if name:
+            S.cmd(f"name {fname} {name}")
+        S.cmd(f"save {fname} {os.path.join(d, fname + '.uni10')}")
+        index.append({"file": fname + ".uni10", "bonds": [[t, [list(r) for r in runs]] for t, runs in bonds],
+                      "labels": labels, "name": name or fname,  # the driver names a tensor after its handle
+                      "elem": [float(x) for x in el] if with_elem else None})
+    S.run()
+    with open(os.path.join(HERE, "saved.json"), "w") as f:
+        json.dump(index, f, indent=0)
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--refroot", default="/root/reference/uni10")
+    ap.add_argument("--refroot", required=True, help="the reference project's uni10/ directory")
+    ap.add_argument("--only", default="", help="comma-separated subset: saved, legacy")
     args = ap.parse_args()
     if not refrun.available():
         sys.exit("build oracle/_ref first: make -C oracle/refbuild")
+    if args.only:
+        parts = set(args.only.split(","))
+        if "saved" in parts:
+            saved_files()
+        if "legacy" in parts:
+            legacy(args.refroot)
+        return
     rng = np.random.default_rng(12345)
     w = Writer()
     workload1(w)

@@ -54,10 +54,11 @@ def test_reference_arm_under_torchrun_prints_once():
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
            "127.0.0.1", "--master-port", str(free_port()), os.path.join(ROOT, "bench.py"), "--impl", "reference",
-           "--gpus", "2", "--steps", "1", "--warmup", "1"]
+           "--gpus", "2", "--steps", "2", "--warmup", "1", "--chi", "6"]
     p = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=ROOT)
     assert p.returncode == 0, p.stderr[-2000:]
     lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["config"]["workload"] == "mera_ternary_chi6" and d["e2e"]["h2d_bytes_per_step"] == 0

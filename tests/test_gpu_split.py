@@ -134,6 +134,41 @@ def test_fast_bf16_reports_bf16_level_error(env, mode):
     assert max(errs) <= 1e-2, errs
 
 
+@pytest.mark.parametrize("shapes", [[(128, 64, 256), (50, 40, 30)],
+                                    [(1, 1, 1), (33, 17, 9), (130, 70, 65), (127, 63, 129), (300, 200, 600)]])
+def test_fast_tf32_reports_tf32_level_error(env, shapes):
+    # TF32 keeps 10 mantissa bits (BF16 7): relative error near 2^-11 per
+    # operand, accumulated in FP32
+    errs = _grouped(env, "tf32_tc", shapes, 6)
+    assert max(errs) <= 2e-3, errs
+    errs_b = _grouped(env, "bf16_tiled", shapes, 6)
+    assert np.mean(errs) < np.mean(errs_b) / 2, (errs, errs_b)
+
+
+def test_fast_tf32_network(env):
+    torch, capi, tu = env
+    c = G.cases()["mera_small"]
+    spec = wl.mera(**c["params"])
+    rng = np.random.default_rng(0)
+    els = {s.name: wl.gen_elems(s, rng) for s in spec["tensors"]}
+    for dname, netx in spec["nets"].items():
+        net = tu.Network(netx)
+        keep = []
+        for s in spec["tensors"]:
+            t = tu.UniTensor(s.bonds, s.labels, els[s.name])
+            keep.append(t)
+            net.put_tensor(s.name, t)
+        r = net.launch(mode="tf32_tc")
+        assert rel(r.get_elem(), G.arr("mera_small", dname)) <= 5e-3, dname
+
+
+def test_fused_tf32_is_refused(env):
+    torch, capi, tu = env
+    with pytest.raises(capi.TnError) as e:
+        _grouped(env, capi.MODE_FAST_TF32 | capi.MODE_TC_ONLY | capi.MODE_TC_FUSED, [(64, 64, 64)], 1)
+    assert e.value.code == 7  # TN_ERR_UNSUPPORTED
+
+
 def test_split_contract_golden_cases(env):
     torch, capi, tu = env
     for case in [c for c in G.cases().values() if c["kind"] == "contract"]:

@@ -1,6 +1,7 @@
-"""Full-size workloads on the GPU against the CPU oracle (FP64, 1e-13) and
-split precision against FP64 (1e-12): the Z2 iPEPS CTM quadrant (chi=128,
-D=8) and the dense MERA ascend at chi=12; batched at n=64 of full-size dims."""
+"""Workloads on the GPU against the CPU oracle (FP64, 1e-13) and split
+precision against FP64 (1e-12): the Z2 iPEPS CTM quadrant at full size
+(chi=128, D=8) and the dense MERA ascend at chi=12 (chi=24 and the full
+1024-contraction batch are in test_gpu_full_size.py)."""
 import numpy as np
 import pytest
 

@@ -82,3 +82,55 @@ def test_noalloc_rejects_work_beyond_the_fixed_scratch(env):
                   A.data_ptr(), A.data_ptr())
     assert e.value.code == 1  # TN_ERR_ARG
     assert "fixed scratch" in str(e.value)
+
+
+def test_noalloc_narrow_sectors_and_many_items(env):
+    # sectors with N <= 8 and 32 <= K take 16-row items (lanes along K); more
+    # items than 16 per SM makes the planner order them by cost
+    torch, capi, stream = env
+    shapes = [(200, 5, 64), (64, 3, 40), (37, 8, 33)] + [(8, 8, 8)] * 3000
+    for seed in (21, 22):  # two calls in a row over the shared array
+        err, out, (a, b, gemms) = _run(env, shapes, seed)
+        assert err <= FP64_TOL
+        for m, n, k, ao, bo, co in gemms[:3] + gemms[-2:]:
+            want = a[ao:ao + m * k].reshape(m, k) @ b[bo:bo + k * n].reshape(k, n)
+            assert np.linalg.norm(out[co:co + m * n].reshape(m, n) - want) <= FP64_TOL * np.linalg.norm(want)
+
+
+def test_noalloc_drops_the_k_split_near_the_item_limit(env):
+    # 11 800 one-tile sectors plus one long-K sector: the K-split plan needs
+    # more work items than the fixed list holds (11 915), the unsplit plan fits
+    _, _, stream = env
+    shapes = [(1, 1, 1)] * 11800 + [(16, 32, 200000)]
+    err, out, (a, b, gemms) = _run(env, shapes, 31)
+    assert err <= FP64_TOL
+    m, n, k, ao, bo, co = gemms[-1]
+    want = a[ao:ao + m * k].reshape(m, k) @ b[bo:bo + k * n].reshape(k, n)
+    assert np.linalg.norm(out[co:co + m * n].reshape(m, n) - want) <= FP64_TOL * np.linalg.norm(want)
+
+
+def test_noalloc_refuses_a_capturing_stream(env):
+    # the work list comes from host memory that dies with the call, so a call
+    # on a stream under capture is refused before it issues anything, and the
+    # caller's capture is left usable
+    torch, capi, _ = env
+    gemms, na, nb, nc = _sectors([(64, 64, 64)])
+    A = torch.ones(na, dtype=torch.float64, device="cuda")
+    x = torch.arange(16, dtype=torch.float64, device="cuda")
+    y = torch.zeros(16, dtype=torch.float64, device="cuda")
+    arr = (capi.SectorGemm * 1)(capi.SectorGemm(*gemms[0]))
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    code = None
+    with torch.cuda.graph(g):
+        y.copy_(x * 2)
+        try:
+            capi.call("tn_contract_sectors_fp64_noalloc", C.c_void_p(torch.cuda.current_stream().cuda_stream), 1, arr,
+                      A.data_ptr(), A.data_ptr(), A.data_ptr())
+        except capi.TnError as e:
+            code = e.code
+    assert code == 7  # TN_ERR_UNSUPPORTED
+    x += 1
+    g.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(y, (x * 2))

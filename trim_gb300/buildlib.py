@@ -79,7 +79,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     if not os.path.isdir(libdir):
         libdir = os.path.join(CUDA, "lib")
     tmp = LIB + ".tmp"
-    link = ["g++", "-shared", "-o", tmp, *objs, "-L" + libdir, "-lcudart", "-lcusolver", "-lcublas",
+    link = ["g++", "-shared", "-o", tmp, *objs, "-L" + libdir, "-lcudart", "-lcusolver",
             "-Wl,-rpath," + libdir]
     _compile(link)
     os.replace(tmp, LIB)

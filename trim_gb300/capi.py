@@ -25,7 +25,8 @@ MODES = {"fp64": MODE_FP64, "split": MODE_SPLIT, "bf16": MODE_FAST_BF16, "tf32":
          "split_fused": MODE_SPLIT | MODE_TC_ONLY | MODE_TC_FUSED,
          "split_tiled": MODE_SPLIT | MODE_TC_ONLY | MODE_TC_TILED,
          "bf16_fused": MODE_FAST_BF16 | MODE_TC_ONLY | MODE_TC_FUSED,
-         "bf16_tiled": MODE_FAST_BF16 | MODE_TC_ONLY | MODE_TC_TILED}
+         "bf16_tiled": MODE_FAST_BF16 | MODE_TC_ONLY | MODE_TC_TILED,
+         "tf32_tc": MODE_FAST_TF32 | MODE_TC_ONLY}
 
 
 class TnError(RuntimeError):
@@ -94,6 +95,19 @@ _PROTOS = {
     "tn_tensor_device_elem": (_I, [_P, C.POINTER(_P), _I64P]),
     "tn_tensor_set_elem_device": (_I, [_P, _DP, _I64]),
     "tn_tensor_set_label": (_I, [_P, _I, _IP]),
+    "tn_tensor_put_block": (_I, [_P, _IP, _I64, _I64, _I, _DP, _I64]),
+    "tn_contract_sectors_loop": (_I, [_P, _I, _I, _P, _DP, _DP, _DP]),
+    "tn_tensor_load": (_I, [_P, C.c_char_p, _P]),
+    "tn_tensor_save": (_I, [_P, C.c_char_p]),
+    "tn_batch_create": (_I, [_I, _P, _P, _P]),
+    "tn_batch_destroy": (_I, [_P]),
+    "tn_batch_put": (_I, [_P, _I, _P, _P]),
+    "tn_batch_launch": (_I, [_P, _I]),
+    "tn_batch_capture": (_I, [_P, _I]),
+    "tn_batch_replay": (_I, [_P]),
+    "tn_batch_output": (_I, [_P, _I, _P]),
+    "tn_batch_sectors": (_I, [_P, _I, _P, _IP]),
+    "tn_tensor_is_diagonal": (_I, [_P, _IP]),
     "tn_tensor_get_labels": (_I, [_P, _IP, _IP]),
     "tn_tensor_bonds": (_I, [_P, _IP, _IP, _IP, _IP, _IP, _I]),
     "tn_tensor_sectormap": (_I, [_P, C.POINTER(_P)]),

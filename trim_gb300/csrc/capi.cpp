@@ -30,6 +30,9 @@ struct tn_tensor_s {
 struct tn_network_s {
   std::unique_ptr<uni10::Network> net;
 };
+struct tn_batch_s {
+  std::unique_ptr<uni10::Batch> batch;
+};
 
 namespace {
 
@@ -357,6 +360,21 @@ int tn_contract_sectors(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* lis
   });
 }
 
+int tn_contract_sectors_loop(tn_ctx_t ctx, int mode, int n, const tn_sector_gemm* list, const double* A,
+                             const double* B, double* C) {
+  return guard([&] {
+    if (n < 0) tn::fail(TN_ERR_ARG, "negative sector count");
+    if (n == 0) return;
+    need(list, "list");
+    tn::Ctx& c = *tn::as_ctx(ctx);
+    std::vector<tn_sector_gemm> one(1);
+    for (int i = 0; i < n; i++) {  // one GEMM launch per sector, in order
+      one[0] = list[i];
+      tn::run_sector_gemms(c, mode, one, A, B, C);
+    }
+  });
+}
+
 int tn_autotune(tn_ctx_t ctx, int on, int64_t* entries) {
   return guard([&] {
     tn::Ctx* c = tn::as_ctx(ctx);
@@ -489,7 +507,7 @@ int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n) {
     if ((size_t)n != t->t.elemNum()) tn::fail(TN_ERR_ARG, "element count does not match the tensor");
     need(host, "host");
     tn::Ctx* c = tn::default_ctx();
-    TN_CUDA(cudaMemcpyAsync(host, t->t.getElem(), n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    TN_CUDA(cudaMemcpyAsync(host, t->t.elemPtr(), n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     c->check_device_error();
   });
 }
@@ -497,7 +515,7 @@ int tn_tensor_get_elem(tn_tensor_t t, double* host, int64_t n) {
 int tn_tensor_device_elem(tn_tensor_t t, double** dev, int64_t* n) {
   return guard([&] {
     need(t, "tensor");
-    if (dev) *dev = t->t.getElem();
+    if (dev) *dev = t->t.getElem();  // writable: the tensor is no longer known to be diagonal
     if (n) *n = (int64_t)t->t.elemNum();
   });
 }
@@ -507,6 +525,44 @@ int tn_tensor_set_elem_device(tn_tensor_t t, const double* dev, int64_t n) {
     need(t, "tensor");
     if ((size_t)n != t->t.elemNum()) tn::fail(TN_ERR_ARG, "element count does not match the tensor");
     t->t.setElem(dev, true);
+  });
+}
+
+int tn_tensor_put_block(tn_tensor_t t, const int* qnum, int64_t rows, int64_t cols, int diag, const double* host,
+                        int64_t n) {
+  return guard([&] {
+    need(t, "tensor");
+    need(qnum, "qnum");
+    if (rows < 0 || cols < 0) tn::fail(TN_ERR_ARG, "negative block extent");
+    const int64_t want = diag ? std::min(rows, cols) : rows * cols;
+    if (n != want) tn::fail(TN_ERR_ARG, "element count does not match the block");
+    if (want) need(host, "host");
+    uni10::Matrix m((size_t)rows, (size_t)cols, host, diag != 0, false);
+    t->t.putBlock(uni10::Qnum((uni10::parityFType)qnum[2], qnum[0], (uni10::parityType)qnum[1]), m);
+  });
+}
+
+int tn_tensor_load(tn_ctx_t, const char* path, tn_tensor_t* out) {
+  return guard([&] {
+    need(path, "path");
+    need(out, "out");
+    *out = new tn_tensor_s{uni10::UniTensor(std::string(path))};
+  });
+}
+
+int tn_tensor_save(tn_tensor_t t, const char* path) {
+  return guard([&] {
+    need(t, "tensor");
+    need(path, "path");
+    t->t.save(std::string(path));
+  });
+}
+
+int tn_tensor_is_diagonal(tn_tensor_t t, int* diag) {
+  return guard([&] {
+    need(t, "tensor");
+    need(diag, "diag");
+    *diag = t->t.isDiagonal() ? 1 : 0;
   });
 }
 
@@ -643,6 +699,82 @@ int tn_contract_batch(int n, const tn_tensor_t* a, const tn_tensor_t* b, int mod
     ModeScope ms(mode);
     std::vector<uni10::UniTensor> r = uni10::contract_batch(A, B);
     for (int i = 0; i < n; i++) out[i] = new tn_tensor_s{std::move(r[i])};
+  });
+}
+
+int tn_batch_create(int n, const tn_tensor_t* a, const tn_tensor_t* b, tn_batch_t* out) {
+  return guard([&] {
+    if (n <= 0) tn::fail(TN_ERR_ARG, "a batch needs at least one pair");
+    need(a, "a");
+    need(b, "b");
+    need(out, "out");
+    std::vector<const uni10::UniTensor*> A(n), B(n);
+    for (int i = 0; i < n; i++) {
+      need(a[i], "a[i]");
+      need(b[i], "b[i]");
+      A[i] = &a[i]->t;
+      B[i] = &b[i]->t;
+    }
+    auto bt = std::make_unique<tn_batch_s>();
+    bt->batch = std::make_unique<uni10::Batch>(A, B);
+    *out = bt.release();
+  });
+}
+
+int tn_batch_destroy(tn_batch_t b) {
+  return guard([&] { delete b; });
+}
+
+int tn_batch_put(tn_batch_t b, int i, tn_tensor_t ta, tn_tensor_t tb) {
+  return guard([&] {
+    need(b, "batch");
+    need(ta, "a");
+    need(tb, "b");
+    if (i < 0) tn::fail(TN_ERR_ARG, "negative pair index");
+    b->batch->putTensors((size_t)i, ta->t, tb->t);
+  });
+}
+
+int tn_batch_launch(tn_batch_t b, int mode) {
+  return guard([&] {
+    need(b, "batch");
+    ModeScope ms(mode);
+    b->batch->launch();
+  });
+}
+
+int tn_batch_capture(tn_batch_t b, int mode) {
+  return guard([&] {
+    need(b, "batch");
+    ModeScope ms(mode);
+    b->batch->capture();
+  });
+}
+
+int tn_batch_replay(tn_batch_t b) {
+  return guard([&] {
+    need(b, "batch");
+    b->batch->replay();
+  });
+}
+
+int tn_batch_output(tn_batch_t b, int i, tn_tensor_t* out) {
+  return guard([&] {
+    need(b, "batch");
+    need(out, "out");
+    if (i < 0 || (size_t)i >= b->batch->size()) tn::fail(TN_ERR_ARG, "pair index out of range");
+    *out = new tn_tensor_s{uni10::UniTensor::alias(b->batch->output((size_t)i))};
+  });
+}
+
+int tn_batch_sectors(tn_batch_t b, int cap, tn_sector_gemm* list, int* n) {
+  return guard([&] {
+    need(b, "batch");
+    need(n, "n");
+    const auto& all = b->batch->sectors();
+    *n = (int)all.size();
+    if (list)
+      for (int i = 0; i < cap && (size_t)i < all.size(); i++) list[i] = all[i];
   });
 }
 

@@ -245,6 +245,12 @@ struct TruncSector {
   int64_t uo_off, so_off, vo_off;   // compact outputs (S as a kept x kept block)
 };
 
+// Entries a context keeps in each device work-list cache before it starts
+// over (a per-sector loop over a large batch plans thousands of one-sector
+// lists; a cache that cleared itself within one such loop would replan them
+// on every call).
+constexpr size_t kPlanCacheCap = 1u << 15;
+
 // ---------------------------------------------------------------- context
 // Per-kernel timing with CUDA events on the context's stream (enabled on
 // demand; used by bench.py for the roofline of the dominant kernel).
@@ -409,6 +415,22 @@ void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems
 void launch_tc_reduce(const TcSector* secs, const int4* ritems, int nred, const double* part, double* C, int grid,
                       cudaStream_t s);
 void launch_scale(double* p, int64_t n, double a, cudaStream_t s);
+
+// A rows x cols piece of a product with a diagonal factor (RDotR's
+// diagRowMul / diagColMul, data-structure/lib/BlockTools.cpp:45-60):
+// C[dst + r*dst_ld + c] = lam[r] * X[src + r*src_ld + c] (side 0) or
+// X[...] * lam[c] (side 1), lam[i] = D[lam + i*lam_stride]; rows (columns)
+// i >= nlam are written as zero without reading X.
+struct DiagItem {
+  int64_t src, dst, lam;
+  int32_t rows, cols, src_ld, dst_ld;
+  int32_t lam_stride, nlam, side, pad;
+};
+void launch_diag_scale(const DiagItem* items, int n, const double* X, const double* D, double* C, int grid,
+                       cudaStream_t s);
+// all pieces in one launch (cut to CTA-sized pieces; the device list cached
+// on the context by content)
+void run_diag_scale(Ctx& ctx, const std::vector<DiagItem>& pieces, const double* X, const double* D, double* C);
 
 // SVD (Block::svd per sector) and truncation
 struct SvdGeom {

@@ -195,7 +195,7 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
     ctx.launched(2);
   }
   {
-    ProfScope ps(ctx, ns == 7 ? "tc_gemm_split" : "tc_gemm_bf16", 0, P->flops);
+    ProfScope ps(ctx, ns == 7 ? "tc_gemm_split" : (ns == 2 ? "tc_gemm_tf32" : "tc_gemm_bf16"), 0, P->flops);
     int grid = (int)std::min<int64_t>((int64_t)P->nitems, (int64_t)ctx.num_sms);
     launch_tc_gemm(ns, dsecs, (const int4*)(mb + P->off_it), P->nitems, images, ea, eb, C, part, err, grid,
                    ctx.stream);

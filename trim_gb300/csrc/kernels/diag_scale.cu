@@ -1,0 +1,120 @@
+// Products with a diagonal factor as row or column scales: the diagonal paths
+// of RDotR (data-structure/lib/BlockTools.cpp:45-60: diagRowMul / diagColMul,
+// GPU _diagRowMul in numeric/lapack/lib/uni10_lapack_gpu.cu:305-325), applied
+// to every block of a contraction in one launch.  A piece is a rows x cols
+// rectangle of the output: dst[r, c] = lam[r] * src[r, c] (side 0) or
+// src[r, c] * lam[c] (side 1); rows (columns) at or beyond nlam are written as
+// zero and their source is not read (the reference resizes the product to the
+// diagonal factor's extent, which pads with zeros).  On finite values the
+// result is bit-identical to the dense product: a sum with one non-zero term,
+// rounded once.  HBM/latency bound: 16 bytes moved per element.
+#include <algorithm>
+#include <cstring>
+
+#include "../engine/engine.h"
+
+namespace tn {
+namespace {
+
+__global__ void __launch_bounds__(256) diag_scale_kernel(const DiagItem* __restrict__ items, int n,
+                                                         const double* __restrict__ X, const double* __restrict__ D,
+                                                         double* __restrict__ C) {
+  for (int it = blockIdx.x; it < n; it += gridDim.x) {
+    const DiagItem t = items[it];
+    const int64_t total = (int64_t)t.rows * t.cols;
+    for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
+      const int r = (int)(e / t.cols), c = (int)(e - (int64_t)r * t.cols);
+      const int li = t.side ? c : r;
+      double v = 0.0;
+      if (li < t.nlam) v = D[t.lam + (int64_t)li * t.lam_stride] * X[t.src + (int64_t)r * t.src_ld + c];
+      C[t.dst + (int64_t)r * t.dst_ld + c] = v;
+    }
+  }
+}
+
+struct DiagPlan {
+  std::vector<DiagItem> items;
+  DevBufP dev;
+  double bytes = 0;
+};
+
+uint64_t hash_items(const std::vector<DiagItem>& v) {
+  uint64_t h = 1469598103934665603ull;
+  const unsigned char* p = (const unsigned char*)v.data();
+  for (size_t i = 0; i < v.size() * sizeof(DiagItem); i++) h = (h ^ p[i]) * 1099511628211ull;
+  return h ^ 0xD1A6ull;
+}
+
+}  // namespace
+
+void launch_diag_scale(const DiagItem* items, int n, const double* X, const double* D, double* C, int grid,
+                       cudaStream_t s) {
+  if (n <= 0) return;
+  diag_scale_kernel<<<grid, 256, 0, s>>>(items, n, X, D, C);
+  TN_CUDA(cudaGetLastError());
+}
+
+// Pieces are cut to at most kDiagPiece elements (whole rows) so that one CTA
+// takes one piece; the device copy of a piece list is cached on the context.
+void run_diag_scale(Ctx& ctx, const std::vector<DiagItem>& pieces, const double* X, const double* D, double* C) {
+  constexpr int64_t kDiagPiece = 8192;
+  std::vector<DiagItem> items;
+  for (const DiagItem& p0 : pieces) {
+    if (p0.rows <= 0 || p0.cols <= 0) continue;
+    // long rows: column chunks first
+    for (int c0 = 0; c0 < p0.cols; c0 += (int)kDiagPiece) {
+      DiagItem p = p0;
+      p.cols = (int)std::min<int64_t>(kDiagPiece, p0.cols - c0);
+      p.src = p0.src + c0;
+      p.dst = p0.dst + c0;
+      if (p0.side == 1) {
+        p.lam = p0.lam + (int64_t)c0 * p0.lam_stride;
+        p.nlam = std::max(0, p0.nlam - c0);
+      }
+      const int rows_per = (int)std::max<int64_t>(1, kDiagPiece / p.cols);
+      for (int r0 = 0; r0 < p.rows; r0 += rows_per) {
+        DiagItem q = p;
+        q.rows = std::min(rows_per, p.rows - r0);
+        q.src = p.src + (int64_t)r0 * p.src_ld;
+        q.dst = p.dst + (int64_t)r0 * p.dst_ld;
+        if (p.side == 0) {
+          q.lam = p.lam + (int64_t)r0 * p.lam_stride;
+          q.nlam = std::max(0, p.nlam - r0);
+        }
+        items.push_back(q);
+      }
+    }
+  }
+  if (items.empty()) return;
+  const uint64_t key = hash_items(items);
+  std::shared_ptr<DiagPlan> P;
+  {
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    auto it = ctx.gemm_cache.find(key);
+    if (it != ctx.gemm_cache.end()) {
+      auto Q = std::static_pointer_cast<DiagPlan>(it->second);
+      if (Q->items.size() == items.size() &&
+          std::memcmp(Q->items.data(), items.data(), items.size() * sizeof(DiagItem)) == 0)
+        P = Q;
+    }
+  }
+  if (!P) {
+    P = std::make_shared<DiagPlan>();
+    P->items = items;
+    for (const auto& t : items) P->bytes += 16.0 * t.rows * t.cols;
+    P->dev = std::make_shared<DevBuf>(items.size() * sizeof(DiagItem), ctx);
+    TN_CUDA(cudaMemcpyAsync(P->dev->ptr, items.data(), items.size() * sizeof(DiagItem), cudaMemcpyHostToDevice,
+                            ctx.stream));
+    TN_CUDA(cudaStreamSynchronize(ctx.stream));  // the host copy dies here
+    std::lock_guard<std::mutex> lk(ctx.mu);
+    if (ctx.gemm_cache.size() > kPlanCacheCap) ctx.gemm_cache.clear();
+    ctx.gemm_cache[key] = P;
+  }
+  ctx.keep_alive(P);
+  const int grid = (int)std::min<int64_t>((int64_t)items.size(), (int64_t)ctx.num_sms * 8);
+  ProfScope ps(ctx, "diag_scale", P->bytes, 0.0);
+  launch_diag_scale((const DiagItem*)P->dev->ptr, (int)items.size(), X, D, C, grid, ctx.stream);
+  ctx.launched();
+}
+
+}  // namespace tn

@@ -8,8 +8,12 @@
 // when it splits K, a workspace for the partial tiles.  Here both live in one
 // file-scope device array of fixed size, TN_NOALLOC_SCRATCH_BYTES, which every
 // GPU that loads this library holds until the process exits:
-//   [0, 1 MiB)        the tile list (GemmTile records)
-//   [1 MiB, 8 MiB)    split-K partial tiles (16x32 doubles each)
+//   [0, 1 MiB)        the work list: 11 915 GemmTile records of 88 bytes (an
+//                     output tile over a K range, or 16 rows of a narrow sector)
+//   [1 MiB, 8 MiB)    split-K partial tiles (512 doubles each)
+// When the K-split plan needs more work items than the list holds, the call is
+// planned again without splitting K; only work that still needs more items
+// than that is rejected.
 // The caller still owns and passes A, B and C.  Nothing here calls cudaMalloc,
 // cudaFree or any allocating library routine.
 //
@@ -17,6 +21,12 @@
 // is only a stand-in symbol), so the address is looked up once per device
 // with cudaGetSymbolAddress, with that device current, on the first call made
 // on it.  Make that first call before any stream capture.
+//
+// The work list is planned on the host and copied from pageable host memory,
+// so each call returns only after the stream's earlier work has completed.
+// For the same reason a call on a stream that is being captured into a CUDA
+// graph is refused (TN_ERR_UNSUPPORTED) before anything is issued, which
+// leaves the caller's capture intact.
 //
 // All calls share the array and it keeps the last call's contents.  Nothing
 // in it has to start at zero: a call uploads its whole tile list, and every
@@ -33,6 +43,7 @@ namespace {
 constexpr size_t kTileRegion = 1u << 20;
 constexpr size_t kScratch = TN_NOALLOC_SCRATCH_BYTES;
 constexpr int kMaxDevices = 64;
+static_assert(sizeof(GemmTile) == 88, "the work-list capacity stated for the fixed scratch assumes 88-byte records");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratch];
 
@@ -58,6 +69,15 @@ void* scratch_address(int dev) {
 
 void contract_sectors_fp64_noalloc(cudaStream_t stream, const std::vector<tn_sector_gemm>& list, const double* A,
                                    const double* B, double* C) {
+  {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const cudaError_t e = cudaStreamIsCapturing(stream, &cs);
+    if (e != cudaSuccess) cudaGetLastError();
+    if (e != cudaSuccess || cs != cudaStreamCaptureStatusNone)
+      fail(TN_ERR_UNSUPPORTED,
+           "tn_contract_sectors_fp64_noalloc: the stream is being captured; the work list is copied from host memory "
+           "that does not outlive the call, so the call issues nothing");
+  }
   int dev = 0;
   TN_CUDA(cudaGetDevice(&dev));
   int sms = 0;
@@ -66,9 +86,10 @@ void contract_sectors_fp64_noalloc(cudaStream_t stream, const std::vector<tn_sec
   const int64_t ws_cap = (int64_t)((kScratch - kTileRegion) / sizeof(double));
   int64_t ws_elems = 0;
   std::vector<GemmTile> tiles = plan_fp64(list, sms, ws_cap, &ws_elems);
+  if ((int64_t)tiles.size() > max_tiles) tiles = plan_fp64(list, sms, 0, &ws_elems);  // K unsplit: fewer items
   if ((int64_t)tiles.size() > max_tiles)
     fail(TN_ERR_ARG, "tn_contract_sectors_fp64_noalloc: the sector GEMMs need " + std::to_string(tiles.size()) +
-                         " output tiles of 16x32, more than the fixed scratch holds (" + std::to_string(max_tiles) +
+                         " work items, more than the fixed scratch holds (" + std::to_string(max_tiles) +
                          "); use tn_contract_sectors");
   if (tiles.empty()) return;
   unsigned char* base = (unsigned char*)scratch_address(dev);

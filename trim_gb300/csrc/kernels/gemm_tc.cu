@@ -23,6 +23,12 @@
 // 48 clocks for 32 of work).
 // Fast BF16 (TN_MODE_FAST_BF16): one slice, the BF16 rounding of each scaled
 // element, FP32 accumulation over the whole K.
+// Fast TF32 (TN_MODE_FAST_TF32, NS = 2 below): the TF32 rounding of each
+// scaled element; a 64-k tile of 4-byte operands is two 128-byte swizzle
+// atoms, stored as two 16 KB (A) / 8 KB (B) images (k 0..31, then 32..63),
+// so the copies run as for two slices; the MMAs are kind::tf32 (K = 8 per
+// instruction, the same 32 bytes per row as kind::f16), FP32 accumulation
+// over the whole K.
 //
 // Layout: operand tiles are written by the slicing kernels as exact images of
 // the tcgen05 shared-memory operand layout (K-major, 128-byte swizzle), so the
@@ -144,6 +150,26 @@ __global__ void __launch_bounds__(256) tc_maxima(const TcSector* __restrict__ se
   }
 }
 
+// 8 consecutive k (chunk c of a 64-k tile) of image row r: the NS digit
+// slices (split, BF16 fast) at chunk c of every image, or (TF32, NS = 2) the
+// two 16-byte halves at chunks 2 (c & 3) and 2 (c & 3) + 1 of image c >> 2
+template <int NS>
+__device__ __forceinline__ void store_chunk(uint8_t* img, int img_bytes, int r, int c, const double (&x)[8], int e) {
+  if constexpr (NS == 2) {
+    uint4 o[2];
+    make_tf32(x, e, o);
+    uint8_t* at = img + (int64_t)(c >> 2) * img_bytes;
+    *(uint4*)(at + swz_off(r, 2 * (c & 3))) = o[0];
+    *(uint4*)(at + swz_off(r, 2 * (c & 3) + 1)) = o[1];
+  } else {
+    uint4 o[NS];
+    make_slices<NS>(x, e, o);
+    const uint32_t off = swz_off(r, c);
+#pragma unroll
+    for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * img_bytes + off) = o[s];
+  }
+}
+
 // A tile t: (sector, mt, kt) -> NS images of 128 rows x 64 k
 template <int NS>
 __device__ __forceinline__ void slice_a_tile(const TcSector* __restrict__ secs, const int64_t* __restrict__ tstart,
@@ -170,11 +196,7 @@ __device__ __forceinline__ void slice_a_tile(const TcSector* __restrict__ secs, 
 #pragma unroll
         for (int q = 0; q < 8; q++) x[q] = 0.0;
       }
-      uint4 o[NS];
-      make_slices<NS>(x, e, o);
-      const uint32_t off = swz_off(r, c);
-#pragma unroll
-      for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * kATile + off) = o[s];
+      store_chunk<NS>(img, kATile, r, c, x, e);
     }
   }
 }
@@ -212,11 +234,7 @@ __device__ __forceinline__ void slice_b_tile(const TcSector* __restrict__ secs, 
     double x[8];
 #pragma unroll
     for (int q = 0; q < 8; q++) x[q] = stage[c * 8 + q][r];
-    uint4 o[NS];
-    make_slices<NS>(x, e, o);
-    const uint32_t off = swz_off(r, c);
-#pragma unroll
-    for (int s = 0; s < NS; s++) *(uint4*)(img + (int64_t)s * kBTile + off) = o[s];
+    store_chunk<NS>(img, kBTile, r, c, x, e);
   }
 }
 
@@ -264,8 +282,9 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
                                                          const unsigned long long* __restrict__ eb,
                                                          double* __restrict__ C, double* __restrict__ part,
                                                          int* __restrict__ err) {
-  constexpr int LV = (NS == 1) ? 1 : kLevels;
-  constexpr int kChunk = (NS == 1) ? 1 << 20 : kChunkTiles;  // fast mode: one chunk over all of K
+  constexpr bool kFast = NS != 7;  // BF16 (NS = 1) or TF32 (NS = 2): one FP32 accumulator
+  constexpr int LV = kFast ? 1 : kLevels;
+  constexpr int kChunk = kFast ? 1 << 20 : kChunkTiles;  // fast modes: one chunk over all of K
   extern __shared__ uint8_t dyn[];
   __shared__ TcShared sh;
   // 1024-byte aligned operand buffers (the swizzle is anchored to 1024 B)
@@ -367,6 +386,20 @@ __global__ void __launch_bounds__(kThreadsTc, 1) tc_gemm(const TcSector* __restr
             }
             tc_fence_after();
             const uint64_t adesc = desc_sw128(smem_u32(abuf + sa * kATile));
+            if constexpr (NS == 2) {
+              // TF32: image s holds k 32 s .. 32 s + 31 of A and of B; steps of 8 k
+              const int kdat = S.K - kt * kTK - 32 * s;  // k of this image holding data
+              const int nk8 = kdat <= 0 ? 0 : min(4, (kdat + 7) >> 3);
+              const uint64_t bdesc = desc_sw128(b_addr + s * kBTile);
+              const uint32_t idesc = idesc_tf32_f32(kTM, kTN);
+              for (int kk = 0; kk < nk8; kk++) {
+                mma_tf32_elect(tmem, adesc + 2 * kk, bdesc + 2 * kk, idesc, (touched | kk) ? 1u : 0u);
+                touched = 1;
+              }
+              mma_commit_elect(&sh.emptyA[sa]);
+              na++;
+              continue;
+            }
             // B digits t = 0 .. T-1 pair with A digit s (s + t <= 7), in
             // groups of at most 4 (7 -> 4 + 3, 6 -> 3 + 3, 5 -> 3 + 2)
             const int T = NS == 1 ? 1 : min(NS, kMaxLevel + 1 - s);
@@ -500,6 +533,8 @@ void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts,
   int g2 = (int)std::min<int64_t>(a_tiles + b_tiles, (int64_t)num_sms * 8);
   if (ns == 7)
     tc_slices<7><<<g2, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax, images);
+  else if (ns == 2)
+    tc_slices<2><<<g2, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax, images);
   else
     tc_slices<1><<<g2, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax, images);
   TN_CUDA(cudaGetLastError());
@@ -518,6 +553,13 @@ void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems,
       attr = true;
     }
     tc_gemm<7><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, part, err);
+  } else if (ns == 2) {
+    static bool attr = false;
+    if (!attr) {
+      TN_CUDA(cudaFuncSetAttribute(tc_gemm<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      attr = true;
+    }
+    tc_gemm<2><<<grid, kThreadsTc, smem, s>>>(secs, items, nitems, ws, ea, eb, C, part, err);
   } else {
     static bool attr = false;
     if (!attr) {

@@ -87,6 +87,29 @@ __device__ __forceinline__ void make_slices(const double (&x)[8], int e, uint4 (
                         __byte_perm(hbits[s][4], hbits[s][5], 0x7632), __byte_perm(hbits[s][6], hbits[s][7], 0x7632));
 }
 
+// TF32 fast mode: 8 consecutive-k values of one row as TF32 patterns of
+// x * 2^(7 - e) (FP32 with the 13 low mantissa bits rounded off, to nearest,
+// ties away from zero), packed as two 16-byte chunks.  The scaling is done on
+// the exponent field as in the BF16 fast mode.
+__device__ __forceinline__ void make_tf32(const double (&x)[8], int e, uint4 (&out)[2]) {
+  uint32_t w[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const uint64_t bits = (uint64_t)__double_as_longlong(x[i]);
+    const int ef = (int)((bits >> 52) & 0x7FF);
+    const int nex = ef + 7 - e;
+    float f;
+    if (ef != 0 && nex >= 1 && nex <= 2046)
+      f = __double2float_rn(__longlong_as_double((long long)((bits & ~(0x7FFull << 52)) | ((uint64_t)nex << 52))));
+    else
+      f = (float)ldexp(x[i], 7 - e);  // zero, subnormal or far below the row's scale
+    const uint32_t u = __float_as_uint(f);
+    w[i] = ((u & 0x7F800000u) == 0x7F800000u) ? u : ((u + 0x1000u) & 0xFFFFE000u);
+  }
+  out[0] = make_uint4(w[0], w[1], w[2], w[3]);
+  out[1] = make_uint4(w[4], w[5], w[6], w[7]);
+}
+
 // S * 2^q as the nearest double (ties to even), integer operations only (the
 // FP64 units and FP64 conversions run at ~2 per clock per SM on GB300)
 __device__ __forceinline__ double fixed_to_double(long long S, int q) {

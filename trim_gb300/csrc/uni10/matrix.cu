@@ -2,6 +2,7 @@
 // SVD truncation of an iTEBD step use (data-structure/lib/Block.cpp,
 // BlockReal.cpp:226-250; tensor-network/lib/MatrixReal.cpp:289-360).
 #include <cmath>
+#include <cstring>
 #include <sstream>
 #include <stdexcept>
 
@@ -116,23 +117,48 @@ Matrix& Matrix::operator*=(double a) {
   return *this;
 }
 
-// dense product through the grouped sector GEMM (one sector)
+// RDotR (data-structure/lib/BlockTools.cpp:38-75): the dense product through
+// the grouped sector GEMM (one sector); with a diagonal factor a row scale
+// (diagRowMul), a column scale (diagColMul) or, both diagonal, the product of
+// the diagonals (vectorMul over the shorter one) -- O(M N), no GEMM.
 Matrix operator*(const Block& a, const Block& b) {
   if (a.col() != b.row()) throw std::runtime_error("The dimensions of the two matrices do not match for matrix multiplication.");
   if (a.isDiag() || b.isDiag()) {
-    Matrix da(a.row(), a.col()), db(b.row(), b.col());
-    auto expand = [](const Block& s, Matrix& d) {
-      if (!s.isDiag()) {
-        TN_CUDA(cudaMemcpyAsync(d.getElem(), s.getElem(), s.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
-                                C().stream));
-        return;
+    tn::DiagItem t;
+    std::memset(&t, 0, sizeof(t));
+    t.lam_stride = 1;
+    if (a.isDiag() && b.isDiag()) {
+      Matrix c(a.row(), b.col(), true);  // zero-filled
+      const size_t n = std::min(std::min(a.elemNum(), b.elemNum()), c.elemNum());
+      if (n) {
+        t.rows = 1;
+        t.cols = (int32_t)n;
+        t.src_ld = t.dst_ld = (int32_t)n;
+        t.nlam = (int32_t)n;
+        t.side = 1;
+        tn::run_diag_scale(C(), std::vector<tn::DiagItem>{t}, a.getElem(), b.getElem(), c.getElem());
       }
-      TN_CUDA(cudaMemcpy2DAsync(d.getElem(), (s.col() + 1) * sizeof(double), s.getElem(), sizeof(double),
-                                sizeof(double), s.elemNum(), cudaMemcpyDeviceToDevice, C().stream));
-    };
-    expand(a, da);
-    expand(b, db);
-    return da * db;
+      return c;
+    }
+    Matrix c(a.row(), b.col());
+    if (c.elemNum() == 0) return c;
+    if ((int64_t)c.row() >= INT32_MAX || (int64_t)c.col() >= INT32_MAX || (int64_t)a.col() >= INT32_MAX)
+      throw std::runtime_error("matrix product with a diagonal factor: extent too large");
+    t.rows = (int32_t)c.row();
+    t.cols = (int32_t)c.col();
+    t.dst_ld = (int32_t)c.col();
+    if (a.isDiag()) {  // c[r, :] = a[r] b[r, :] for r < a's diagonal length, zero beyond
+      t.src_ld = (int32_t)b.col();
+      t.nlam = (int32_t)a.elemNum();
+      t.side = 0;
+      tn::run_diag_scale(C(), std::vector<tn::DiagItem>{t}, b.getElem(), a.getElem(), c.getElem());
+    } else {  // c[:, j] = a[:, j] b[j] for j < b's diagonal length, zero beyond
+      t.src_ld = (int32_t)a.col();
+      t.nlam = (int32_t)b.elemNum();
+      t.side = 1;
+      tn::run_diag_scale(C(), std::vector<tn::DiagItem>{t}, a.getElem(), b.getElem(), c.getElem());
+    }
+    return c;
   }
   Matrix c(a.row(), b.col());
   std::vector<tn_sector_gemm> list(1);

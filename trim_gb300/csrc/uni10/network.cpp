@@ -584,7 +584,7 @@ void Network::capture() {
         direct = false;
         continue;
       }
-      in.dst[in.count] = t->getElem();
+      in.dst[in.count] = const_cast<double*>(t->elemPtr());
       in.src[in.count] = hp;
       in.n[in.count] = (int64_t)host_in_n[i];
       in.count++;
@@ -594,7 +594,7 @@ void Network::capture() {
       c.launched();
     } else {
       for (size_t i = 0; i < host_in.size(); i++)
-        TN_CUDA(cudaMemcpyAsync(tensors[host_in[i].first]->getElem(), host_in[i].second, host_in_n[i] * sizeof(double),
+        TN_CUDA(cudaMemcpyAsync(const_cast<double*>(tensors[host_in[i].first]->elemPtr()), host_in[i].second, host_in_n[i] * sizeof(double),
                                 cudaMemcpyHostToDevice, cap));
     }
     UniTensor r = launch();
@@ -605,13 +605,13 @@ void Network::capture() {
       tn::CopyList out{};
       out.dst[0] = graph_out.getElem();
       out.dst[1] = const_cast<double*>(hout);
-      out.src[0] = out.src[1] = r.getElem();
+      out.src[0] = out.src[1] = r.elemPtr();
       out.n[0] = out.n[1] = (int64_t)r.elemNum();
       out.count = 2;
       tn::launch_copy_list(out, c.num_sms * 4, cap);
       c.launched();
     } else {
-      TN_CUDA(cudaMemcpyAsync(graph_out.getElem(), r.getElem(), r.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
+      TN_CUDA(cudaMemcpyAsync(graph_out.getElem(), r.elemPtr(), r.elemNum() * sizeof(double), cudaMemcpyDeviceToDevice,
                               cap));
       if (host_out)
         TN_CUDA(cudaMemcpyAsync(host_out, graph_out.getElem(), host_out_n * sizeof(double), cudaMemcpyDeviceToHost, cap));

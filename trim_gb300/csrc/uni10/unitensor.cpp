@@ -12,6 +12,7 @@
 
 #include "../../../include/uni10/UniTensor.h"
 #include "../engine/engine.h"
+#include "contract_work.h"
 
 namespace uni10 {
 
@@ -108,7 +109,7 @@ void UniTensor::initUniT(bool zero) {
 
 UniTensor::UniTensor(const UniTensor& o)
     : name(o.name), bonds(o.bonds), labels(o.labels), RBondNum(o.RBondNum), m_elemNum(o.m_elemNum), status(o.status),
-      smap(o.smap) {
+      smap(o.smap), diag_(o.diag_) {
   if (o.elem) {
     elem = alloc_elem(m_elemNum);
     TN_CUDA(cudaMemcpyAsync(dptr(elem), dptr(o.elem), m_elemNum * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
@@ -124,6 +125,7 @@ UniTensor& UniTensor::operator=(const UniTensor& o) {
   m_elemNum = o.m_elemNum;
   status = o.status;
   smap = o.smap;
+  diag_ = o.diag_;
   if (o.elem) {
     if (!elem || elem->bytes < m_elemNum * sizeof(double)) elem = alloc_elem(m_elemNum);
     TN_CUDA(cudaMemcpyAsync(dptr(elem), dptr(o.elem), m_elemNum * sizeof(double), cudaMemcpyDeviceToDevice, C().stream));
@@ -143,12 +145,14 @@ void UniTensor::setElem(const double* e, bool _ongpu) {
                           _ongpu ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c.stream));
   if (!_ongpu) TN_CUDA(cudaStreamSynchronize(c.stream));  // the caller may reuse its buffer at once
   status |= HAVEELEM;
+  diag_ = false;
 }
 
 void UniTensor::setElemAsync(const double* host) {
   if (!elem) throw std::runtime_error("Setting elements to an empty tensor is not supported.");
   TN_CUDA(cudaMemcpyAsync(dptr(elem), host, m_elemNum * sizeof(double), cudaMemcpyHostToDevice, C().stream));
   status |= HAVEELEM;
+  diag_ = false;
 }
 
 void UniTensor::setElem(const std::vector<double>& e, bool _ongpu) {
@@ -160,7 +164,14 @@ void UniTensor::setElem(const std::vector<double>& e, bool _ongpu) {
   setElem(e.data(), _ongpu);
 }
 
-double* UniTensor::getElem() { return dptr(elem); }
+// the caller may write through the device pointer: the tensor is no longer
+// known to be diagonal
+double* UniTensor::getElem() {
+  diag_ = false;
+  return dptr(elem);
+}
+
+const double* UniTensor::elemPtr() const { return dptr(elem); }
 
 std::vector<double> UniTensor::hostElem() const {
   std::vector<double> h(m_elemNum);
@@ -186,6 +197,7 @@ double UniTensor::at(size_t idx) const {
 void UniTensor::set_zero() {
   if (elem) TN_CUDA(cudaMemsetAsync(dptr(elem), 0, m_elemNum * sizeof(double), C().stream));
   status |= HAVEELEM;
+  diag_ = bonds.size() == 2 && RBondNum == 1;  // all zero: diagonal
 }
 
 // dense raw layout <-> blocks (UniTensorReal.cpp:96-174, 241-280): the raw
@@ -332,6 +344,12 @@ void UniTensor::putBlock(const Qnum& q, const Block& mat) {
   }
   double* dst = dptr(elem) + (smap ? smap->blocks[bi].off : 0);
   tn::Ctx& cx = C();
+  // a diagonal tensor stays one while only diagonal blocks are put into it
+  // after creation (zero-filled) or set_zero
+  if (!mat.isDiag())
+    diag_ = false;
+  else if (!(status & HAVEELEM) || diag_)
+    diag_ = bonds.size() == 2 && RBondNum == 1;
   if (mat.isDiag()) {
     TN_CUDA(cudaMemsetAsync(dst, 0, r * c * sizeof(double), cx.stream));
     size_t n = mat.elemNum();
@@ -354,6 +372,7 @@ UniTensor UniTensor::alias(const UniTensor& t) {
   a.status = t.status;
   a.smap = t.smap;
   a.elem = t.elem;  // shared buffer
+  a.diag_ = t.diag_;
   return a;
 }
 
@@ -396,6 +415,8 @@ UniTensor UniTensor::permuted(const UniTensor& src, const std::vector<int>& newL
     out.status |= HAVEELEM;
   }
   out.labels = newLabels;
+  // a diagonal tensor permuted to (column | row) is block-wise transposed
+  out.diag_ = src.diag_ && n == 2 && rowBondNum == 1;
   return out;
 }
 
@@ -493,6 +514,7 @@ UniTensor& UniTensor::combineBond(const std::vector<int>& cmbLabels) {
     }
   }
   permute(rsp_labels, RBnum);
+  diag_ = false;
   UniTensor out(newBonds, reduced, name);
   if (out.m_elemNum != m_elemNum) throw std::runtime_error("combineBond: element counts differ");
   bonds = std::move(out.bonds);
@@ -566,6 +588,119 @@ static PermShape permuted_shape(const UniTensor& src, const std::vector<int>& ne
   for (int j = 0; j < n; j++) p.bonds[j].change(j < rowBondNum ? BD_IN : BD_OUT);
   p.smap = tn::get_sectormap(to_sigs(p.bonds));  // cached per signature
   return p;
+}
+
+// One contraction with a diagonal operand (see contract_diag).
+struct UniTensor::DiagCall {
+  UniTensor* Ta;
+  UniTensor* Tb;
+  bool d_is_a;  // the diagonal operand is Ta (a row scale) or Tb (a column scale)
+  const PermShape* sa;
+  const PermShape* sb;
+  const std::vector<int>* newLabelA;
+  const std::vector<int>* newLabelB;
+  int conBond;
+  const std::vector<tn_sector_gemm>* list;
+  const std::vector<int>* a_blk;
+  const std::vector<int>* b_blk;
+  UniTensor* Tc;
+  bool fast, mutate;
+};
+
+// Ta . Tb where one operand D is a diagonal tensor (isDiagonal()) and one bond
+// is contracted: every sector product C_q = D_q . X_q (X_q . D_q) is a row
+// (column) scale of X_q -- the diagonal paths of RDotR, diagRowMul /
+// diagColMul (data-structure/lib/BlockTools.cpp:45-60), over all blocks in one
+// launch.  X is read through views of its unpermuted source where its
+// permute allows and the operands are left as they were; otherwise it is
+// permuted first (in place when contract() mutates its operands, as the
+// reference does).  Returns false (nothing done) when a piece exceeds the
+// kernel's 32-bit extents; the caller then takes the sector GEMMs.
+bool UniTensor::contract_diag(const DiagCall& d) {
+  tn::Ctx& c = C();
+  UniTensor& D = d.d_is_a ? *d.Ta : *d.Tb;
+  UniTensor& X = d.d_is_a ? *d.Tb : *d.Ta;
+  const PermShape& sd = d.d_is_a ? *d.sa : *d.sb;
+  const PermShape& sx = d.d_is_a ? *d.sb : *d.sa;
+  const std::vector<int>& labD = d.d_is_a ? *d.newLabelA : *d.newLabelB;
+  const std::vector<int>& labX = d.d_is_a ? *d.newLabelB : *d.newLabelA;
+  const int rD = 1;  // (kept | contracted) or (contracted | kept)
+  const int rX = d.d_is_a ? d.conBond : (int)X.bonds.size() - d.conBond;
+  const auto& list = *d.list;
+  const tn::SectorMap* md = sd.smap.get();
+  const tn::SectorMap* mx = sx.smap.get();
+  bool square = true, fits = true;
+  for (size_t i = 0; i < list.size(); i++) {
+    const auto& bd = md->blocks[d.d_is_a ? (*d.a_blk)[i] : (*d.b_blk)[i]];
+    const auto& bx = mx->blocks[d.d_is_a ? (*d.b_blk)[i] : (*d.a_blk)[i]];
+    square &= bd.rows == bd.cols;
+    fits &= list[i].M < INT32_MAX && list[i].N < INT32_MAX && bx.cols < INT32_MAX && bd.cols + 1 < INT32_MAX;
+  }
+  if (!fits) return false;
+  UniTensor dp, xp;
+  const double* Dp = dptr(D.elem);
+  if (sd.moves) {
+    if (d.mutate) {
+      D.permute(labD, rD);
+      Dp = dptr(D.elem);
+    } else {
+      dp = permuted(D, labD, rD);
+      Dp = dptr(dp.elem);
+    }
+  }
+  tn::OpViewsP vx;
+  if (sx.moves && (!d.mutate || !d.fast) && square) {
+    vx = tn::get_op_views(c, *X.smap, *sx.smap, sx.rsp);
+    if (vx && !vx->ok) vx.reset();
+  }
+  const double* Xp = dptr(X.elem);
+  if (sx.moves && !vx) {
+    if (d.mutate) {
+      X.permute(labX, rX);
+      Xp = dptr(X.elem);
+    } else {
+      xp = permuted(X, labX, rX);
+      Xp = dptr(xp.elem);
+    }
+  }
+  const int side = d.d_is_a ? 0 : 1;
+  std::vector<tn::DiagItem> pieces;
+  for (size_t i = 0; i < list.size(); i++) {
+    const auto& g = list[i];
+    const int ibx = d.d_is_a ? (*d.b_blk)[i] : (*d.a_blk)[i];
+    const auto& bd = md->blocks[d.d_is_a ? (*d.a_blk)[i] : (*d.b_blk)[i]];
+    const auto& bx = mx->blocks[ibx];
+    const int64_t nlam = std::min(bd.rows, bd.cols);
+    auto piece = [&](int64_t src, int64_t src_ld, int64_t r0, int64_t r1, int64_t c0, int64_t c1) {
+      tn::DiagItem t;
+      std::memset(&t, 0, sizeof(t));
+      const int64_t l0 = side == 0 ? r0 : c0;
+      t.src = src;
+      t.src_ld = (int32_t)src_ld;
+      t.dst = g.c_off + r0 * g.N + c0;
+      t.dst_ld = (int32_t)g.N;
+      t.rows = (int32_t)(r1 - r0);
+      t.cols = (int32_t)(c1 - c0);
+      t.lam = bd.off + l0 * (bd.cols + 1);
+      t.lam_stride = (int32_t)(bd.cols + 1);
+      t.nlam = (int32_t)std::max<int64_t>(0, nlam - l0);
+      t.side = side;
+      pieces.push_back(t);
+    };
+    if (!vx) {
+      piece(bx.off, bx.cols, 0, g.M, 0, g.N);  // C_q is g.M x g.N; X_q is read only where D_q has a diagonal
+    } else {
+      const tn::ViewHdr& h = vx->hdrs[vx->hdr_of_block[ibx]];
+      const int64_t* pool = vx->pool.data();
+      for (int r = 0; r < h.nr; r++)
+        for (int cc = 0; cc < h.nc; cc++) {
+          const int64_t* e = pool + h.tab + 2 * ((int64_t)r * h.nc + cc);
+          piece(e[0], e[1], pool[h.rs + r], pool[h.rs + r + 1], pool[h.cs + cc], pool[h.cs + cc + 1]);
+        }
+    }
+  }
+  tn::run_diag_scale(c, pieces, Xp, Dp, dptr(d.Tc->elem));
+  return true;
 }
 
 // mutate: permute the operands in place like the reference (restored unless
@@ -650,6 +785,24 @@ UniTensor UniTensor::contract_impl(UniTensor& Ta, UniTensor& Tb, bool fast, bool
     // blocks no sector GEMM writes need it
     UniTensor Tc = (!mc || list.size() == mc->blocks.size()) ? UniTensor(cBonds, "", NoFill{}) : UniTensor(cBonds);
     if (!cBonds.empty()) Tc.setLabel(newLabelC);
+    // a diagonal operand contracted over one bond: a row or column scale
+    const bool d_a = Ta.diag_ && an == 2 && conBond == 1;
+    const bool d_b = !d_a && Tb.diag_ && bn == 2 && conBond == 1;
+    if (d_a || d_b) {
+      const DiagCall dc{&Ta, &Tb, d_a, &sa, &sb, &newLabelA, &newLabelB, conBond, &list, &a_blk, &b_blk, &Tc, fast,
+                        mutate};
+      if (contract_diag(dc)) {
+        Tc.status |= UniTensor::HAVEELEM;
+        if (mutate && !fast) {
+          Ta.permute(oldLabelA, oldRnumA);
+          Tb.permute(oldLabelB, oldRnumB);
+        } else if (mutate) {
+          Ta.permute(newLabelA, an - conBond);
+          Tb.permute(newLabelB, conBond);
+        }
+        return Tc;
+      }
+    }
     tn::OpViewsP va, vb;
     if ((!mutate || !fast) && tn::sectors_take_views(c, g_mode, list)) {
       if (sa.moves) va = tn::get_op_views(c, *Ta.smap, *sa.smap, sa.rsp);
@@ -729,15 +882,20 @@ UniTensor otimes(const UniTensor& Ta, const UniTensor& Tb) {
 }
 
 // ---------------------------------------------------------------- batches
-// One pair of a batch: permuted operands (aliases when already in contraction
-// order), the output and its sector GEMMs (offsets relative to the buffers).
-struct UniTensor::ContractWork {
-  UniTensor pa, pb, tc;
-  std::vector<tn_sector_gemm> sectors;
-  bool outer = false;
-  std::vector<int> outer_labels;
-  int outer_rn = 0;
-};
+// (UniTensor::ContractWork, one pair of a batch, is in contract_work.h)
+
+// bond order of a permute to newLabels (permuted()'s rsp) and whether it moves data
+static bool permute_moves(const UniTensor& t, const std::vector<int>& newLabels, int rowBondNum, std::vector<int>& rsp) {
+  const std::vector<int> l = t.label();
+  const int n = (int)l.size();
+  rsp.assign(n, 0);
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++)
+      if (l[i] == newLabels[j]) rsp[j] = i;
+  bool inorder = true;
+  for (int i = 1; i < n; i++) inorder &= rsp[i] == i;
+  return !(inorder && (int)t.inBondNum() == rowBondNum);
+}
 
 // the label matching, permutes and output construction of contract
 // (UniTensorTools.cpp:138-200) without modifying Ta or Tb
@@ -774,6 +932,8 @@ void UniTensor::prepare_contract(const UniTensor& Ta, const UniTensor& Tb, Contr
   const int conBond = (int)interLabel.size();
   w.pa = permuted(Ta, newLabelA, an - conBond);
   w.pb = permuted(Tb, newLabelB, conBond);
+  w.move_a = permute_moves(Ta, newLabelA, an - conBond, w.rsp_a);
+  w.move_b = permute_moves(Tb, newLabelB, conBond, w.rsp_b);
   std::vector<Bond> cBonds;
   for (int i = 0; i < an - conBond; i++) cBonds.push_back(w.pa.bonds[i]);
   for (int i = conBond; i < bn; i++) cBonds.push_back(w.pb.bonds[i]);
@@ -819,9 +979,9 @@ std::vector<UniTensor> contract_batch(const std::vector<const UniTensor*>& As, c
     if (!As[i] || !Bs[i]) throw std::runtime_error("contract_batch: null operand");
     UniTensor::prepare_contract(*As[i], *Bs[i], work[i]);
     // absolute element addresses: the grouped launch gets null base pointers
-    const int64_t a0 = (int64_t)(uintptr_t)work[i].pa.getElem() / 8;
-    const int64_t b0 = (int64_t)(uintptr_t)work[i].pb.getElem() / 8;
-    const int64_t c0 = (int64_t)(uintptr_t)work[i].tc.getElem() / 8;
+    const int64_t a0 = (int64_t)(uintptr_t)work[i].pa.elemPtr() / 8;
+    const int64_t b0 = (int64_t)(uintptr_t)work[i].pb.elemPtr() / 8;
+    const int64_t c0 = (int64_t)(uintptr_t)work[i].tc.elemPtr() / 8;
     for (auto g : work[i].sectors) {
       g.a_off += a0;
       g.b_off += b0;
@@ -939,6 +1099,7 @@ double svdTruncate(const UniTensor& theta, int64_t chi, UniTensor& U, UniTensor&
   U.status |= UniTensor::HAVEELEM;
   S.status |= UniTensor::HAVEELEM;
   VT.status |= UniTensor::HAVEELEM;
+  S.diag_ = true;  // kept x kept diagonal blocks
   // the host list must outlive the copy above
   TN_CUDA(cudaStreamSynchronize(c.stream));
   return norm;
@@ -978,60 +1139,109 @@ void UniTensor::save(const std::string& fname) const {
   std::fclose(fp);
 }
 
-UniTensor::UniTensor(const std::string& fname) : status(0) {
-  FILE* fp = std::fopen(fname.c_str(), "rb");
-  if (!fp) throw std::runtime_error("Error in opening file '" + fname + "'.");
-  auto rd = [&](void* p, size_t sz, size_t n) {
-    if (std::fread(p, sz, n, fp) != n) {
-      std::fclose(fp);
-      throw std::runtime_error("Error in reading file '" + fname + "' in.");
-    }
-  };
-  int rflag, cflag, namelen, st, bn;
-  size_t qsz;
-  rd(&rflag, 4, 1);
-  rd(&cflag, 4, 1);
-  rd(&namelen, 4, 1);
-  name.assign(namelen, ' ');
-  if (namelen) rd(&name[0], 1, namelen);
-  rd(&st, 4, 1);
-  rd(&bn, 4, 1);
-  rd(&qsz, sizeof(size_t), 1);
-  if (qsz != sizeof(Qnum) || rflag != 1) {
-    std::fclose(fp);
-    throw std::runtime_error("Error in reading file '" + fname + "' in.");
+namespace {
+// bounded reads from a file held in memory
+struct ByteReader {
+  const std::vector<char>& b;
+  size_t pos = 0;
+  bool get(void* p, size_t n) {
+    if (n > b.size() - pos) return false;
+    if (n) std::memcpy(p, b.data() + pos, n);
+    pos += n;
+    return true;
   }
+};
+
+struct SavedTensor {
+  int status = 0;
+  std::vector<Bond> bonds;
+  std::vector<int> labels;
+  std::vector<double> elem;
+  bool has_elem = false;
+};
+
+// The part both layouts share (UniTensor.cpp:501-575): status, bonds (type,
+// charge runs as (U1, parity, fermionic parity) triples and degeneracies),
+// labels, and the elements when status has HAVEELEM.  False when the bytes
+// do not follow it.
+bool read_saved_body(ByteReader& r, SavedTensor& t, int have_elem) {
+  int bn = 0;
+  size_t qsz = 0;
+  if (!r.get(&t.status, 4) || !r.get(&bn, 4) || !r.get(&qsz, sizeof(size_t))) return false;
+  if (qsz != 12 || bn < 0 || bn > 1024) return false;
   for (int b = 0; b < bn; b++) {
-    int t, nq;
-    rd(&t, 4, 1);
-    rd(&nq, 4, 1);
-    std::vector<Qnum> qn(nq);
-    std::vector<int> qd(nq);
-    rd(qn.data(), sizeof(Qnum), nq);
-    rd(qd.data(), sizeof(int), nq);
+    int tp = 0, nq = 0;
+    if (!r.get(&tp, 4) || !r.get(&nq, 4)) return false;
+    if ((tp != BD_IN && tp != BD_OUT) || nq <= 0 || (size_t)nq > r.b.size()) return false;
+    std::vector<int> q(3 * (size_t)nq), deg((size_t)nq);
+    if (!r.get(q.data(), 12 * (size_t)nq) || !r.get(deg.data(), 4 * (size_t)nq)) return false;
     std::vector<Qnum> tot;
-    for (int q = 0; q < nq; q++)
-      for (int d = 0; d < qd[q]; d++) tot.push_back(qn[q]);
-    bonds.push_back(Bond((bondType)t, tot));
+    for (int i = 0; i < nq; i++) {
+      if (deg[i] < 0 || (q[3 * i + 1] != 0 && q[3 * i + 1] != 1) || (q[3 * i + 2] != 0 && q[3 * i + 2] != 1))
+        return false;
+      const Qnum qn((parityFType)q[3 * i + 2], q[3 * i], (parityType)q[3 * i + 1]);
+      for (int d = 0; d < deg[i]; d++) tot.push_back(qn);
+    }
+    t.bonds.push_back(Bond((bondType)tp, tot));
   }
-  initUniT();
-  int nl;
-  rd(&nl, 4, 1);
-  std::vector<int> lab(nl);
-  rd(lab.data(), sizeof(int), nl);
-  if ((size_t)nl != bonds.size()) {
+  int nl = 0;
+  if (!r.get(&nl, 4) || nl != bn) return false;
+  t.labels.assign((size_t)nl, 0);
+  if (!r.get(t.labels.data(), 4 * (size_t)nl)) return false;
+  if (t.status & have_elem) {
+    size_t ne = 0;
+    if (!r.get(&ne, sizeof(size_t)) || ne > (r.b.size() - r.pos) / sizeof(double)) return false;
+    t.elem.resize(ne);
+    if (!r.get(t.elem.data(), ne * sizeof(double))) return false;
+    t.has_elem = true;
+  }
+  return r.pos == r.b.size();
+}
+}  // namespace
+
+// UniTensor(const std::string& fname) (UniTensor.cpp:486-583): the layout
+// UniTensor::save writes -- int r_flag, int c_flag, int namelen, the name,
+// then the shared body.  Files without the first three fields and the name
+// (the reference's older layout, in which its own fixtures such as
+// Swig/examples/egU3_W are stored, and which its current reader rejects) are
+// read as well.  Real (RTYPE) tensors only.
+UniTensor::UniTensor(const std::string& fname) : status(0) {
+  std::vector<char> buf;
+  {
+    FILE* fp = std::fopen(fname.c_str(), "rb");
+    if (!fp) throw std::runtime_error("Error in opening file '" + fname + "'.");
+    char chunk[1 << 16];
+    size_t got;
+    while ((got = std::fread(chunk, 1, sizeof(chunk), fp)) > 0) buf.insert(buf.end(), chunk, chunk + got);
     std::fclose(fp);
-    throw std::runtime_error("Error in reading file '" + fname + "' in.");
   }
-  labels = lab;
-  if (st & HAVEELEM) {
-    size_t ne;
-    rd(&ne, sizeof(size_t), 1);
-    std::vector<double> h(m_elemNum);
-    rd(h.data(), sizeof(double), m_elemNum);
-    setElem(h.data(), false);
+  SavedTensor t;
+  bool ok = false;
+  {
+    ByteReader r{buf};
+    int rflag = 0, cflag = 0, namelen = -1;
+    if (r.get(&rflag, 4) && r.get(&cflag, 4) && r.get(&namelen, 4) && rflag == 1 && cflag == 0 && namelen >= 0 &&
+        (size_t)namelen <= buf.size()) {
+      std::string nm((size_t)namelen, ' ');
+      if (r.get(namelen ? &nm[0] : nullptr, (size_t)namelen) && read_saved_body(r, t, HAVEELEM)) {
+        ok = true;
+        name = nm;
+      }
+    }
   }
-  std::fclose(fp);
+  if (!ok) {  // the older layout
+    t = SavedTensor();
+    ByteReader r{buf};
+    ok = read_saved_body(r, t, HAVEELEM);
+  }
+  if (!ok) throw std::runtime_error("Error in reading file '" + fname + "' in.");
+  bonds = t.bonds;
+  initUniT();
+  labels = t.labels;
+  if (t.has_elem) {
+    if (t.elem.size() != m_elemNum) throw std::runtime_error("Error in reading file '" + fname + "' in.");
+    setElem(t.elem.data(), false);
+  }
 }
 
 }  // namespace uni10

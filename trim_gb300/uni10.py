@@ -228,6 +228,39 @@ class UniTensor:
         call("tn_tensor_get_elem", self.h, out.ctypes.data, out.size)
         return out
 
+    def get_elem_host_ptr(self, ptr: int, n: int) -> None:
+        """getElem into caller-owned host memory (e.g. a pinned buffer) of n doubles."""
+        call("tn_tensor_get_elem", self.h, ptr, n)
+
+    def put_block(self, qnum, mat, diag: bool = False) -> None:
+        """UniTensor::putBlock(qnum, Matrix): mat is a rows x cols array, or
+        with diag=True the diagonal of a rows x cols matrix given as
+        (rows, cols, values)."""
+        q = int_array(list(qnum))
+        if diag:
+            rows, cols, vals = mat
+            v = np.ascontiguousarray(vals, dtype=np.float64)
+            call("tn_tensor_put_block", self.h, q, int(rows), int(cols), 1, v.ctypes.data, v.size)
+        else:
+            m = np.ascontiguousarray(mat, dtype=np.float64)
+            call("tn_tensor_put_block", self.h, q, m.shape[0], m.shape[1], 0, m.ctypes.data, m.size)
+
+    @staticmethod
+    def load(path: str) -> "UniTensor":
+        """UniTensor(fname): the reference's binary layout (current or older)."""
+        h = C.c_void_p()
+        call("tn_tensor_load", None, str(path).encode(), C.byref(h))
+        return UniTensor(_h=h)
+
+    def save(self, path: str) -> None:
+        """UniTensor::save in the reference's binary layout."""
+        call("tn_tensor_save", self.h, str(path).encode())
+
+    def is_diagonal(self) -> bool:
+        d = C.c_int()
+        call("tn_tensor_is_diagonal", self.h, C.byref(d))
+        return bool(d.value)
+
     # -- labels / bonds
     def set_label(self, labels) -> None:
         call("tn_tensor_set_label", self.h, len(labels), int_array(labels))
@@ -299,6 +332,56 @@ def contract(a: UniTensor, b: UniTensor, fast: bool = False, mode="fp64") -> Uni
     h = C.c_void_p()
     call("tn_contract", a.h, b.h, int(bool(fast)), _mode(mode), C.byref(h))
     return UniTensor(_h=h)
+
+
+def contract_sectors_loop(mode, gemms, a_ptr: int, b_ptr: int, c_ptr: int) -> None:
+    """The sector GEMMs one launch each (the reference's per-sector loop), in C++."""
+    arr = (capi.SectorGemm * max(1, len(gemms)))(*[capi.SectorGemm(*g) for g in gemms])
+    call("tn_contract_sectors_loop", None, _mode(mode), len(gemms), arr, a_ptr, b_ptr, c_ptr)
+
+
+class Batch:
+    """n independent contractions a[i] . b[i] with persistent operands and
+    outputs: launch() is one grouped launch on a work list planned once;
+    capture()/replay() run it as one CUDA graph."""
+
+    def __init__(self, As, Bs):
+        n = len(As)
+        a = (C.c_void_p * max(1, n))(*[t.h.value for t in As])
+        b = (C.c_void_p * max(1, n))(*[t.h.value for t in Bs])
+        h = C.c_void_p()
+        call("tn_batch_create", n, a, b, C.byref(h))
+        self.h, self.n = h, n
+
+    def __del__(self):
+        try:
+            capi.lib().tn_batch_destroy(self.h)
+        except Exception:
+            pass
+
+    def put(self, i: int, a: "UniTensor", b: "UniTensor") -> None:
+        call("tn_batch_put", self.h, int(i), a.h, b.h)
+
+    def launch(self, mode="fp64") -> None:
+        call("tn_batch_launch", self.h, _mode(mode))
+
+    def capture(self, mode="fp64") -> None:
+        call("tn_batch_capture", self.h, _mode(mode))
+
+    def replay(self) -> None:
+        call("tn_batch_replay", self.h)
+
+    def output(self, i: int) -> "UniTensor":
+        h = C.c_void_p()
+        call("tn_batch_output", self.h, int(i), C.byref(h))
+        return UniTensor(_h=h)
+
+    def sectors(self):
+        n = C.c_int()
+        call("tn_batch_sectors", self.h, 0, None, C.byref(n))
+        arr = (capi.SectorGemm * max(1, n.value))()
+        call("tn_batch_sectors", self.h, n.value, arr, C.byref(n))
+        return [(g.M, g.N, g.K, g.a_off, g.b_off, g.c_off) for g in arr[: n.value]]
 
 
 def contract_batch(As, Bs, mode="fp64") -> list:

@@ -127,6 +127,18 @@ def block_shapes(bonds):
     return [(q, r[q], c[q]) for q in sorted((q for q in r if q in c), key=_qkey)]
 
 
+def diag_blocks(bonds, elems):
+    """[(qnum, rows, cols, diagonal)] of a tensor whose blocks are diagonal,
+    read from its elements in block order (what putBlock with diagonal
+    matrices rebuilds)."""
+    out, off = [], 0
+    for q, r, c in block_shapes(bonds):
+        blk = np.asarray(elems[off : off + r * c]).reshape(r, c)
+        out.append((q, r, c, np.diagonal(blk).copy()))
+        off += r * c
+    return out
+
+
 def gen_elems(spec: TensorSpec, rng: np.random.Generator) -> np.ndarray:
     n = elem_count(spec.bonds)
     if spec.kind == "uniform":
