@@ -87,6 +87,7 @@ def kernels_dtype(names) -> str:
     names = set(names)
     tc_split = any(n.endswith("_split") for n in names if n.startswith("tc_"))
     tc_bf16 = any(n.endswith("_bf16") for n in names if n.startswith("tc_"))
+    tc_tf32 = any(n.endswith("_tf32") for n in names if n.startswith("tc_"))
     f64 = "gemm_fp64" in names
     if tc_split and f64:
         return "f64 (split: 7 bf16 digit slices on tcgen05, fp32 accumulation, fp64 recombination; thin sectors on the fp64 kernel)"
@@ -94,6 +95,8 @@ def kernels_dtype(names) -> str:
         return "f64 (split: 7 bf16 digit slices on tcgen05, fp32 accumulation, fp64 recombination)"
     if tc_bf16:
         return "bf16 (tcgen05, fp32 accumulation)"
+    if tc_tf32:
+        return "tf32 (tcgen05 kind::tf32, fp32 accumulation)"
     return "f64"
 
 
@@ -343,7 +346,7 @@ def mera_section(args, torch, tu, stream, local, world, peaks):
             outs[d] = net.launch(mode)
 
     res, ref = {}, None
-    fast = [m for m in args.fast_modes.split(",") if m and m != args.mode]
+    fast = [m for m in args.fast_modes.split(",") if m and m not in (args.mode, "none")]
     for mode in ["fp64", args.mode] + fast:
         # FP64 takes ~2 s per step at chi=24: it is timed over fewer steps;
         # the fast (BF16 / TF32) modes are reported beside the headline
@@ -416,11 +419,7 @@ def mera_section(args, torch, tu, stream, local, world, peaks):
         (e2e_ms,) = max_over_ranks(torch, [e2e_ms], "cuda")
     R = res[mode]
     roof = roofline_of(torch, R["prof"], R["timed_steps"], peaks, sustained=True)
-    if roof["kernel"] == "tc_gemm_split":
-        # dram__bytes_read.sum + dram__bytes_write.sum of one tc_gemm_split
-        # launch of the chi=16 diagrams (ncu), scaled by FP64-equivalent flops
-        # per launch to chi=24 (the operand images are re-read per output tile
-        # column block, so traffic grows with the flops)
+    if roof["kernel"] == "tc_gemm_split" and chi == 24:
         roof.update(TC_GEMM_TRAFFIC_NOTE)
     del pinned, out_host
     outs.clear()
@@ -431,8 +430,14 @@ def mera_section(args, torch, tu, stream, local, world, peaks):
                  "matches_device": e2e_ok}, roof
 
 
-# filled from the ncu capture summarised in profiles/ (None until captured)
-TC_GEMM_TRAFFIC_NOTE = {"traffic": None}
+# dram__bytes_read.sum + dram__bytes_write.sum of one chi^8 tc_gemm_split
+# launch of the chi=16 diagrams (ncu, 236.9 + 92.4 MB), scaled by the operand
+# elements (24/16)^6 to the chi=24 launch of the same contraction
+TC_GEMM_TRAFFIC_NOTE = {
+    "traffic": 3.75e9, "traffic_unit": "bytes per chi^8 launch (the big-operand contractions)",
+    "traffic_source": "ncu on the chi=16 diagrams (329.3 MB for one chi^8 launch: the digit images read once, "
+                      "the output partly still in L2), scaled by (24/16)^6; algorithmic bytes of that launch "
+                      "at chi=24: 4.2 GB (digit images 14 B + FP64 output 8 B per element)"}
 
 
 # ----------------------------------------------------------------- iTEBD

@@ -139,7 +139,7 @@ def test_rectangular_diagonal_blocks(tu):
         lam.put_block(q, (r, c, d), diag=True)
         olam.put_block(st.Qnum(*q), d, diag=True, fresh=True)
     assert lam.is_diagonal()
-    byin = wl.change(by, 1)
+    byin = (1, by[1])  # the same charges, incoming (a bond joins an OUT leg to an IN leg)
     bz = (-1, [(-1, 0, 0, 4), (0, 0, 0, 2), (1, 0, 0, 3)])
     ex = rng.standard_normal(wl.elem_count([byin, bz]))
     x = tu.UniTensor([byin, bz], [2, 3], ex)

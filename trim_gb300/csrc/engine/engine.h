@@ -410,7 +410,8 @@ void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems,
 // digit products; levels are summed as 64-bit fixed point, exactly.
 size_t tc_fused_smem(int ns);
 void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems, const double* A, const double* B,
-                     double* C, const ViewHdr* views, const int64_t* pool, int* err, int grid, cudaStream_t s);
+                     double* C, const ViewHdr* views, const int64_t* pool, int* err, int grid, int rpi,
+                     cudaStream_t s);
 // C tile = sum over the K ranges of its FP64 partial tiles, in range order
 void launch_tc_reduce(const TcSector* secs, const int4* ritems, int nred, const double* part, double* C, int grid,
                       cudaStream_t s);

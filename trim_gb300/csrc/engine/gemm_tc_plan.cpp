@@ -217,6 +217,7 @@ struct FusedPlan {
   std::vector<std::pair<int, int>> vw;  // per sector: (A view, B view) header indices, -1: none
   const void* table = nullptr;          // the view table the indices refer to
   int ns = 7;
+  int rpi = kTM;  // rows of an item: 128, or 64 / 32 when 128-row items would leave SMs idle
   DevBufP meta;
   size_t off_it = 0;
   int nsec = 0, nitems = 0;
@@ -239,6 +240,10 @@ static std::shared_ptr<FusedPlan> build_fused_plan(Ctx& ctx, const std::vector<t
   if (vw) P->vw = *vw;
   P->table = table;
   P->ns = ns;
+  // fewer 128-row items than SMs: each item takes 64 or 32 rows, so more CTAs
+  // share the contraction and each one's serial chain is shorter
+  const int64_t items128 = fused_items(list);
+  P->rpi = items128 * 4 <= ctx.num_sms ? 32 : (items128 * 2 <= ctx.num_sms ? 64 : kTM);
   std::vector<TcSector> secs;
   std::vector<int4> items;
   for (size_t gi = 0; gi < list.size(); gi++) {
@@ -256,7 +261,7 @@ static std::shared_ptr<FusedPlan> build_fused_plan(Ctx& ctx, const std::vector<t
     s.M = (int32_t)g.M;
     s.N = (int32_t)g.N;
     s.K = (int32_t)g.K;
-    s.nmt = (int32_t)cdiv(g.M, kTM);
+    s.nmt = (int32_t)cdiv(g.M, P->rpi);
     s.nnt = (int32_t)cdiv(g.N, kTN);
     s.nkt = (int32_t)cdiv(g.K, kTK);
     s.nsplit = 1;
@@ -323,7 +328,7 @@ void run_tc_fused(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
   ProfScope ps(ctx, ns == 7 ? "tc_fused_split" : "tc_fused_bf16", P->in_bytes, P->flops);
   const int grid = (int)std::min<int64_t>((int64_t)P->nitems, (int64_t)ctx.num_sms);
   launch_tc_fused(ns, (const TcSector*)mb, (const int4*)(mb + P->off_it), P->nitems, A, B, C, views, pool,
-                  ctx.device_error_word(), grid, ctx.stream);
+                  ctx.device_error_word(), grid, P->rpi, ctx.stream);
   ctx.launched();
 }
 

@@ -16,18 +16,25 @@
 namespace tn {
 namespace {
 
+// A warp per row of a piece, lanes along its columns (coalesced, no index
+// division); a CTA takes one piece at a time.
 __global__ void __launch_bounds__(256) diag_scale_kernel(const DiagItem* __restrict__ items, int n,
                                                          const double* __restrict__ X, const double* __restrict__ D,
                                                          double* __restrict__ C) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int it = blockIdx.x; it < n; it += gridDim.x) {
     const DiagItem t = items[it];
-    const int64_t total = (int64_t)t.rows * t.cols;
-    for (int64_t e = threadIdx.x; e < total; e += blockDim.x) {
-      const int r = (int)(e / t.cols), c = (int)(e - (int64_t)r * t.cols);
-      const int li = t.side ? c : r;
-      double v = 0.0;
-      if (li < t.nlam) v = D[t.lam + (int64_t)li * t.lam_stride] * X[t.src + (int64_t)r * t.src_ld + c];
-      C[t.dst + (int64_t)r * t.dst_ld + c] = v;
+    for (int r = warp; r < t.rows; r += nw) {
+      const double* __restrict__ x = X + t.src + (int64_t)r * t.src_ld;
+      double* __restrict__ c = C + t.dst + (int64_t)r * t.dst_ld;
+      if (t.side == 0) {  // one diagonal entry for the whole row
+        const bool live = r < t.nlam;
+        const double lam = live ? D[t.lam + (int64_t)r * t.lam_stride] : 0.0;
+        for (int j = lane; j < t.cols; j += 32) c[j] = live ? lam * x[j] : 0.0;
+      } else {
+        for (int j = lane; j < t.cols; j += 32)
+          c[j] = j < t.nlam ? D[t.lam + (int64_t)j * t.lam_stride] * x[j] : 0.0;
+      }
     }
   }
 }
@@ -54,10 +61,11 @@ void launch_diag_scale(const DiagItem* items, int n, const double* X, const doub
   TN_CUDA(cudaGetLastError());
 }
 
-// Pieces are cut to at most kDiagPiece elements (whole rows) so that one CTA
-// takes one piece; the device copy of a piece list is cached on the context.
+// Pieces are cut to at most kDiagPiece elements (whole rows where they fit)
+// so that a small contraction still spreads over many CTAs; the device copy of
+// a piece list is cached on the context.
 void run_diag_scale(Ctx& ctx, const std::vector<DiagItem>& pieces, const double* X, const double* D, double* C) {
-  constexpr int64_t kDiagPiece = 8192;
+  constexpr int64_t kDiagPiece = 2048;
   std::vector<DiagItem> items;
   for (const DiagItem& p0 : pieces) {
     if (p0.rows <= 0 || p0.cols <= 0) continue;

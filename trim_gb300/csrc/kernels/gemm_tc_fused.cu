@@ -1,7 +1,11 @@
 // Fused tensor-core sector GEMM for contractions made of small sectors (the
 // iTEBD theta network's blocks are at most a few hundred rows and columns with
 // K <= 68).  One launch does what the tiled form does in three (maxima,
-// slicing, GEMM).  A work item is one 128 x 64 output tile of one sector; its
+// slicing, GEMM).  A work item is one rpi x 64 output tile of one sector, rpi
+// = 128 rows, or 64 / 32 when a contraction has too few 128-row tiles to give
+// every SM one (the CTA's latency chain -- operand loads, A slicing, FP64
+// assembly -- shrinks with its rows; the M = 128 MMAs read the image rows past
+// rpi, whatever they hold, into accumulator rows that are never drained).  Its
 // CTA
 //   1. takes the power-of-two scale of each row of A and each column of B over
 //      the sector's K (from the 64-k block itself when K <= 64, else from a
@@ -11,8 +15,11 @@
 //      permute fused into the load),
 //      writes the NS digit images of both into shared memory in the tcgen05
 //      K-major 128-byte swizzled layout and issues the digit products (34 for
-//      NS = 7, s + t <= 7) as tcgen05.mma kind::f16 into 6 TMEM accumulators
-//      (levels 0..4 exact, 5..7 shared), only the 16-k steps that hold data,
+//      NS = 7, s + t <= 7) as tcgen05.mma kind::f16 into 8 TMEM accumulators,
+//      level l = s + t at columns 64 l, so one MMA with N = 64 n (n <= 4)
+//      takes A digit s with B digits t0 .. t0 + n - 1 (their images lie back
+//      to back): 11 MMAs per 16-k step instead of 34, only the steps that
+//      hold data,
 //   3. every 128 k (the exact-accumulation chunk) and at the end, drains the
 //      levels into 64-bit fixed point in units of 2^-35: the exact levels
 //      convert without rounding (FP32 magic-number conversion) and the
@@ -43,7 +50,6 @@ using namespace ptx;
 constexpr int kFM = 128, kFN = 64, kFK = 64;
 constexpr int kFThreads = 512;
 constexpr int kFixUnit = 35;   // fixed-point sums in units of 2^-35
-constexpr int kFLevels = 6;    // exact levels 0..4 + one shared accumulator for 5..7
 constexpr int kFMaxLevel = 7;  // digit products with s + t <= 7 are kept
 constexpr int kAImg = kFM * kFK * 2;  // bytes of one A digit image
 constexpr int kBImg = kFN * kFK * 2;  // bytes of one B digit image
@@ -142,8 +148,8 @@ __device__ __forceinline__ int magic_int(float v) {
 
 // One TMEM level sum in units of 2^-35.  Level l < 5 holds integers times
 // 2^-7l, at most 28800 * 128 < 2^22 of them over a 128-k chunk, so
-// v * 2^7l converts exactly; the shared level 5..7 (at most ~16600 * 2^-34
-// per k) is rounded to units of 2^-34.
+// v * 2^7l converts exactly; levels 5..7 (together at most ~16600 * 2^-34 per
+// k), summed in FP32, are rounded to units of 2^-34.
 template <int LVL>
 __device__ __forceinline__ long long level_fixed(float v) {
   if constexpr (LVL < 5)
@@ -159,9 +165,9 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
                                                          const int4* __restrict__ items, int nitems,
                                                          const double* __restrict__ A, const double* __restrict__ B,
                                                          double* __restrict__ C, const ViewHdr* __restrict__ views,
-                                                         const int64_t* __restrict__ pool, int* __restrict__ err) {
+                                                         const int64_t* __restrict__ pool, int* __restrict__ err,
+                                                         int rpi) {
   using L = FusedLayout<NS>;
-  constexpr int LV = (NS == 1) ? 1 : kFLevels;
   constexpr int kGroups = kFThreads / kFN;  // column-maximum partials per column
   // 64-k blocks per exact-accumulation chunk: 128 k keeps every exact level
   // under 2^22 (split); fast mode sums the whole K in FP32
@@ -197,7 +203,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
     const int4 w = items[it];
     const TcSector& S = secs[w.x];
     const int mt = w.y, nt = w.z, n0 = nt * kFN, K = S.K, nkt = S.nkt;
-    const int64_t row0 = (int64_t)mt * kFM;
+    const int64_t row0 = (int64_t)mt * rpi;
     const ViewHdr* av = S.a_vw >= 0 ? views + S.a_vw : nullptr;
     const ViewHdr* bv = S.b_vw >= 0 ? views + S.b_vw : nullptr;
     constexpr int kPairs = (kFM * 8) / kFThreads;  // (row, 8-k chunk) pairs per thread
@@ -205,8 +211,9 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
     int ri[kPairs];
 #pragma unroll
     for (int p = 0; p < kPairs; p++) {
-      const int64_t i = row0 + ((tid + p * kFThreads) >> 3);
-      ri[p] = (av && i < S.M) ? find_start(pool + av->rs, av->nr, i) : 0;
+      const int r = (tid + p * kFThreads) >> 3;
+      const int64_t i = row0 + r;
+      ri[p] = (av && r < rpi && i < S.M) ? find_start(pool + av->rs, av->nr, i) : 0;
     }
     const int bn = tid & 63;
     const int cj = (bv && n0 + bn < S.N) ? find_start(pool + bv->cs, bv->nc, n0 + bn) : 0;
@@ -216,7 +223,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       for (int p = 0; p < kPairs; p++) {
         const int v = tid + p * kFThreads, r = v >> 3, c = v & 7;
         unsigned long long m = 0;
-        if (row0 + r < S.M) {
+        if (r < rpi && row0 + r < S.M) {
           for (int k = c * 8; k < K; k += kFK) {
             double x[8];
             load_a8(A, S, av, pool, row0 + r, ri[p], k, K, x);
@@ -277,7 +284,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       for (int p = 0; p < kPairs; p++) {
         const int v = tid + p * kFThreads, r = v >> 3, c = v & 7;
         const int64_t i = row0 + r;
-        load_a8(A, S, av, pool, i, ri[p], k0 + c * 8, i < S.M ? K : 0, xa[p]);
+        load_a8(A, S, av, pool, i, ri[p], k0 + c * 8, (r < rpi && i < S.M) ? K : 0, xa[p]);
       }
 #pragma unroll
       for (int p = 0; p < kPairs; p++) {
@@ -300,7 +307,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
         } else {
           e = sh.ea[r];
         }
-        if (c < nch) {
+        if (c < nch && r < rpi) {
           uint4 o[NS];
           make_slices<NS>(xa[p], e, o);
           const uint32_t off = swz_off(r, c);
@@ -352,28 +359,40 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
         // bar.sync does not reconverge a warp: elect.sync below needs all 32
         // lanes together, and a diverged warp pays for it on every product
         __syncwarp();
-        // straight-line issue (all loops unrolled, descriptors base + constant);
-        // a level's first product of the block overwrites its accumulator at
-        // the start of a chunk: (s, t, kk) = (0, l, 0) in this order, the
-        // shared level first met at (0, 5, 0)
         const uint32_t carry = (kt % kChunk) != 0;
-        const uint32_t idesc = idesc_bf16_f32(kFM, kFN);
+        const uint32_t idesc1 = idesc_bf16_f32(kFM, kFN);
         const uint64_t a0 = desc_sw128(smem_u32(adig)), b0 = desc_sw128(smem_u32(bdig));
-#pragma unroll
-        for (int s = 0; s < NS; s++)
-#pragma unroll
-          for (int t = 0; t < NS; t++)
-            if (s + t <= (NS == 1 ? 0 : kFMaxLevel)) {
-              const int lvl = min(s + t, LV - 1);
-#pragma unroll
-              for (int kk = 0; kk < kFK / 16; kk++)
-                if (kk < nks) {
-                  const bool first = s == 0 && kk == 0 && t <= LV - 1;
-                  // +32 bytes per 16-k step inside the swizzle atom: +2 in the address field
-                  mma_bf16_elect(tmem + lvl * kFN, a0 + (uint64_t)(s * (kAImg >> 4) + 2 * kk),
-                                 b0 + (uint64_t)(t * (kBImg >> 4) + 2 * kk), idesc, first ? carry : 1u);
+        if constexpr (NS == 1) {
+          for (int kk = 0; kk < nks; kk++)
+            // +32 bytes per 16-k step inside the swizzle atom: +2 in the address field
+            mma_bf16_elect(tmem, a0 + 2 * kk, b0 + 2 * kk, idesc1, (carry | (uint32_t)kk) ? 1u : 0u);
+        } else {
+          // A digit s with B digits t0 .. t0 + tn - 1 in one MMA (N = 64 tn, at
+          // most 4; 7 -> 4 + 3, 6 -> 3 + 3, 5 -> 3 + 2), the group cut where a
+          // level is written for the first time in this chunk (one accumulate
+          // flag per MMA): in the first block of a chunk that is level 7, first
+          // met at s = 1
+          uint32_t touched = carry ? 0xFFu : 0u;
+          for (int s = 0; s < NS; s++) {
+            const int T = min(NS, kFMaxLevel + 1 - s);
+            for (int t0 = 0; t0 < T;) {
+              int tn = T - t0 > 4 ? (T - t0 + 1) >> 1 : T - t0;
+              const int l0 = s + t0;
+              const uint32_t acc = (touched >> l0) & 1u;
+              for (int q = 1; q < tn; q++)
+                if (((touched >> (l0 + q)) & 1u) != acc) {
+                  tn = q;
+                  break;
                 }
+              const uint32_t idesc = idesc1 + ((uint32_t)(tn - 1) * (kFN >> 3) << 17);
+              const uint64_t ad = a0 + (uint64_t)(s * (kAImg >> 4)), bd = b0 + (uint64_t)(t0 * (kBImg >> 4));
+              for (int kk = 0; kk < nks; kk++)
+                mma_bf16_elect(tmem + l0 * kFN, ad + 2 * kk, bd + 2 * kk, idesc, kk ? 1u : acc);
+              touched |= ((1u << tn) - 1u) << l0;
+              t0 += tn;
             }
+          }
+        }
         mma_commit_elect(&sh.mma_bar);
       }
       // warp 0 waits for the products; the others sleep in the barrier
@@ -409,9 +428,14 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
           tmem_ld16(la + 4 * kFN, v);
 #pragma unroll
           for (int j = 0; j < 16; j++) acc[j] += level_fixed<4>(v[j]);
-          tmem_ld16(la + 5 * kFN, v);
+          float w5[16];
+          tmem_ld16(la + 5 * kFN, w5);
+          tmem_ld16(la + 6 * kFN, v);
 #pragma unroll
-          for (int j = 0; j < 16; j++) acc[j] += level_fixed<5>(v[j]);
+          for (int j = 0; j < 16; j++) w5[j] += v[j];
+          tmem_ld16(la + 7 * kFN, v);
+#pragma unroll
+          for (int j = 0; j < 16; j++) acc[j] += level_fixed<5>(w5[j] + v[j]);
         }
         tc_fence_before();
       }
@@ -419,7 +443,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
     }
     if (!ok) break;
     // ---- FP64 tile through the stage (reusing the digit images), coalesced writes
-    {
+    if (rl < rpi) {
       const int q = sh.ea[rl] - 14;
 #pragma unroll
       for (int j = 0; j < 16; j++) {
@@ -429,7 +453,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       }
     }
     __syncthreads();
-    for (int f = tid; f < kFM * kFN; f += kFThreads) {
+    for (int f = tid; f < rpi * kFN; f += kFThreads) {
       const int r = f >> 6, c = f & 63;
       const int64_t i = row0 + r;
       if (i < S.M && n0 + c < S.N) C[S.c_off + i * S.N + n0 + c] = ost[r * kStride + c];
@@ -452,7 +476,9 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
 size_t tc_fused_smem(int ns) { return ns == 7 ? (size_t)FusedLayout<7>::bytes : (size_t)FusedLayout<1>::bytes; }
 
 void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems, const double* A, const double* B,
-                     double* C, const ViewHdr* views, const int64_t* pool, int* err, int grid, cudaStream_t s) {
+                     double* C, const ViewHdr* views, const int64_t* pool, int* err, int grid, int rpi,
+                     cudaStream_t s) {
+  if (rpi != 32 && rpi != 64 && rpi != 128) fail(TN_ERR_ARG, "fused tensor-core form: rows per item must be 32, 64 or 128");
   if (nitems <= 0) return;
   const size_t smem = tc_fused_smem(ns);
   if (ns == 7) {
@@ -461,14 +487,14 @@ void launch_tc_fused(int ns, const TcSector* secs, const int4* items, int nitems
       TN_CUDA(cudaFuncSetAttribute(tc_fused<7>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr = true;
     }
-    tc_fused<7><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, views, pool, err);
+    tc_fused<7><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, views, pool, err, rpi);
   } else {
     static bool attr = false;
     if (!attr) {
       TN_CUDA(cudaFuncSetAttribute(tc_fused<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
       attr = true;
     }
-    tc_fused<1><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, views, pool, err);
+    tc_fused<1><<<grid, kFThreads, smem, s>>>(secs, items, nitems, A, B, C, views, pool, err, rpi);
   }
   TN_CUDA(cudaGetLastError());
 }
