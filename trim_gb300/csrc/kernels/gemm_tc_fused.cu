@@ -54,6 +54,7 @@ constexpr int kFMaxLevel = 7;  // digit products with s + t <= 7 are kept
 constexpr int kAImg = kFM * kFK * 2;  // bytes of one A digit image
 constexpr int kBImg = kFN * kFK * 2;  // bytes of one B digit image
 constexpr int kStride = kFN + 1;      // row stride (doubles) of the FP64 stages
+constexpr int kGroups = kFThreads / kFN;  // threads per column in the column passes over B
 
 template <int NS>
 struct FusedLayout {
@@ -131,13 +132,38 @@ __device__ __forceinline__ void load_a8(const double* __restrict__ A, const TcSe
   }
 }
 
-// element index of B(k, n); cj = column tuple of n when viewed
-__device__ __forceinline__ int64_t b_index(const TcSector& S, const ViewHdr* bv, const int64_t* __restrict__ pool,
-                                           int k, int n, int cj) {
-  if (!bv) return S.b_off + (int64_t)k * S.N + n;
-  const int sk = find_start(pool + bv->rs, bv->nr, k);
-  const int64_t* pr = pool + bv->tab + 2 * ((int64_t)sk * bv->nc + cj);
-  return __ldg(pr) + (k - __ldg(pool + bv->rs + sk)) * __ldg(pr + 1) + (n - __ldg(pool + bv->cs + cj));
+// max |B(k, n)| over k = g, g + kGroups, ... < K of column n (cj: its column
+// tuple when viewed).  The view's (base, ld) is loaded once per row tuple, so
+// the element loads are independent and stay in flight together.
+__device__ __forceinline__ unsigned long long b_col_max(const double* __restrict__ B, const TcSector& S,
+                                                        const ViewHdr* bv, const int64_t* __restrict__ pool, int n,
+                                                        int cj, int g, int K) {
+  unsigned long long m = 0;
+  if (!bv) {
+    const double* col = B + S.b_off + n;
+#pragma unroll 4
+    for (int k = g; k < K; k += kGroups) {
+      const unsigned long long b = abs_bits(__ldg(col + (int64_t)k * S.N));
+      m = b > m ? b : m;
+    }
+    return m;
+  }
+  const int64_t coff = n - __ldg(pool + bv->cs + cj);
+  for (int sk = 0; sk < bv->nr; sk++) {
+    const int64_t r0 = __ldg(pool + bv->rs + sk);
+    if (r0 >= K) break;
+    const int64_t r1 = min((int64_t)K, __ldg(pool + bv->rs + sk + 1));
+    const int64_t* pr = pool + bv->tab + 2 * ((int64_t)sk * bv->nc + cj);
+    const double* base = B + __ldg(pr) + coff;
+    const int64_t ld = __ldg(pr + 1);
+    int64_t k = r0 + (((g - r0) % kGroups) + kGroups) % kGroups;  // the first k >= r0 of this thread's residue
+#pragma unroll 4
+    for (; k < r1; k += kGroups) {
+      const unsigned long long b = abs_bits(__ldg(base + (k - r0) * ld));
+      m = b > m ? b : m;
+    }
+  }
+  return m;
 }
 
 // nearest integer to v for |v| < 2^22 (ties to even): the FP32 add of
@@ -168,7 +194,6 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
                                                          const int64_t* __restrict__ pool, int* __restrict__ err,
                                                          int rpi) {
   using L = FusedLayout<NS>;
-  constexpr int kGroups = kFThreads / kFN;  // column-maximum partials per column
   // 64-k blocks per exact-accumulation chunk: 128 k keeps every exact level
   // under 2^22 (split); fast mode sums the whole K in FP32
   constexpr int kChunk = (NS == 1) ? (1 << 30) : 2;
@@ -177,7 +202,6 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
   uint8_t* base = (uint8_t*)(((uintptr_t)dyn + 1023) & ~(uintptr_t)1023);
   uint8_t* adig = base;                        // NS x 16 KB
   uint8_t* bdig = base + NS * kAImg;           // NS x 8 KB
-  double* ost = (double*)base;                 // [128][65], once the last MMAs are done
   double* bst = (double*)(base + L::region0);  // [64][65]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
@@ -243,13 +267,7 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       }
       {
         const int g = tid >> 6;
-        unsigned long long m = 0;
-        if (n0 + bn < S.N)
-          for (int k = g; k < K; k += kGroups) {
-            const unsigned long long bts = abs_bits(__ldg(B + b_index(S, bv, pool, k, n0 + bn, cj)));
-            m = bts > m ? bts : m;
-          }
-        sh.colpart[g][bn] = m;
+        sh.colpart[g][bn] = (n0 + bn < S.N) ? b_col_max(B, S, bv, pool, n0 + bn, cj, g, K) : 0ull;
       }
       __syncthreads();
       if (tid < kFN) {
@@ -272,11 +290,46 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       const int nks = (kval + 15) >> 4, nch = 2 * nks;  // 16-k MMA steps, 8-k chunks holding data
       // ---- B block -> FP64 stage, coalesced along n (asynchronous copies,
       // in flight while A is sliced)
+      {
+        // thread (column bn, k = kb + kGroups j); through a view, the (base, ld)
+        // of the current row tuple is kept in registers and moved on as k
+        // passes the tuple's end (tuples ascend with k), so the copies'
+        // addresses need no loads of their own
+        const int n = n0 + bn, kb = tid >> 6;
+        const bool nvalid = n < S.N;
+        if (!bv) {
+          const double* col = B + S.b_off + n;
 #pragma unroll
-      for (int j = 0; j < (kFK * kFN) / kFThreads; j++) {
-        const int k = (tid >> 6) + j * (kFThreads / kFN);  // f = tid + j * 512: n = f & 63 = bn, k = f >> 6
-        const bool valid = k < kval && n0 + bn < S.N;
-        cp_async8(bst + k * kStride + bn, valid ? B + b_index(S, bv, pool, k0 + k, n0 + bn, cj) : B, valid);
+          for (int j = 0; j < kFK / kGroups; j++) {
+            const int k = kb + kGroups * j;
+            const bool valid = k < kval && nvalid;
+            cp_async8(bst + k * kStride + bn, valid ? col + (int64_t)(k0 + k) * S.N : B, valid);
+          }
+        } else {
+          const int64_t* rs = pool + bv->rs;
+          int sk = (nvalid && kb < kval) ? find_start(rs, bv->nr, k0 + kb) : 0;
+          int64_t r0 = __ldg(rs + sk), r1 = __ldg(rs + sk + 1);
+          const int64_t coff = n - __ldg(pool + bv->cs + cj);
+          const int64_t* pr = pool + bv->tab + 2 * ((int64_t)sk * bv->nc + cj);
+          const double* bbase = B + __ldg(pr) + coff;
+          int64_t ld = __ldg(pr + 1);
+#pragma unroll
+          for (int j = 0; j < kFK / kGroups; j++) {
+            const int k = kb + kGroups * j;
+            const bool valid = k < kval && nvalid;
+            if (valid && k0 + k >= r1) {  // past this row tuple: the next one holding k0 + k
+              do {
+                sk++;
+                r0 = r1;
+                r1 = __ldg(rs + sk + 1);
+              } while (k0 + k >= r1);
+              pr = pool + bv->tab + 2 * ((int64_t)sk * bv->nc + cj);
+              bbase = B + __ldg(pr) + coff;
+              ld = __ldg(pr + 1);
+            }
+            cp_async8(bst + k * kStride + bn, valid ? bbase + (k0 + k - r0) * ld : B, valid);
+          }
+        }
       }
       // ---- A: thread (row r, 8-k chunk c), both of its chunks loaded first
       double xa[kPairs][8];
@@ -405,10 +458,13 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       }
       tc_fence_after();
       if (kt % kChunk == kChunk - 1 || kt == nkt - 1) {
-        // ---- drain the chunk: fixed point (split) or the FP32 sum (fast)
+        // ---- drain the chunk: fixed point (split) or the FP32 sum (fast), by
+        // the warps whose TMEM lane quadrant holds rows of this item
         const uint32_t la = tmem + ((uint32_t)(qd * 32) << 16) + cg * 16;
         float v[16];
-        if constexpr (NS == 1) {
+        if (qd * 32 >= rpi) {
+          // no live row in this quadrant
+        } else if constexpr (NS == 1) {
           tmem_ld16(la, v);
 #pragma unroll
           for (int j = 0; j < 16; j++) accf[j] += v[j];
@@ -442,21 +498,29 @@ __global__ void __launch_bounds__(kFThreads, 1) tc_fused(const TcSector* __restr
       __syncthreads();  // digit images, stage and accumulators are reused by the next block
     }
     if (!ok) break;
-    // ---- FP64 tile through the stage (reusing the digit images), coalesced writes
+    // ---- the sums through a shared stage (reusing the digit images), then
+    // every thread converts outputs to FP64 and writes them, consecutive
+    // threads on consecutive columns: the integer conversion is spread over
+    // all 16 warps instead of the few whose lanes hold the rows
+    long long* st64 = (long long*)base;  // [rpi][64] fixed-point sums (split)
+    float* stf = (float*)base;            // [rpi][64] FP32 sums (fast)
     if (rl < rpi) {
-      const int q = sh.ea[rl] - 14;
 #pragma unroll
       for (int j = 0; j < 16; j++) {
-        const int qj = q + sh.eb[cg * 16 + j];
-        ost[rl * kStride + cg * 16 + j] =
-            NS == 1 ? scale_pow2((double)accf[j], qj) : fixed_to_double(acc[j], qj - kFixUnit);
+        if constexpr (NS == 1)
+          stf[rl * kFN + cg * 16 + j] = accf[j];
+        else
+          st64[rl * kFN + cg * 16 + j] = acc[j];
       }
     }
     __syncthreads();
     for (int f = tid; f < rpi * kFN; f += kFThreads) {
       const int r = f >> 6, c = f & 63;
       const int64_t i = row0 + r;
-      if (i < S.M && n0 + c < S.N) C[S.c_off + i * S.N + n0 + c] = ost[r * kStride + c];
+      if (i < S.M && n0 + c < S.N) {
+        const int q = sh.ea[r] - 14 + sh.eb[c];
+        C[S.c_off + i * S.N + n0 + c] = NS == 1 ? scale_pow2((double)stf[f], q) : fixed_to_double(st64[f], q - kFixUnit);
+      }
     }
     __syncthreads();  // the stage is the next item's digit images
   }
