@@ -218,10 +218,11 @@ typedef struct {
 
 /* All n sector SVDs in FP64 on the GPU, in one batch (one-sided Jacobi, each
  * sector on a thread-block cluster: FP32 sweeps, an FP64 orthogonalisation
- * of their rotations, FP64 sweeps; sectors too large for shared memory use
- * cuSOLVER's gesvdj).  list is a host array; A, U, S, VT are device buffers.
- * sweeps (host, n entries, may be NULL) receives per sector the FP64 sweeps
- * plus 100 times the FP32 sweeps (0 for the cuSOLVER fallback; FP64 part -1
+ * of their rotations, a second FP32 pass on the product, FP64 sweeps; sectors
+ * too large for shared memory use cuSOLVER's gesvdj).  list is a host array;
+ * A, U, S, VT are device buffers.  sweeps (host, n entries, may be NULL)
+ * receives per sector the FP64 sweeps plus 100 times the FP32 sweeps of both
+ * passes (0 for the cuSOLVER fallback; FP64 part -1
  * if the sector did not converge in 40 FP64 sweeps); it makes the call
  * synchronous.  Columns of U (or rows of VT) that belong to an exactly zero
  * singular value are returned as zero vectors. */

@@ -78,7 +78,7 @@ def test_svd_batched_shapes(env):
     mats = [rng.uniform(-1, 1, size=s) for s in SHAPES]
     res, sweeps = run_svd(env, mats)
     for a, (u, s, vt), sw, shp in zip(mats, res, sweeps, SHAPES):
-        assert 0 < sw % 100 < 40 and sw // 100 <= 20, (shp, sw)
+        assert 0 < sw % 100 < 40 and sw // 100 <= 2 * 20, (shp, sw)  # two FP32 passes
         check_svd(a, u, s, vt)
 
 

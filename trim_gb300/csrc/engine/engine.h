@@ -199,10 +199,11 @@ struct TcSector {
 };
 
 // One sector of the cluster Jacobi SVD (M x N, row-major).  Stage 1 (FP32):
-// the sector at a_off of the input, rotation product V (nx x nx) and V^T out
-// at v_off.  Stage 2 (FP64): X1 (M x N) at a_off, Q^T at v_off in; U (M x k)
-// at u_off, S (k) at s_off, VT (k x N) at vt_off out, k = min(M, N).  b
-// columns per block (2P blocks per sector), record length L (multiple of 4).
+// the sector at a_off of the input (A, or A Q1 on the second pass), rotation
+// product V (nx x nx) and V^T out at v_off.  Stage 2 (FP64): the sector at
+// a_off (A Q), Q^T at v_off in; U (M x k) at u_off, S (k) at s_off, VT (k x N)
+// at vt_off out, k = min(M, N).  b columns per block (2P blocks per sector),
+// record length L (multiple of 4).
 struct SvdJob {
   int64_t a_off, v_off, u_off, s_off, vt_off;
   int32_t M, N, b, L;
@@ -210,13 +211,37 @@ struct SvdJob {
 };
 constexpr int kSvdMaxSweeps = 40;    // FP64 stage
 constexpr int kSvdMaxSweeps32 = 20;  // FP32 stage
-constexpr int kSvdMaxPairs = 40;     // pairs of one sub-round (b + 1 at most)
 constexpr int kSvdMaxSmem = 227 * 1024;
+
+// The Jacobi kernel instance a record of L entries takes (es = 4: FP32 stage,
+// 8: FP64 stage): records held in registers, K entries per lane, padded to
+// 32 K entries (K in 1..12, 14, 16, 20, 24, 28, 32); one warp per column pair
+// of a sub-round, at most max_warps warps per CTA (the register budget).
+// K = 0: no instance (the sector goes to the library fallback).
+struct SvdKernelCaps {
+  int K, max_warps;
+};
+__host__ __device__ inline SvdKernelCaps svd_kernel_caps(int es, int64_t L) {
+  const int64_t k = (L + 31) / 32;
+  int K;
+  if (k < 1)
+    K = 1;
+  else if (k <= 12)
+    K = (int)k;
+  else if (k <= 16)
+    K = k <= 14 ? 14 : 16;
+  else if (k <= 32)
+    K = k <= 20 ? 20 : (k <= 24 ? 24 : (k <= 28 ? 28 : 32));
+  else
+    return {0, 0};
+  if (es == 4) return {K, K <= 12 ? 24 : (K <= 20 ? 16 : 12)};
+  return {K, K <= 12 ? 16 : (K <= 20 ? 12 : 8)};
+}
 
 // Shared-memory layout of one CTA of the Jacobi kernel (byte offsets);
 // es = 4 (FP32 stage) or 8 (FP64 stage).
 struct SvdSmem {
-  size_t sig, all, red, rec, nrm, pd, ph, ps, pf, cnt, misc, total;
+  size_t sig, all, red, rec, nrm, cnt, misc, total;
 };
 __host__ __device__ inline SvdSmem svd_smem(int P, int b, int L, int es) {
   SvdSmem m;
@@ -227,11 +252,7 @@ __host__ __device__ inline SvdSmem svd_smem(int P, int b, int L, int es) {
   m.red = m.all + 8 * nsig;
   m.rec = (m.red + 8 * 32 + 15) & ~(size_t)15;
   m.nrm = m.rec + (size_t)es * nbuf * 2 * b * L;
-  m.pd = m.nrm + (size_t)es * nbuf * 2 * b;
-  m.ph = m.pd + (size_t)es * kSvdMaxPairs;
-  m.ps = m.ph + (size_t)es * kSvdMaxPairs;
-  m.pf = (m.ps + (size_t)es * kSvdMaxPairs + 7) & ~(size_t)7;
-  m.cnt = m.pf + 4 * kSvdMaxPairs;
+  m.cnt = (m.nrm + (size_t)es * nbuf * 2 * b + 7) & ~(size_t)7;
   m.misc = m.cnt + 4 * 32;
   m.total = m.misc + 4 * 4;
   return m;
@@ -436,7 +457,8 @@ void run_diag_scale(Ctx& ctx, const std::vector<DiagItem>& pieces, const double*
 // SVD (Block::svd per sector) and truncation
 struct SvdGeom {
   int P = 0, b = 0, L = 0;  // P == 0: too large for the cluster kernel
-  int threads = 0;          // one warp per column pair of a sub-round, 8..24 warps
+  int K = 0;                // register capacity of the kernel instance (svd_kernel_caps)
+  int threads = 0;          // one warp per column pair of a sub-round, at least 8 warps
   size_t smem = 0;
 };
 // cluster size P, columns per block b, record length L, threads per CTA and
@@ -444,12 +466,17 @@ struct SvdGeom {
 SvdGeom svd_geometry(int64_t M, int64_t N, int max_cluster);
 SvdGeom svd_geometry32(int64_t M, int64_t N, int max_cluster);
 int svd_max_cluster();  // largest cluster size the device schedules (<= 16)
-// stage 1: FP32 sweeps from the identity, V and V^T out to Vout; stage 2:
-// FP64 sweeps from X1 and Q^T (in X and Vin), U, S, VT out
-void launch_svd_jacobi(int stage, const SvdJob* jobs, int njobs, int P, int threads, size_t smem, const double* X,
-                       const double* Vin, double* Vout, double* U, double* S, double* VT, int* info, cudaStream_t s);
+// stage 1: FP32 sweeps from the identity, V and V^T out to Vout (pass 0
+// writes the sweep count to info, pass 1 adds to it); stage 2: FP64 sweeps
+// from A Q and Q^T (in X and Vin), U, S, VT out.  K: the register capacity
+// of the instance (svd_kernel_caps of the jobs' longest record).
+void launch_svd_jacobi(int stage, int pass, const SvdJob* jobs, int njobs, int P, int threads, size_t smem,
+                       const double* X, const double* Vin, double* Vout, double* U, double* S, double* VT, int* info,
+                       cudaStream_t s, int K);
 // T = 3/2 I - (G + G^T)/4 for every (n, g_off, t_off) triple of tab (device)
 void launch_ns_factor(const int64_t* tab, int njobs, double* ws, cudaStream_t s);
+// dst = src^T (n x n) for every (n, src_off, dst_off) triple of tab (device)
+void launch_ns_transpose(const int64_t* tab, int njobs, double* ws, cudaStream_t s);
 void launch_truncate(const int64_t* s_off, const int64_t* s_cnt, int nsec, double* S, int64_t chi, int64_t* kept,
                      double* norm, cudaStream_t s);
 void launch_gather_truncated(const TruncSector* secs, int nsec, const double* U, const double* S, const double* VT,

@@ -8,103 +8,92 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <map>
 
 #include "engine.h"
 
 namespace tn {
 
-// Threads of a CTA: one warp per column pair of a sub-round (b + 1 pairs at
-// most), between 8 and 24 warps; the FP64 stage runs 8 warps.
-static int svd_threads(int b, bool fp64) {
-  if (fp64) return 256;
-  return 32 * std::max(8, std::min(24, b + (b & 1)));
-}
+// Threads of a CTA: one warp per column pair of a sub-round (b rounded up to
+// even), at least 8 warps for the loads and exchanges.
+static int svd_threads(int64_t b) { return 32 * (int)std::max<int64_t>(8, b + (b & 1)); }
 
-// FP64 stage: the smallest power-of-two cluster whose blocks hold at most
-// bmax columns (8, or 4 from nx = 96 on, where the stage is bound by the FP64
-// rate of the cluster's SMs) within shared memory; larger sectors take
-// P = max_cluster with wider blocks while they fit.  P = 0: the sector does
-// not fit at all (cuSOLVER fallback).
-SvdGeom svd_geometry(int64_t M, int64_t N, int max_cluster) {
+// The smallest power-of-two cluster whose blocks hold at most bmax columns
+// within shared memory and the warps of the kernel instance; larger sectors
+// take P = max_cluster with wider blocks while they fit.  P = 0: the sector
+// does not fit at all (cuSOLVER fallback).
+static SvdGeom geometry(int64_t M, int64_t N, int max_cluster, int es, int64_t bmax) {
   SvdGeom g;
   const int64_t mx = std::max(M, N), nx = std::min(M, N);
   if (nx <= 0 || mx > INT_MAX / 4) return g;
-  const int L = (int)((mx + nx + 3) & ~int64_t(3));
-  const int64_t bmax = nx >= 96 ? 4 : 8;
+  const SvdKernelCaps caps = svd_kernel_caps(es, mx + nx);
+  if (!caps.K) return g;
+  const int64_t L = 32 * (int64_t)caps.K;  // record length (padded)
   for (int P = 1; P <= max_cluster; P *= 2) {
     const int64_t b = (nx + 2 * P - 1) / (2 * P);
     const bool last = 2 * P > max_cluster;
     if (b > bmax && !last) continue;
-    const size_t smem = svd_smem(P, (int)std::min<int64_t>(b, INT_MAX), L, 8).total;
-    if (b + 1 > kSvdMaxPairs || smem > (size_t)kSvdMaxSmem) {
+    if (b + (b & 1) > caps.max_warps) {
+      if (last) return g;
+      continue;
+    }
+    const size_t smem = svd_smem(P, (int)b, (int)L, es).total;
+    if (smem > (size_t)kSvdMaxSmem) {
       if (last) return g;
       continue;
     }
     g.P = P;
     g.b = (int)b;
-    g.L = L;
-    g.threads = svd_threads(g.b, true);
+    g.L = (int)L;
+    g.K = caps.K;
+    g.threads = svd_threads(b);
     g.smem = smem;
     return g;
   }
   return g;
 }
 
-// FP32 stage: the smallest power-of-two cluster with b <= 24 (one warp per
-// pair, 24 warps at most), which keeps the block exchanges (2P - 1 per
-// sweep) few; wider blocks when the cluster size is capped.
-SvdGeom svd_geometry32(int64_t M, int64_t N, int max_cluster) {
-  SvdGeom g;
-  const int64_t mx = std::max(M, N), nx = std::min(M, N);
-  if (nx <= 0 || mx > INT_MAX / 4) return g;
-  const int L = (int)((mx + nx + 3) & ~int64_t(3));
-  for (int P = 1; P <= max_cluster; P *= 2) {
-    const int64_t b = (nx + 2 * P - 1) / (2 * P);
-    const bool last = 2 * P > max_cluster;
-    if (b > 23 && !last) continue;
-    const size_t smem = svd_smem(P, (int)std::min<int64_t>(b, INT_MAX), L, 4).total;
-    if (b + 1 > kSvdMaxPairs || smem > (size_t)kSvdMaxSmem) {
-      if (last) return g;
-      continue;
-    }
-    g.P = P;
-    g.b = (int)b;
-    g.L = L;
-    g.threads = svd_threads(g.b, false);
-    g.smem = smem;
-    return g;
-  }
-  return g;
+// FP64 stage: blocks of at most 8 columns (4 from nx = 96 on), so that the
+// FP64 work of a sub-round spreads over the SMs of a larger cluster.
+SvdGeom svd_geometry(int64_t M, int64_t N, int max_cluster) {
+  return geometry(M, N, max_cluster, 8, std::min(M, N) >= 96 ? 4 : 8);
 }
+
+// FP32 stage: blocks of at most 9 columns.  A sub-round is latency bound
+// (about 600 cycles from b = 4 to 8, 780 at b = 16, measured on GB300), and
+// more blocks cost more exchanges (2P - 1 per sweep, about 1 to 2 us each),
+// which balance near b = 9.
+SvdGeom svd_geometry32(int64_t M, int64_t N, int max_cluster) { return geometry(M, N, max_cluster, 4, 9); }
 
 namespace {
 
 struct SvdClass {
-  int P = 0;
+  int P = 0, K = 0;
   int njobs = 0;
   int64_t first = 0;  // index of the first job of this class in its job buffer
   int threads = 256;
   size_t smem = 0;
 };
 
-// Workspace of one Jacobi sector (doubles): V | V^T, Q | Q^T (Newton-Schulz
-// ping-pong), G, T, X1.
+// Workspace of one Jacobi sector (doubles): V | V^T, Q | Q^T, R | R^T
+// (Newton-Schulz ping-pong; Q1 ends in V, Q2 in Q, Q^T = (Q1 Q2)^T in R), G,
+// T, X1 = A Q1, X2 = A Q1 Q2 (M x N each).
 struct SvdWs {
-  int64_t v, q, g, t, x1;
+  int64_t v, q, r, g, t, x1, x2;
 };
 
 struct SvdPlan {
   std::vector<tn_svd_sector> list;
-  DevBufP jobs1, jobs2;  // stage 1 / stage 2 job lists, grouped by class
-  DevBufP ns_tab;        // (n, g_off, t_off) per Jacobi sector
+  DevBufP jobs1, jobs1b, jobs2;  // FP32 passes 0 and 1, FP64 stage; grouped by class
+  DevBufP ns_tab;                // (n, g_off, t_off) per Jacobi sector
+  DevBufP tr_tab;                // (n, src, dst) per sector for each of the 4 Newton-Schulz steps
   std::vector<SvdClass> classes1, classes2;  // per stage, largest cluster first
   std::vector<tn_svd_sector> jac;  // the Jacobi sectors
   std::vector<SvdWs> ws;
   int64_t ws_elems = 0;
-  // grouped FP64 GEMMs of the orthogonalisation, all in workspace offsets
-  std::vector<tn_sector_gemm> gram1, prod1, gram2, prod2;
-  std::vector<tn_sector_gemm> x1_direct;  // X1 = A Q   (A operand in the input)
-  std::vector<tn_sector_gemm> x1_trans;   // X1^T = Q^T A (B operand in the input)
+  // grouped FP64 GEMMs of the orthogonalisations and products, in workspace
+  // offsets (x1_a, x1_b: the first operand in the input)
+  std::vector<tn_sector_gemm> gram1, prod1, gram2, prod2, x1_a, x1_b, gram3, prod3, gram4, prod4, fin;
   std::vector<int> fallback;  // sectors for cuSOLVER
   std::vector<int> empty;     // sectors with M or N == 0
 };
@@ -122,6 +111,18 @@ DevBufP upload(Ctx& ctx, const void* p, size_t bytes) {
   return b;
 }
 
+// Newton-Schulz step on the pair (Y, Y^T) at `from` into `to`: G = Y^T Y,
+// T = 3/2 I - (G + G^T)/4 (launch_ns_factor), Y T, and its transpose (T is
+// symmetric, so (Y T)^T = T Y^T) by a copy
+void ns_step(std::vector<tn_sector_gemm>& gram, std::vector<tn_sector_gemm>& prod, std::vector<int64_t>& tr,
+             int64_t n, int64_t from, int64_t to, const SvdWs& w) {
+  gram.push_back(tn_sector_gemm{n, n, n, from + n * n, from, w.g});
+  prod.push_back(tn_sector_gemm{n, n, n, from, w.t, to});
+  tr.push_back(n);
+  tr.push_back(to);
+  tr.push_back(to + n * n);
+}
+
 std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>& list) {
   const int maxp = svd_max_cluster();
   const uint64_t key = hash_svd(list, maxp);
@@ -134,10 +135,14 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
   }
   auto plan = std::make_shared<SvdPlan>();
   plan->list = list;
-  std::vector<SvdJob> byP1[5], byP2[5];
-  size_t smem1[5] = {0, 0, 0, 0, 0}, smem2[5] = {0, 0, 0, 0, 0};
-  int thr1[5] = {256, 256, 256, 256, 256}, thr2[5] = {256, 256, 256, 256, 256};
-  std::vector<int64_t> tab;
+  // jobs per class (cluster size, kernel instance), per stage
+  struct Acc {
+    std::vector<SvdJob> a, b;  // stage 1: passes 0 and 1 (same geometry); stage 2: a only
+    size_t smem = 0;
+    int threads = 0;
+  };
+  std::map<std::pair<int, int>, Acc> cls1, cls2;
+  std::vector<int64_t> tab, tr[4];
   for (size_t i = 0; i < list.size(); i++) {
     const tn_svd_sector& s = list[i];
     if (s.M < 0 || s.N < 0) fail(TN_ERR_ARG, "svd: negative sector dimension");
@@ -152,28 +157,35 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
       plan->fallback.push_back((int)i);
       continue;
     }
-    const int64_t n = std::min(s.M, s.N);
+    const int64_t n = std::min(s.M, s.N), mn = s.M * s.N;
     SvdWs w;
     w.v = plan->ws_elems;
     w.q = w.v + 2 * n * n;
-    w.g = w.q + 2 * n * n;
+    w.r = w.q + 2 * n * n;
+    w.g = w.r + 2 * n * n;
     w.t = w.g + n * n;
     w.x1 = w.t + n * n;
-    plan->ws_elems = w.x1 + s.M * s.N;
+    w.x2 = w.x1 + mn;
+    plan->ws_elems = w.x2 + mn;
     plan->ws.push_back(w);
     plan->jac.push_back(s);
-    // Newton-Schulz: G = V^T V, T = 3/2 I - (G + G^T)/4, Q = V T, Q^T = T V^T;
-    // then the same from Q back into V
-    plan->gram1.push_back(tn_sector_gemm{n, n, n, w.v + n * n, w.v, w.g});
-    plan->prod1.push_back(tn_sector_gemm{n, n, n, w.v, w.t, w.q});
-    plan->prod1.push_back(tn_sector_gemm{n, n, n, w.t, w.v + n * n, w.q + n * n});
-    plan->gram2.push_back(tn_sector_gemm{n, n, n, w.q + n * n, w.q, w.g});
-    plan->prod2.push_back(tn_sector_gemm{n, n, n, w.q, w.t, w.v});
-    plan->prod2.push_back(tn_sector_gemm{n, n, n, w.t, w.q + n * n, w.v + n * n});
+    // Q1: two Newton-Schulz steps from the FP32 rotations V (V -> Q -> V)
+    ns_step(plan->gram1, plan->prod1, tr[0], n, w.v, w.q, w);
+    ns_step(plan->gram2, plan->prod2, tr[1], n, w.q, w.v, w);
+    // X1 = A Q1 (stored as X1^T = Q1^T A when M < N, the kernel's A^T layout)
     if (s.M >= s.N)
-      plan->x1_direct.push_back(tn_sector_gemm{s.M, s.N, s.N, s.a_off, w.v, w.x1});
+      plan->x1_a.push_back(tn_sector_gemm{s.M, s.N, s.N, s.a_off, w.v, w.x1});
     else
-      plan->x1_trans.push_back(tn_sector_gemm{s.M, s.N, s.M, w.v + n * n, s.a_off, w.x1});
+      plan->x1_b.push_back(tn_sector_gemm{s.M, s.N, s.M, w.v + n * n, s.a_off, w.x1});
+    // Q2 from the second FP32 pass's rotations (Q -> R -> Q)
+    ns_step(plan->gram3, plan->prod3, tr[2], n, w.q, w.r, w);
+    ns_step(plan->gram4, plan->prod4, tr[3], n, w.r, w.q, w);
+    // X2 = X1 Q2 and (Q1 Q2)^T = Q2^T Q1^T into R
+    if (s.M >= s.N)
+      plan->fin.push_back(tn_sector_gemm{s.M, s.N, s.N, w.x1, w.q, w.x2});
+    else
+      plan->fin.push_back(tn_sector_gemm{s.M, s.N, s.M, w.q + n * n, w.x1, w.x2});
+    plan->fin.push_back(tn_sector_gemm{n, n, n, w.q + n * n, w.v + n * n, w.r});
     tab.push_back(n);
     tab.push_back(w.g);
     tab.push_back(w.t);
@@ -188,42 +200,53 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     j1.b = g1.b;
     j1.L = g1.L;
     j1.id = (int)i;
+    SvdJob j1b = j1;
+    j1b.a_off = w.x1;
+    j1b.v_off = w.q;
     SvdJob j2 = j1;
-    j2.a_off = w.x1;
-    j2.v_off = w.v + n * n;  // Q^T after the second Newton-Schulz step
+    j2.a_off = w.x2;
+    j2.v_off = w.r;  // (Q1 Q2)^T
     j2.b = g.b;
     j2.L = g.L;
-    int c1 = 0, c2 = 0;
-    while ((1 << c1) < g1.P) c1++;
-    while ((1 << c2) < g.P) c2++;
-    byP1[c1].push_back(j1);
-    byP2[c2].push_back(j2);
-    smem1[c1] = std::max(smem1[c1], g1.smem);
-    smem2[c2] = std::max(smem2[c2], g.smem);
-    thr1[c1] = std::max(thr1[c1], g1.threads);
-    thr2[c2] = std::max(thr2[c2], g.threads);
+    Acc& c1 = cls1[{g1.P, g1.K}];
+    c1.a.push_back(j1);
+    c1.b.push_back(j1b);
+    c1.smem = std::max(c1.smem, g1.smem);
+    c1.threads = std::max(c1.threads, g1.threads);
+    Acc& c2 = cls2[{g.P, g.K}];
+    c2.a.push_back(j2);
+    c2.smem = std::max(c2.smem, g.smem);
+    c2.threads = std::max(c2.threads, g.threads);
   }
-  auto group = [&](std::vector<SvdJob>* by, size_t* smem, int* thr, std::vector<SvdClass>& classes) {
-    std::vector<SvdJob> all;
-    for (int c = 4; c >= 0; c--) {
-      if (by[c].empty()) continue;
+  // largest clusters first
+  auto group = [&](std::map<std::pair<int, int>, Acc>& by, bool second, std::vector<SvdClass>& classes,
+                   std::vector<SvdJob>& all) {
+    for (auto c = by.rbegin(); c != by.rend(); ++c) {
+      const std::vector<SvdJob>& jobs = second ? c->second.b : c->second.a;
       SvdClass k;
-      k.P = 1 << c;
-      k.njobs = (int)by[c].size();
+      k.P = c->first.first;
+      k.K = c->first.second;
+      k.njobs = (int)jobs.size();
       k.first = (int64_t)all.size();
-      k.smem = smem[c];
-      k.threads = thr[c];
-      classes.push_back(k);
-      all.insert(all.end(), by[c].begin(), by[c].end());
+      k.smem = c->second.smem;
+      k.threads = c->second.threads;
+      if (!second) classes.push_back(k);
+      all.insert(all.end(), jobs.begin(), jobs.end());
     }
-    return all;
   };
-  std::vector<SvdJob> all1 = group(byP1, smem1, thr1, plan->classes1);
-  std::vector<SvdJob> all2 = group(byP2, smem2, thr2, plan->classes2);
+  std::vector<SvdJob> all1, all1b, all2;
+  group(cls1, false, plan->classes1, all1);
+  std::vector<SvdClass> unused;
+  group(cls1, true, unused, all1b);
+  group(cls2, false, plan->classes2, all2);
   if (!all1.empty()) {
     plan->jobs1 = upload(ctx, all1.data(), all1.size() * sizeof(SvdJob));
+    plan->jobs1b = upload(ctx, all1b.data(), all1b.size() * sizeof(SvdJob));
     plan->jobs2 = upload(ctx, all2.data(), all2.size() * sizeof(SvdJob));
     plan->ns_tab = upload(ctx, tab.data(), tab.size() * sizeof(int64_t));
+    std::vector<int64_t> trs;
+    for (int k = 0; k < 4; k++) trs.insert(trs.end(), tr[k].begin(), tr[k].end());
+    plan->tr_tab = upload(ctx, trs.data(), trs.size() * sizeof(int64_t));
     TN_CUDA(cudaStreamSynchronize(ctx.stream));
   }
   ctx.svd_cache[key] = plan;
@@ -287,33 +310,49 @@ void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const dou
     ProfScope ps(ctx, "svd");
     DevBuf wsb((size_t)plan->ws_elems * sizeof(double), ctx);
     double* ws = (double*)wsb.ptr;
-    auto stage = [&](int st) {
+    // st 1: FP32 sweeps on A (pass 0) or on X1 = A Q1 (pass 1); st 2: FP64
+    // sweeps on [X2 | Q1 Q2]
+    auto stage = [&](int st, int pass) {
       ProfScope pst(ctx, st == 1 ? "svd_stage1_fp32" : "svd_stage2_fp64");
       const std::vector<SvdClass>& cls = st == 1 ? plan->classes1 : plan->classes2;
+      const DevBufP& jl = st == 2 ? plan->jobs2 : (pass == 0 ? plan->jobs1 : plan->jobs1b);
       const int nc = (int)cls.size();
       ctx.fork(nc);
       for (int c = 0; c < nc; c++) {
         const SvdClass& k = cls[c];
-        const SvdJob* jobs = (const SvdJob*)(st == 1 ? plan->jobs1 : plan->jobs2)->ptr + k.first;
-        launch_svd_jacobi(st, jobs, k.njobs, k.P, k.threads, k.smem, st == 1 ? A : ws, ws,
-                          ws, U, S, VT, info, ctx.side_stream(c));
+        const SvdJob* jobs = (const SvdJob*)jl->ptr + k.first;
+        launch_svd_jacobi(st, pass, jobs, k.njobs, k.P, k.threads, k.smem, st == 1 && pass == 0 ? A : ws, ws, ws, U,
+                          S, VT, info, ctx.side_stream(c), k.K);
         ctx.launched();
       }
       ctx.join(nc);
     };
     const int nj = (int)plan->jac.size();
-    stage(1);  // FP32 sweeps: V, V^T
-    run_sector_gemms(ctx, TN_MODE_FP64, plan->gram1, ws, ws, ws);
-    launch_ns_factor((const int64_t*)plan->ns_tab->ptr, nj, ws, ctx.stream);
-    ctx.launched();
-    run_sector_gemms(ctx, TN_MODE_FP64, plan->prod1, ws, ws, ws);
-    run_sector_gemms(ctx, TN_MODE_FP64, plan->gram2, ws, ws, ws);
-    launch_ns_factor((const int64_t*)plan->ns_tab->ptr, nj, ws, ctx.stream);
-    ctx.launched();
-    run_sector_gemms(ctx, TN_MODE_FP64, plan->prod2, ws, ws, ws);
-    if (!plan->x1_direct.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_direct, A, ws, ws);
-    if (!plan->x1_trans.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_trans, ws, A, ws);
-    stage(2);  // FP64 sweeps on [X1 | Q]: U, S, VT
+    const int64_t* tab = (const int64_t*)plan->ns_tab->ptr;
+    auto ns = [&](const std::vector<tn_sector_gemm>& gram, const std::vector<tn_sector_gemm>& prod, int step) {
+      run_sector_gemms(ctx, TN_MODE_FP64, gram, ws, ws, ws);
+      launch_ns_factor(tab, nj, ws, ctx.stream);
+      ctx.launched();
+      run_sector_gemms(ctx, TN_MODE_FP64, prod, ws, ws, ws);
+      launch_ns_transpose((const int64_t*)plan->tr_tab->ptr + 3 * (int64_t)nj * step, nj, ws, ctx.stream);
+      ctx.launched();
+    };
+    // The FP32 rotations of A leave the columns of its small singular values
+    // inaccurate relative to their own norms (FP32 rounding of the large
+    // ones); a second FP32 pass on X1 = A Q1, whose columns are nearly
+    // orthogonal, rotates by small angles and is accurate relative to each
+    // column, so the FP64 stage starts near 1e-5 and needs two rotating
+    // sweeps and a confirming one.
+    stage(1, 0);  // FP32 sweeps on A: V, V^T
+    ns(plan->gram1, plan->prod1, 0);
+    ns(plan->gram2, plan->prod2, 1);  // Q1 in V
+    if (!plan->x1_a.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_a, A, ws, ws);
+    if (!plan->x1_b.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_b, ws, A, ws);
+    stage(1, 1);  // FP32 sweeps on X1
+    ns(plan->gram3, plan->prod3, 2);
+    ns(plan->gram4, plan->prod4, 3);  // Q2 in Q
+    run_sector_gemms(ctx, TN_MODE_FP64, plan->fin, ws, ws, ws);  // X2, (Q1 Q2)^T
+    stage(2, 0);  // FP64 sweeps on [X2 | Q1 Q2]: U, S, VT
   }
   for (int i : plan->fallback) {
     svd_fallback(ctx, list[i], A, U, S, VT);
