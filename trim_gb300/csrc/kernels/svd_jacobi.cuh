@@ -171,22 +171,35 @@ __device__ __forceinline__ int rot_params(double a, double b, double g, double t
   return counted;
 }
 
-// FP32 (stage 1, preconditioning only): fast reciprocal, square root and
-// division are accurate enough here
-__device__ __forceinline__ int rot_params(float a, float b, float g, float tol2, float* h, float* s, float* na,
+// FP32 (stage 1, preconditioning only): a Givens rotation, c = 1/sqrt(1+t^2),
+// s = c t with t = 2g / (D + sign(D) sqrt(D^2 + 4g^2)), D = b - a (the same
+// smaller root), three dependent fast reciprocal / square-root steps.
+__device__ __forceinline__ int rot_params(float a, float b, float g, float tol2, float* c, float* s, float* na,
                                           float* nb) {
   if (!(a > 0.0f) || !(b > 0.0f)) return 0;
   if (!(g * g > tol2 * a * b)) return 0;
-  const float z = __fdividef(b - a, 2.0f * g);
-  const float z2 = fmaf(z, z, 1.0f);
-  const float t = fabsf(z) > 1e18f ? __fdividef(0.5f, z) : copysignf(__fdividef(1.0f, fabsf(z) + z2 * rsqrtf(z2)), z);
-  const float c = rsqrtf(fmaf(t, t, 1.0f));
-  const float sn = c * t;
-  *h = __fdividef(sn, 1.0f + c);
-  *s = sn;
+  const float D = b - a;
+  const float Q = fmaf(D, D, 4.0f * g * g);
+  const float t = __fdividef(2.0f * g, D + copysignf(Q * rsqrtf(Q), D));
+  const float cs = rsqrtf(fmaf(t, t, 1.0f));
+  *c = cs;
+  *s = cs * t;
   *na = fmaf(-t, g, a);
   *nb = fmaf(t, g, b);
   return 2;
+}
+
+// FP32 dot product of a pair from the lanes' partial sums: the partials as
+// fixed-point integers scaled by 2^(28 - e), 2^e > sqrt(a b) >= the sum of
+// their magnitudes (Cauchy-Schwarz), summed exactly by one warp reduction
+// instead of five shuffle-add steps.  Resolution 2^-28 sqrt(a b); with a
+// margin of 8 for norms a, b that lag the columns' own, no overflow.
+__device__ __forceinline__ float fixed_point_sum(float partial, float a, float b) {
+  const int ea = (__float_as_int(a) >> 23) & 0xff, eb = (__float_as_int(b) >> 23) & 0xff;
+  const int e = ((ea + eb + 1) >> 1) - 126;  // a < 2^(ea - 126), b < 2^(eb - 126)
+  const int k = min(max(28 - e, -126), 126);
+  const int q = __float2int_rn(partial * __int_as_float((k + 127) << 23));
+  return (float)__reduce_add_sync(0xffffffffu, q) * __int_as_float((127 - k) << 23);
 }
 
 // A record (one column [x | v | zeros], 32 K entries) in the registers of a
@@ -221,24 +234,53 @@ __device__ __forceinline__ T reg_dot(const T (&x)[K], const T (&y)[K], int n, in
 }
 
 // One Jacobi rotation of the pair (x, y) held in registers: dot product over
-// the first mx entries, rotation, shears x -= h y, y += s x, x -= h y over
-// the whole records (x and v parts; the zero padding stays zero).  an, bn:
-// the squared norms, updated (a norm update that cancels is recomputed).
+// the first mx entries, rotation over the whole records (x and v parts; the
+// zero padding stays zero): FP64 as three shears x -= h y, y += s x,
+// x -= h y (3 FMAs an entry pair on the scarce FP64 pipe), FP32 as
+// x' = c x - s y, y' = s x + c y (a shorter dependent chain).  an, bn: the
+// squared norms, updated (a norm update that cancels is recomputed).
 // Returns rot_params' code (0: not rotated).
 template <typename T, int K>
 __device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, int mx, int lane, T tol2) {
-  const T g = reg_dot<T, K>(x, y, mx, lane);
+  T g;
+  if constexpr (sizeof(T) == 4) {
+    float p0 = 0.0f, p1 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      if (32 * k >= mx) break;
+      if (lane + 32 * k < mx) {
+        if (k & 1)
+          p1 = fmaf(x[k], y[k], p1);
+        else
+          p0 = fmaf(x[k], y[k], p0);
+      }
+    }
+    if (!(an > 0.0f) || !(bn > 0.0f)) return 0;
+    g = fixed_point_sum(p0 + p1, an, bn);
+  } else {
+    g = reg_dot<T, K>(x, y, mx, lane);
+  }
   T h, sn, na, nb;
   const int rc = rot_params(an, bn, g, tol2, &h, &sn, &na, &nb);
   if (!rc) return 0;
+  if constexpr (sizeof(T) == 4) {
+    const float c = h;  // FP32: (c, s)
 #pragma unroll
-  for (int k = 0; k < K; k++) {
-    T xv = x[k], yv = y[k];
-    xv = fma(-h, yv, xv);
-    yv = fma(sn, xv, yv);
-    xv = fma(-h, yv, xv);
-    x[k] = xv;
-    y[k] = yv;
+    for (int k = 0; k < K; k++) {
+      const float xv = x[k], yv = y[k];
+      x[k] = fmaf(-sn, yv, c * xv);
+      y[k] = fmaf(sn, xv, c * yv);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      T xv = x[k], yv = y[k];
+      xv = fma(-h, yv, xv);
+      yv = fma(sn, xv, yv);
+      xv = fma(-h, yv, xv);
+      x[k] = xv;
+      y[k] = yv;
+    }
   }
   if (na < (T)0.25 * an) na = reg_dot<T, K>(x, x, mx, lane);
   if (nb < (T)0.25 * bn) nb = reg_dot<T, K>(y, y, mx, lane);
@@ -337,6 +379,10 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
   const T tol = kFinal ? (T)(sqrt((double)mx) * 8.8817841970012523e-16) : (T)1e-5;
   const T tol2 = tol * tol;
   const int max_sweeps = kFinal ? kSvdMaxSweeps : kSvdMaxSweeps32;
+  // the first FP32 pass stops once a sweep rotates at most a tenth of the
+  // pairs: its last sweeps only chase the columns of the small singular
+  // values, which it cannot resolve and the second pass does
+  const int stop_at = (!kFinal && pass == 0) ? (int)((int64_t)nx * (nx - 1) / 20) : 0;
 
   int cur = 0, sweeps = -1;
   const size_t buf = (size_t)nb2 * L;
@@ -439,7 +485,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
     int total = 0;
     const int* rc = cl.map_shared_rank(cnt, 0);
     for (int q = 0; q < P; q++) total += rc[(sweep & 1) * 16 + q];
-    if (total == 0) {
+    if (total <= stop_at) {
       sweeps = sweep + 1;
       break;
     }
