@@ -311,8 +311,9 @@ class MeraRefSampler:
         return sum(self.acc), dt
 
 
-def mera_cpu_sample(chi, seconds, min_steps=2):
+def mera_cpu_sample(chi, seconds, min_steps=2, threads=None):
     """Bounded sample of the MERA workload on the host cores (numpy port)."""
+    threads = threads or os.cpu_count()
     s = MeraRefSampler(chi)
     fl = tm = 0.0
     n = 0
@@ -321,9 +322,25 @@ def mera_cpu_sample(chi, seconds, min_steps=2):
         fl += f
         tm += dt
         n += 1
-    return {"value": fl / tm / 1e12, "unit": "TFLOP/s", "cores": os.cpu_count(), "kind": "port",
+    return {"value": fl / tm / 1e12, "unit": "TFLOP/s", "cores": threads, "kind": "port",
             "sample": f"{n} pairwise contract() calls of the chi={chi} MERA diagrams in network order "
-                      f"({fl:.3g} FP64 flop, {tm:.1f} s), numpy BLAS dgemm on {os.cpu_count()} host threads"}
+                      f"({fl:.3g} FP64 flop, {tm:.1f} s), numpy BLAS dgemm on {threads} host thread(s)"}
+
+
+def mera_cpu_sample_one_thread(chi, seconds):
+    """The same sample with the BLAS pinned to one thread (a child process,
+    since the thread count is fixed when numpy's BLAS loads)."""
+    env = dict(os.environ, OPENBLAS_NUM_THREADS="1", OMP_NUM_THREADS="1", MKL_NUM_THREADS="1")
+    code = f"import json, bench; print(json.dumps(bench.mera_cpu_sample({int(chi)}, {float(seconds)}, 1, 1)))"
+    try:
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True, timeout=900,
+                           cwd=os.path.dirname(os.path.abspath(__file__)))
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode == 0 and lines:
+            return json.loads(lines[-1])
+        return {"unavailable": f"child exited {r.returncode}: {r.stderr.strip()[-200:]}"}
+    except Exception as e:  # a reported baseline only
+        return {"unavailable": f"{type(e).__name__}: {str(e)[:200]}"}
 
 
 def mera_section(args, torch, tu, stream, local, world, peaks):
@@ -1101,6 +1118,8 @@ def gpu_main(args, rank, local, world):
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu:
         cpu = mera_cpu_sample(args.chi, args.cpu_seconds)
+        if args.cpu1_seconds > 0:
+            cpu["one_thread"] = mera_cpu_sample_one_thread(args.chi, args.cpu1_seconds)
     R = modes[args.mode]
     sections = {}
     if wanted == "all":
@@ -1150,6 +1169,8 @@ def main():
                     help="iTEBD: the tensor-core mode timed beside FP64 (split_fused / split_tiled force that form)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="MERA CPU baseline sample length")
     ap.add_argument("--itebd-cpu-seconds", type=float, default=8.0)
+    ap.add_argument("--cpu1-seconds", type=float, default=8.0,
+                    help="MERA CPU baseline with the BLAS on one thread (0: skip)")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--clock-seconds", type=float, default=1.0,
                     help="repeat the timed region for at least this long while SM clocks are sampled (0: once)")

@@ -258,6 +258,7 @@ __device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, i
     if (!(an > 0.0f) || !(bn > 0.0f)) return 0;
     g = fixed_point_sum(p0 + p1, an, bn);
   } else {
+    if (!(an > 0.0) || !(bn > 0.0)) return 0;  // a padding (or zero) column: no FP64 work
     g = reg_dot<T, K>(x, y, mx, lane);
   }
   T h, sn, na, nb;
@@ -270,6 +271,15 @@ __device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, i
       const float xv = x[k], yv = y[k];
       x[k] = fmaf(-sn, yv, c * xv);
       y[k] = fmaf(sn, xv, c * yv);
+    }
+  } else if (fabs(h) < 0x1p-27) {
+    // c = 1 - h s rounds to 1: x' = x - s y, y' = s x + y is the rotation to
+    // FP64 rounding, 2 FMAs an entry pair instead of 3
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      const T xv = x[k], yv = y[k];
+      x[k] = fma(-sn, yv, xv);
+      y[k] = fma(sn, xv, yv);
     }
   } else {
 #pragma unroll
@@ -348,7 +358,10 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
   if (E == 0) E = 1023;  // zero or subnormal maximum: no scaling
   const double sc = __hiloint2double((2046 - E) << 20, 0), unsc = __hiloint2double(E << 20, 0);
 
-  // round-0 layout: slot 0 holds column block `rank`, slot 1 block 2P-1-rank
+  // round-0 layout: slot 0 holds column block `rank`, slot 1 block 2P-1-rank;
+  // column c of block k is column c 2P + k of X, so that the padding columns
+  // (from nx to 2P b) spread over the blocks: the pairs they are in are
+  // skipped, which evens the work of the CTAs
   for (int idx = threadIdx.x; idx < nb2 * L; idx += nthr) {
     int col, r;
     if (tr) {  // record entries along r are contiguous rows of the matrix
@@ -359,7 +372,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
       r = idx / nb2;
     }
     const int slot = col / b, c = col % b;
-    const int g = (slot == 0 ? rank : nblk - 1 - rank) * b + c;
+    const int g = c * nblk + (slot == 0 ? rank : nblk - 1 - rank);
     double v = 0.0;
     if (g < nx) {
       if (r < mx)
@@ -497,7 +510,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
     double* v = Vout + jb.v_off;
     double* vtr = v + (size_t)nx * nx;
     for (int col = warp; col < nb2; col += nwarps) {
-      const int g = ((col / b) == 0 ? rank : nblk - 1 - rank) * b + col % b;
+      const int g = (col % b) * nblk + ((col / b) == 0 ? rank : nblk - 1 - rank);
       if (g >= nx) continue;
       const T* x = R + (size_t)col * L + mx;
       for (int i = lane; i < nx; i += 32) {
@@ -518,7 +531,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
   // (descending sigma, ties by column index) and writes them out
   double* rsig = cl.map_shared_rank(sig, 0);
   for (int col = warp; col < nb2; col += nwarps) {
-    const int g = ((col / b) == 0 ? rank : nblk - 1 - rank) * b + col % b;
+    const int g = (col % b) * nblk + ((col / b) == 0 ? rank : nblk - 1 - rank);
     const double s = sqrt((double)wdot<T>(R + (size_t)col * L, R + (size_t)col * L, mx, lane));
     if (lane == 0 && g < nx) rsig[g] = s;
   }
@@ -529,7 +542,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
   double* u = U + jb.u_off;
   double* vt = VT + jb.vt_off;
   for (int col = warp; col < nb2; col += nwarps) {
-    const int g = ((col / b) == 0 ? rank : nblk - 1 - rank) * b + col % b;
+    const int g = (col % b) * nblk + ((col / b) == 0 ? rank : nblk - 1 - rank);
     if (g >= nx) continue;
     const double s = allsig[g];
     int before = 0;
