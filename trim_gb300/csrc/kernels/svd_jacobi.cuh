@@ -117,6 +117,10 @@ __device__ __forceinline__ double f64_of_bits(float f) {
   return __hiloint2double((int)hi, (int)(u << 29));
 }
 
+// Positive doubles order like their bit patterns: tests without an FP64
+// instruction (one warp issues an FP64 instruction per 64 cycles on GB300).
+__device__ __forceinline__ long long dbits(double x) { return __double_as_longlong(x); }
+
 // Rotation of two columns with squared norms a, b and dot product g (FP64).
 // The Jacobi tangent t (the smaller root of g t^2 + (b - a) t - g = 0) and the
 // half-angle tangent h = t / (1 + sqrt(1 + t^2)) are found in FP32 from
@@ -125,21 +129,25 @@ __device__ __forceinline__ double f64_of_bits(float f) {
 // seed and one third-order correction), c = 1 - h s, new squared norms
 // a + s u and b - s u with u = s d - 2 c g (the identities of a rotation, not
 // of the exact Jacobi angle).  So the rotation is orthogonal to FP64
-// rounding, its angle accurate to FP32, and the dependent chain holds 8 FP64
-// operations.  Returns 0 when |g| <= tol sqrt(a b) (no rotation), 2 when
-// |g| > 4 tol sqrt(a b) (a rotation that counts against convergence), else 1:
-// the rotations just above the tolerance, which rounding noise in the dot
-// products produces, are applied but do not call for another sweep.
-__device__ __forceinline__ int rot_params(double a, double b, double g, double tol2, double* h, double* s,
+// rounding, its angle accurate to FP32, and the FP64 chain holds 11
+// instructions (4 when |h| < 2^-27, where s = 2h and c = 1 to FP64 rounding).
+// The tolerance tests run in FP32 on the scaled values.  Returns 0 (no
+// rotation: |g| <= tol sqrt(a b)), else 1 | 2 when |g| > 4 tol sqrt(a b) (a
+// rotation that counts against convergence; those just above the tolerance,
+// which rounding noise in the dot products produces, are applied but do not
+// call for another sweep) | 4 when the angle is tiny.
+__device__ __forceinline__ int rot_params(double a, double b, double g, float tol2, double* h, double* s,
                                           double* na, double* nb) {
-  if (!(a > 0.0) || !(b > 0.0)) return 0;
-  if (!(g * g > tol2 * a * b)) return 0;
-  const double d = b - a;
+  if (dbits(a) <= 0 || dbits(b) <= 0) return 0;
   const int eg = ((__double2hiint(g) >> 20) & 0x7ff) - 1023;
-  const float g32 = f32_scaled(g, eg), d32 = f32_scaled(d, eg);  // |g32| in [1, 2)
-  const int counted = g32 * g32 > 16.0f * (float)tol2 * f32_scaled(a, eg) * f32_scaled(b, eg) ? 2 : 1;
-  const float z = __fdividef(d32, 2.0f * g32);
-  double hd, q0;
+  const float g32 = f32_scaled(g, eg);  // |g32| in [1, 2); 0 for a zero or subnormal g
+  const float ab32 = f32_scaled(a, eg) * f32_scaled(b, eg), g2 = g32 * g32;
+  if (!(g2 > tol2 * ab32)) return 0;
+  const int code = g2 > 16.0f * tol2 * ab32 ? 3 : 1;
+  const double d = b - a;
+  const float z = __fdividef(f32_scaled(d, eg), 2.0f * g32);
+  double hd, hd2, q0;
+  bool tiny;
   if (fabsf(z) > 1e30f) {  // tangent below FP32's range: h = t / 2 = g / (2 d) to first order, in FP64
     const int ed = min(((__double2hiint(d) >> 20) & 0x7ff) - 1023, 1022);
     const double p2 = __hiloint2double((1023 - ed) << 20, 0);  // 2^-ed: d p2 in [1, 2) in magnitude
@@ -148,7 +156,9 @@ __device__ __forceinline__ int rot_params(double a, double b, double g, double t
     r = r * fma(-ds, r, 2.0);
     r = r * fma(-ds, r, 2.0);
     hd = 0.5 * (g * p2) * r;
+    hd2 = 2.0 * hd;
     q0 = 1.0;
+    tiny = true;
   } else {
     const float z2 = fmaf(z, z, 1.0f);
     const float t = fabsf(z) > 1e18f ? __fdividef(0.5f, z)
@@ -156,19 +166,52 @@ __device__ __forceinline__ int rot_params(double a, double b, double g, double t
     const float t2 = fmaf(t, t, 1.0f);
     const float h32 = __fdividef(t, 1.0f + t2 * rsqrtf(t2));
     hd = f64_of_bits(h32);
+    hd2 = f64_of_bits(2.0f * h32);
     q0 = f64_of_bits(__fdividef(1.0f, fmaf(h32, h32, 1.0f)));
+    tiny = fabsf(h32) < 0x1p-27f;
   }
-  const double w = fma(hd, hd, 1.0);
-  const double e = fma(-w, q0, 1.0);  // q0 = (1 - e) / w
-  const double s0 = (hd + hd) * q0;
-  const double sn = fma(s0, fma(e, e, e), s0);  // 2h / w to 2^-69
-  const double m2c = fma(hd + hd, sn, -2.0);     // -2c
-  const double u = fma(sn, d, m2c * g);
+  double sn, u;
+  if (tiny) {  // s = 2h (1 - h^2 + ...) rounds to 2h, c to 1: u = s d - 2 g
+    sn = hd2;
+    const int hg = __double2hiint(g);
+    u = fma(sn, d, __hiloint2double((hg ^ (int)0x80000000) + (1 << 20), __double2loint(g)));  // -2 g from its bits
+  } else {
+    const double w = fma(hd, hd, 1.0);
+    const double e = fma(-w, q0, 1.0);  // q0 = (1 - e) / w
+    const double s0 = hd2 * q0;
+    sn = fma(s0, fma(e, e, e), s0);             // 2h / w to 2^-69
+    const double m2c = fma(hd2, sn, -2.0);      // -2c
+    u = fma(sn, d, m2c * g);
+  }
   *h = hd;
   *s = sn;
   *na = fma(sn, u, a);
   *nb = fma(-sn, u, b);
-  return counted;
+  return code | (tiny ? 4 : 0);
+}
+
+// FP64 dot product of a pair from the lanes' partial sums, summed exactly as
+// 58-bit fixed-point integers (scaled by 2^(58 - e), 2^e > sqrt(a b) >= the
+// sum of the partials' magnitudes by Cauchy-Schwarz): three 32-bit warp
+// reductions of 20-bit pieces and integer exponent shifts, where a tree of
+// FP64 adds would take five dependent FP64 instructions.  Resolution
+// 2^-58 sqrt(a b) a lane, 2^-53 for the sum: as fine as the FP64 sum.
+__device__ __forceinline__ double fixed_point_sum(double partial, double a, double b) {
+  const int ea = (__double2hiint(a) >> 20) & 0x7ff, eb = (__double2hiint(b) >> 20) & 0x7ff;
+  const int e = ((ea + eb + 1) >> 1) - 1022;  // a < 2^(ea - 1022), b < 2^(eb - 1022)
+  const int hi = __double2hiint(partial);
+  const int ep = (hi >> 20) & 0x7ff, en = ep + 58 - e;  // partial 2^(58 - e) by its exponent field
+  long long q = 0;
+  if (ep != 0 && en > 0)
+    q = __double2ll_rn(__hiloint2double((hi & (int)0x800fffff) | (en << 20), __double2loint(partial)));
+  const long long sum = ((long long)__reduce_add_sync(0xffffffffu, (int)(q >> 40)) << 40) +
+                        ((long long)__reduce_add_sync(0xffffffffu, (int)((q >> 20) & 0xfffff)) << 20) +
+                        (long long)__reduce_add_sync(0xffffffffu, (int)(q & 0xfffff));
+  if (sum == 0) return 0.0;
+  const double sd = __ll2double_rn(sum);  // |sum| < 2^59
+  const int sh = __double2hiint(sd), es = ((sh >> 20) & 0x7ff) + e - 58;
+  if (es <= 0) return 0.0;  // below the smallest normal: negligible against sqrt(a b)
+  return __hiloint2double(sh + ((e - 58) << 20), __double2loint(sd));
 }
 
 // FP32 (stage 1, preconditioning only): a Givens rotation, c = 1/sqrt(1+t^2),
@@ -186,7 +229,7 @@ __device__ __forceinline__ int rot_params(float a, float b, float g, float tol2,
   *s = cs * t;
   *na = fmaf(-t, g, a);
   *nb = fmaf(t, g, b);
-  return 2;
+  return 3;
 }
 
 // FP32 dot product of a pair from the lanes' partial sums: the partials as
@@ -241,7 +284,7 @@ __device__ __forceinline__ T reg_dot(const T (&x)[K], const T (&y)[K], int n, in
 // squared norms, updated (a norm update that cancels is recomputed).
 // Returns rot_params' code (0: not rotated).
 template <typename T, int K>
-__device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, int mx, int lane, T tol2) {
+__device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, int mx, int lane, float tol2) {
   T g;
   if constexpr (sizeof(T) == 4) {
     float p0 = 0.0f, p1 = 0.0f;
@@ -258,8 +301,14 @@ __device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, i
     if (!(an > 0.0f) || !(bn > 0.0f)) return 0;
     g = fixed_point_sum(p0 + p1, an, bn);
   } else {
-    if (!(an > 0.0) || !(bn > 0.0)) return 0;  // a padding (or zero) column: no FP64 work
-    g = reg_dot<T, K>(x, y, mx, lane);
+    if (dbits(an) <= 0 || dbits(bn) <= 0) return 0;  // a padding (or zero) column: no FP64 work
+    double p = 0.0;  // one chain: a warp's FP64 instructions serialise anyway
+#pragma unroll
+    for (int k = 0; k < K; k++) {
+      if (32 * k >= mx) break;
+      if (lane + 32 * k < mx) p = fma(x[k], y[k], p);
+    }
+    g = fixed_point_sum(p, an, bn);
   }
   T h, sn, na, nb;
   const int rc = rot_params(an, bn, g, tol2, &h, &sn, &na, &nb);
@@ -272,7 +321,7 @@ __device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, i
       x[k] = fmaf(-sn, yv, c * xv);
       y[k] = fmaf(sn, xv, c * yv);
     }
-  } else if (fabs(h) < 0x1p-27) {
+  } else if (rc & 4) {
     // c = 1 - h s rounds to 1: x' = x - s y, y' = s x + y is the rotation to
     // FP64 rounding, 2 FMAs an entry pair instead of 3
 #pragma unroll
@@ -292,11 +341,16 @@ __device__ __forceinline__ int pair_rotate(T (&x)[K], T (&y)[K], T& an, T& bn, i
       y[k] = yv;
     }
   }
-  if (na < (T)0.25 * an) na = reg_dot<T, K>(x, x, mx, lane);
-  if (nb < (T)0.25 * bn) nb = reg_dot<T, K>(y, y, mx, lane);
+  if constexpr (sizeof(T) == 4) {
+    if (na < 0.25f * an) na = reg_dot<T, K>(x, x, mx, lane);
+    if (nb < 0.25f * bn) nb = reg_dot<T, K>(y, y, mx, lane);
+  } else {  // below a quarter: the exponent field lower by 2 (or negative)
+    if (dbits(na) < dbits(an) - (2ll << 52)) na = reg_dot<T, K>(x, x, mx, lane);
+    if (dbits(nb) < dbits(bn) - (2ll << 52)) nb = reg_dot<T, K>(y, y, mx, lane);
+  }
   an = na;
   bn = nb;
-  return rc;
+  return rc & 3;
 }
 
 __device__ __forceinline__ double block_max(double v, double* red) {
@@ -391,6 +445,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
   // rounding noise
   const T tol = kFinal ? (T)(sqrt((double)mx) * 8.8817841970012523e-16) : (T)1e-5;
   const T tol2 = tol * tol;
+  const float tol2f = (float)tol2;  // the tests run in FP32 (scaled values)
   const int max_sweeps = kFinal ? kSvdMaxSweeps : kSvdMaxSweeps32;
   // the first FP32 pass stops once a sweep rotates at most a tenth of the
   // pairs: its last sweeps only chase the columns of the small singular
@@ -424,7 +479,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
             load_rec<T, K>(xr, R + (size_t)ci * L, lane);
             load_rec<T, K>(yr, R + (size_t)cj * L, lane);
             T an = NR[ci], bn = NR[cj];
-            const int rc = pair_rotate<T, K>(xr, yr, an, bn, mx, lane, tol2);
+            const int rc = pair_rotate<T, K>(xr, yr, an, bn, mx, lane, tol2f);
             if (rc) {
               store_rec<T, K>(xr, R + (size_t)ci * L, lane);
               store_rec<T, K>(yr, R + (size_t)cj * L, lane);
@@ -453,7 +508,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
           T yr[K];
           load_rec<T, K>(yr, y, lane);
           T bn = NR[b + c];
-          const int rc = pair_rotate<T, K>(xr, yr, an, bn, mx, lane, tol2);
+          const int rc = pair_rotate<T, K>(xr, yr, an, bn, mx, lane, tol2f);
           if (rc) {
             store_rec<T, K>(yr, y, lane);
             if (lane == 0) {
