@@ -473,8 +473,9 @@ int svd_max_cluster();  // largest cluster size the device schedules (<= 16)
 void launch_svd_jacobi(int stage, int pass, const SvdJob* jobs, int njobs, int P, int threads, size_t smem,
                        const double* X, const double* Vin, double* Vout, double* U, double* S, double* VT, int* info,
                        cudaStream_t s, int K);
-// T = 3/2 I - (G + G^T)/4 for every (n, g_off, t_off) triple of tab (device)
-void launch_ns_factor(const int64_t* tab, int njobs, double* ws, cudaStream_t s);
+// the factor T of a Newton-Schulz step of order 2 or 3 for every (n, g_off,
+// g2_off, t_off) entry of tab (device)
+void launch_ns_factor(const int64_t* tab, int njobs, double* ws, int order, cudaStream_t s);
 // dst = src^T (n x n) for every (n, src_off, dst_off) triple of tab (device)
 void launch_ns_transpose(const int64_t* tab, int njobs, double* ws, cudaStream_t s);
 void launch_truncate(const int64_t* s_off, const int64_t* s_cnt, int nsec, double* S, int64_t chi, int64_t* kept,

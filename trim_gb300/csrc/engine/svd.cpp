@@ -75,25 +75,26 @@ struct SvdClass {
   size_t smem = 0;
 };
 
-// Workspace of one Jacobi sector (doubles): V | V^T, Q | Q^T, R | R^T
-// (Newton-Schulz ping-pong; Q1 ends in V, Q2 in Q, Q^T = (Q1 Q2)^T in R), G,
-// T, X1 = A Q1, X2 = A Q1 Q2 (M x N each).
+// Workspace of one Jacobi sector (doubles): V | V^T (the FP32 passes'
+// rotations, later (Q1 Q2)^T), Q | Q^T and R | R^T (Newton-Schulz
+// ping-pong; Q1 ends in R, Q2 in Q), G = Y^T Y, G2 = G G, T (the
+// Newton-Schulz factor), X1 = A Q1, X2 = A Q1 Q2 (M x N each).
 struct SvdWs {
-  int64_t v, q, r, g, t, x1, x2;
+  int64_t v, q, r, g, g2, t, x1, x2;
 };
 
 struct SvdPlan {
   std::vector<tn_svd_sector> list;
   DevBufP jobs1, jobs1b, jobs2;  // FP32 passes 0 and 1, FP64 stage; grouped by class
-  DevBufP ns_tab;                // (n, g_off, t_off) per Jacobi sector
-  DevBufP tr_tab;                // (n, src, dst) per sector for each of the 4 Newton-Schulz steps
+  DevBufP ns_tab;                // (n, g_off, g2_off, t_off) per Jacobi sector
+  DevBufP tr_tab;                // (n, src, dst) per sector for each of the 3 Newton-Schulz steps
   std::vector<SvdClass> classes1, classes2;  // per stage, largest cluster first
   std::vector<tn_svd_sector> jac;  // the Jacobi sectors
   std::vector<SvdWs> ws;
   int64_t ws_elems = 0;
   // grouped FP64 GEMMs of the orthogonalisations and products, in workspace
   // offsets (x1_a, x1_b: the first operand in the input)
-  std::vector<tn_sector_gemm> gram1, prod1, gram2, prod2, x1_a, x1_b, gram3, prod3, gram4, prod4, fin;
+  std::vector<tn_sector_gemm> gram1, prod1, gram2, prod2, x1_a, x1_b, gram3, sq3, prod3, fin;
   std::vector<int> fallback;  // sectors for cuSOLVER
   std::vector<int> empty;     // sectors with M or N == 0
 };
@@ -111,12 +112,16 @@ DevBufP upload(Ctx& ctx, const void* p, size_t bytes) {
   return b;
 }
 
-// Newton-Schulz step on the pair (Y, Y^T) at `from` into `to`: G = Y^T Y,
-// T = 3/2 I - (G + G^T)/4 (launch_ns_factor), Y T, and its transpose (T is
-// symmetric, so (Y T)^T = T Y^T) by a copy
-void ns_step(std::vector<tn_sector_gemm>& gram, std::vector<tn_sector_gemm>& prod, std::vector<int64_t>& tr,
-             int64_t n, int64_t from, int64_t to, const SvdWs& w) {
+// One Newton-Schulz step on the pair (Y, Y^T) at `from` into `to`: G = Y^T Y,
+// the symmetric factor T (launch_ns_factor), Y T, and its transpose by a copy
+// (T is symmetric).  With Y^T Y = I + E: second order, T = 3/2 I - G/2,
+// leaves O(E^2); third order (sq != nullptr), G2 = G G and
+// T = (15 I - 10 G + 3 G2) / 8, leaves O(E^3) with three GEMMs instead of the
+// four of two second-order steps.
+void ns_step(std::vector<tn_sector_gemm>& gram, std::vector<tn_sector_gemm>* sq, std::vector<tn_sector_gemm>& prod,
+             std::vector<int64_t>& tr, int64_t n, int64_t from, int64_t to, const SvdWs& w) {
   gram.push_back(tn_sector_gemm{n, n, n, from + n * n, from, w.g});
+  if (sq) sq->push_back(tn_sector_gemm{n, n, n, w.g, w.g, w.g2});
   prod.push_back(tn_sector_gemm{n, n, n, from, w.t, to});
   tr.push_back(n);
   tr.push_back(to);
@@ -142,7 +147,7 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     int threads = 0;
   };
   std::map<std::pair<int, int>, Acc> cls1, cls2;
-  std::vector<int64_t> tab, tr[4];
+  std::vector<int64_t> tab, tr[3];
   for (size_t i = 0; i < list.size(); i++) {
     const tn_svd_sector& s = list[i];
     if (s.M < 0 || s.N < 0) fail(TN_ERR_ARG, "svd: negative sector dimension");
@@ -163,31 +168,34 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     w.q = w.v + 2 * n * n;
     w.r = w.q + 2 * n * n;
     w.g = w.r + 2 * n * n;
-    w.t = w.g + n * n;
+    w.g2 = w.g + n * n;
+    w.t = w.g2 + n * n;
     w.x1 = w.t + n * n;
     w.x2 = w.x1 + mn;
     plan->ws_elems = w.x2 + mn;
     plan->ws.push_back(w);
     plan->jac.push_back(s);
-    // Q1: two Newton-Schulz steps from the FP32 rotations V (V -> Q -> V)
-    ns_step(plan->gram1, plan->prod1, tr[0], n, w.v, w.q, w);
-    ns_step(plan->gram2, plan->prod2, tr[1], n, w.q, w.v, w);
+    // Q1 from the first FP32 pass's rotations, whose E reaches 1e-4: two
+    // second-order steps (V -> Q -> R)
+    ns_step(plan->gram1, nullptr, plan->prod1, tr[0], n, w.v, w.q, w);
+    ns_step(plan->gram2, nullptr, plan->prod2, tr[1], n, w.q, w.r, w);
     // X1 = A Q1 (stored as X1^T = Q1^T A when M < N, the kernel's A^T layout)
     if (s.M >= s.N)
-      plan->x1_a.push_back(tn_sector_gemm{s.M, s.N, s.N, s.a_off, w.v, w.x1});
+      plan->x1_a.push_back(tn_sector_gemm{s.M, s.N, s.N, s.a_off, w.r, w.x1});
     else
-      plan->x1_b.push_back(tn_sector_gemm{s.M, s.N, s.M, w.v + n * n, s.a_off, w.x1});
-    // Q2 from the second FP32 pass's rotations (Q -> R -> Q)
-    ns_step(plan->gram3, plan->prod3, tr[2], n, w.q, w.r, w);
-    ns_step(plan->gram4, plan->prod4, tr[3], n, w.r, w.q, w);
-    // X2 = X1 Q2 and (Q1 Q2)^T = Q2^T Q1^T into R
+      plan->x1_b.push_back(tn_sector_gemm{s.M, s.N, s.M, w.r + n * n, s.a_off, w.x1});
+    // Q2 from the second FP32 pass's rotations, small angles from the
+    // identity (E ~ 1e-6): one third-order step (V -> Q)
+    ns_step(plan->gram3, &plan->sq3, plan->prod3, tr[2], n, w.v, w.q, w);
+    // X2 = X1 Q2 and (Q1 Q2)^T = Q2^T Q1^T into V
     if (s.M >= s.N)
       plan->fin.push_back(tn_sector_gemm{s.M, s.N, s.N, w.x1, w.q, w.x2});
     else
       plan->fin.push_back(tn_sector_gemm{s.M, s.N, s.M, w.q + n * n, w.x1, w.x2});
-    plan->fin.push_back(tn_sector_gemm{n, n, n, w.q + n * n, w.v + n * n, w.r});
+    plan->fin.push_back(tn_sector_gemm{n, n, n, w.q + n * n, w.r + n * n, w.v});
     tab.push_back(n);
     tab.push_back(w.g);
+    tab.push_back(w.g2);
     tab.push_back(w.t);
     SvdJob j1;
     j1.a_off = s.a_off;
@@ -202,10 +210,10 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     j1.id = (int)i;
     SvdJob j1b = j1;
     j1b.a_off = w.x1;
-    j1b.v_off = w.q;
+    j1b.v_off = w.v;
     SvdJob j2 = j1;
     j2.a_off = w.x2;
-    j2.v_off = w.r;  // (Q1 Q2)^T
+    j2.v_off = w.v;  // (Q1 Q2)^T
     j2.b = g.b;
     j2.L = g.L;
     Acc& c1 = cls1[{g1.P, g1.K}];
@@ -245,7 +253,7 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     plan->jobs2 = upload(ctx, all2.data(), all2.size() * sizeof(SvdJob));
     plan->ns_tab = upload(ctx, tab.data(), tab.size() * sizeof(int64_t));
     std::vector<int64_t> trs;
-    for (int k = 0; k < 4; k++) trs.insert(trs.end(), tr[k].begin(), tr[k].end());
+    for (int k = 0; k < 3; k++) trs.insert(trs.end(), tr[k].begin(), tr[k].end());
     plan->tr_tab = upload(ctx, trs.data(), trs.size() * sizeof(int64_t));
     TN_CUDA(cudaStreamSynchronize(ctx.stream));
   }
@@ -329,9 +337,11 @@ void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const dou
     };
     const int nj = (int)plan->jac.size();
     const int64_t* tab = (const int64_t*)plan->ns_tab->ptr;
-    auto ns = [&](const std::vector<tn_sector_gemm>& gram, const std::vector<tn_sector_gemm>& prod, int step) {
+    auto ns = [&](const std::vector<tn_sector_gemm>& gram, const std::vector<tn_sector_gemm>* sq,
+                  const std::vector<tn_sector_gemm>& prod, int step) {
       run_sector_gemms(ctx, TN_MODE_FP64, gram, ws, ws, ws);
-      launch_ns_factor(tab, nj, ws, ctx.stream);
+      if (sq) run_sector_gemms(ctx, TN_MODE_FP64, *sq, ws, ws, ws);
+      launch_ns_factor(tab, nj, ws, sq ? 3 : 2, ctx.stream);
       ctx.launched();
       run_sector_gemms(ctx, TN_MODE_FP64, prod, ws, ws, ws);
       launch_ns_transpose((const int64_t*)plan->tr_tab->ptr + 3 * (int64_t)nj * step, nj, ws, ctx.stream);
@@ -343,15 +353,14 @@ void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const dou
     // orthogonal, rotates by small angles and is accurate relative to each
     // column, so the FP64 stage starts near 1e-5 and needs two rotating
     // sweeps and a confirming one.
-    stage(1, 0);  // FP32 sweeps on A: V, V^T
-    ns(plan->gram1, plan->prod1, 0);
-    ns(plan->gram2, plan->prod2, 1);  // Q1 in V
+    stage(1, 0);                                     // FP32 sweeps on A: V, V^T
+    ns(plan->gram1, nullptr, plan->prod1, 0);
+    ns(plan->gram2, nullptr, plan->prod2, 1);        // Q1 in R
     if (!plan->x1_a.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_a, A, ws, ws);
     if (!plan->x1_b.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_b, ws, A, ws);
-    stage(1, 1);  // FP32 sweeps on X1
-    ns(plan->gram3, plan->prod3, 2);
-    ns(plan->gram4, plan->prod4, 3);  // Q2 in Q
-    run_sector_gemms(ctx, TN_MODE_FP64, plan->fin, ws, ws, ws);  // X2, (Q1 Q2)^T
+    stage(1, 1);                                     // FP32 sweeps on X1: V, V^T
+    ns(plan->gram3, &plan->sq3, plan->prod3, 2);     // Q2 in Q
+    run_sector_gemms(ctx, TN_MODE_FP64, plan->fin, ws, ws, ws);  // X2, (Q1 Q2)^T in V
     stage(2, 0);  // FP64 sweeps on [X2 | Q1 Q2]: U, S, VT
   }
   for (int i : plan->fallback) {

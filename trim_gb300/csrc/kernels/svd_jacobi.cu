@@ -21,14 +21,22 @@ namespace {
 
 using svdk::warp_sum_i;
 
-// T = 3/2 I - (G + G^T) / 4 per sector: the symmetric factor of a
-// Newton-Schulz step Q <- Q T
-__global__ void ns_factor_kernel(const int64_t* __restrict__ tab, int njobs, double* __restrict__ ws) {
+// The symmetric factor T of a Newton-Schulz step Q <- Q T per sector, tab =
+// (n, G, G2, T offsets), G = Q^T Q and G2 = G G symmetrised: second order
+// (order 2) T = 3/2 I - (G + G^T)/4, third order T = (15 I - 5 (G + G^T)
+// + 3/2 (G2 + G2^T)) / 8
+__global__ void ns_factor_kernel(const int64_t* __restrict__ tab, int njobs, int order, double* __restrict__ ws) {
   const int j = blockIdx.y;
-  const int64_t n = tab[3 * j], g = tab[3 * j + 1], t = tab[3 * j + 2];
+  const int64_t n = tab[4 * j], g = tab[4 * j + 1], g2 = tab[4 * j + 2], t = tab[4 * j + 3];
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < n * n; e += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = e / n, c = e % n;
-    ws[t + e] = (r == c ? 1.5 : 0.0) - 0.25 * (ws[g + r * n + c] + ws[g + c * n + r]);
+    const double gs = ws[g + r * n + c] + ws[g + c * n + r];
+    if (order == 2) {
+      ws[t + e] = fma(-0.25, gs, r == c ? 1.5 : 0.0);
+    } else {
+      const double g2s = ws[g2 + r * n + c] + ws[g2 + c * n + r];
+      ws[t + e] = fma(0.1875, g2s, fma(-0.625, gs, r == c ? 1.875 : 0.0));
+    }
   }
 }
 
@@ -185,9 +193,9 @@ int svd_max_cluster() {
   return best;
 }
 
-void launch_ns_factor(const int64_t* tab, int njobs, double* ws, cudaStream_t s) {
+void launch_ns_factor(const int64_t* tab, int njobs, double* ws, int order, cudaStream_t s) {
   if (njobs == 0) return;
-  ns_factor_kernel<<<dim3(16, (unsigned)njobs), 256, 0, s>>>(tab, njobs, ws);
+  ns_factor_kernel<<<dim3(16, (unsigned)njobs), 256, 0, s>>>(tab, njobs, order, ws);
   TN_CUDA(cudaGetLastError());
 }
 

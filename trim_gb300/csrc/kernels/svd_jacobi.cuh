@@ -6,12 +6,13 @@
 // nx <= mx) is the block A or its transpose.  Pairs of columns of X are
 // rotated until every pair is orthogonal to a tolerance; X V = U diag(sigma)
 // then holds with sigma_j = ||x_j|| and V the product of the rotations,
-// accumulated in the same records.  GB300 issues one warp-wide FP64 FMA per
-// 64 cycles per SM sub-partition (2 per clock per SM), so the sweeps that take
-// the columns from random to nearly orthogonal run in FP32 (stage 1, tolerance
-// 1e-5), twice: on A, and, after the host has made the FP32 rotation product
-// exactly orthogonal in FP64 (two Newton-Schulz steps Q <- Q (3 I - Q^T Q) / 2
-// as grouped FP64 GEMMs), on X1 = A Q1, whose nearly orthogonal columns the
+// accumulated in the same records.  GB300 runs FP64 at 2 FMAs per clock per
+// SM, and one warp issues an FP64 instruction only every 64 cycles, so the
+// sweeps that take the columns from random to nearly orthogonal run in FP32
+// (stage 1, tolerance 1e-5), twice: on A, and, after the host has made the
+// FP32 rotation product exactly orthogonal in FP64 (one third-order
+// Newton-Schulz step Q <- Q (15 I - 10 Q^T Q + 3 (Q^T Q)^2) / 8 as grouped
+// FP64 GEMMs), on X1 = A Q1, whose nearly orthogonal columns the
 // second pass rotates by small angles, accurately relative to each column
 // (the first pass cannot resolve the columns of the small singular values
 // against the FP32 rounding of the large ones).  Stage 2 runs FP64 sweeps on
