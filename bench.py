@@ -633,6 +633,18 @@ def itebd_section(args, torch, tu, stream, flush, local, rank, world):
                         if svd["ms_cpu_port"] is not None and cpu else None}}
 
 
+def svd_section(args, torch, tu, stream, flush, rank, world):
+    """The SVD / truncation of the iTEBD update alone: theta from the FP64
+    network, then the batched SVD with the global truncation and Block::eigh
+    of the same blocks (the eigendecomposition runs on the same solver)."""
+    spec, els = itebd_inputs()
+    names, dev, net = _itebd_device(tu, spec, els)
+    theta64 = net.launch("fp64").get_elem()
+    return {"workload": "itebd_theta_svd_truncate", "blocks": "19 sectors up to 130x130, chi 1024 -> 512",
+            "svd_truncate": itebd_svd_section(args, torch, tu, stream, flush, spec, els, theta64, rank, world),
+            "eigh": itebd_eigh_section(args, torch, tu, stream, flush, spec, els, theta64, rank, world)}
+
+
 def itebd_eigh_section(args, torch, tu, stream, flush, spec, els, theta64, rank, world):
     """Block::eigh of every (square) sector of the iTEBD theta, lower triangle
     read as dsyev 'U' reads the reference's row-major buffer: one batched call
@@ -1112,6 +1124,9 @@ def gpu_main(args, rank, local, world):
     if wanted == "ipeps":
         emit(ipeps_section(args, torch, tu, stream))
         return
+    if wanted == "svd":
+        emit(svd_section(args, torch, tu, stream, flush, rank, world))
+        return
 
     # headline: MERA chi=24 split vs FP64, then the other workloads as sections
     modes, e2e, roof = mera_section(args, torch, tu, stream, local, world, peaks)
@@ -1160,7 +1175,7 @@ def main():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="all", choices=["all", "mera", "itebd", "permute", "batched", "ipeps", "u1"],
+    ap.add_argument("--workload", default="all", choices=["all", "mera", "itebd", "permute", "batched", "ipeps", "u1", "svd"],
                     help="all: the MERA headline line with every other workload as a section; mera: the headline "
                          "alone; the others print that section alone")
     ap.add_argument("--mode", default="split", choices=["split", "bf16", "split_tiled"],
