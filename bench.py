@@ -227,7 +227,7 @@ def roofline_of(torch, prof, steps_done, peaks, sustained):
     measured HBM copy rate."""
     dname, d = max(prof.items(), key=lambda kv: kv[1]["ms"])
     avg_ms = d["ms"] / max(d["launches"], 1)
-    if dname in ("permute", "tc_slice"):
+    if dname in ("permute", "tc_slice", "tc_maxima"):
         ach = d["bytes"] / d["launches"] / (avg_ms * 1e-3) / 1e9
         peak = peaks.get("hbm_gbs", 6800.0)
         roof = {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s",

@@ -418,9 +418,14 @@ void launch_copy_list(const CopyList& L, int grid, cudaStream_t s);
 // cannot address it (pageable memory: then it takes a copy engine)
 const double* mapped_host(const void* host);
 void launch_fill(double* p, int64_t n, double v, cudaStream_t s);
-void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
-                    int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,
-                    unsigned long long* bmax, int64_t nmax, uint8_t* images, int num_sms, cudaStream_t s);
+// the row / column maxima of the operands (zeroed first), then their slice images
+void launch_tc_maxima(const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
+                      int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,
+                      unsigned long long* bmax, int64_t nmax, int num_sms, cudaStream_t s);
+void launch_tc_slices(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles,
+                      const int64_t* b_ts, int64_t b_tiles, const double* A, const double* B,
+                      const unsigned long long* amax, const unsigned long long* bmax, uint8_t* images, int num_sms,
+                      cudaStream_t s);
 size_t tc_gemm_smem(int ns);
 void launch_tc_gemm(int ns, const TcSector* secs, const int4* items, int nitems, const uint8_t* ws,
                     const unsigned long long* ea, const unsigned long long* eb, double* C, double* part, int* err,

@@ -188,11 +188,19 @@ void run_tc_gemms(Ctx& ctx, int ns, const std::vector<tn_sector_gemm>& list, con
   uint8_t* images = ws + max_bytes;
   double* part = (double*)(images + img_bytes);
   int* err = ctx.device_error_word();
+  const int64_t* ats = (const int64_t*)(mb + P->off_at);
+  const int64_t* bts = (const int64_t*)(mb + P->off_bt);
   {
-    ProfScope ps(ctx, "tc_slice", 2 * P->in_bytes + (double)P->img, 0);
-    launch_tc_prep(ns, dsecs, P->nsec, (const int64_t*)(mb + P->off_at), P->a_tiles, (const int64_t*)(mb + P->off_bt),
-                   P->b_tiles, A, B, ea, eb, P->rows + P->cols, images, ctx.num_sms, ctx.stream);
-    ctx.launched(2);
+    ProfScope ps(ctx, "tc_maxima", P->in_bytes, 0);
+    launch_tc_maxima(dsecs, P->nsec, ats, P->a_tiles, bts, P->b_tiles, A, B, ea, eb, P->rows + P->cols, ctx.num_sms,
+                     ctx.stream);
+    ctx.launched();
+  }
+  {
+    ProfScope ps(ctx, "tc_slice", P->in_bytes + (double)P->img, 0);
+    launch_tc_slices(ns, dsecs, P->nsec, ats, P->a_tiles, bts, P->b_tiles, A, B, ea, eb, images, ctx.num_sms,
+                     ctx.stream);
+    ctx.launched();
   }
   {
     ProfScope ps(ctx, ns == 7 ? "tc_gemm_split" : (ns == 2 ? "tc_gemm_tf32" : "tc_gemm_bf16"), 0, P->flops);

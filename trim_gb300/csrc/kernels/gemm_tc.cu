@@ -523,13 +523,19 @@ __global__ void __launch_bounds__(256) tc_reduce(const TcSector* __restrict__ se
 }  // namespace
 
 // ---------------------------------------------------------------- launchers
-void launch_tc_prep(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
-                    int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,
-                    unsigned long long* bmax, int64_t nmax, uint8_t* images, int num_sms, cudaStream_t s) {
+void launch_tc_maxima(const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles, const int64_t* b_ts,
+                      int64_t b_tiles, const double* A, const double* B, unsigned long long* amax,
+                      unsigned long long* bmax, int64_t nmax, int num_sms, cudaStream_t s) {
   TN_CUDA(cudaMemsetAsync(amax, 0, (size_t)nmax * sizeof(unsigned long long), s));  // bmax follows amax
   int g1 = (int)std::min<int64_t>(a_tiles + b_tiles, (int64_t)num_sms * 8);
   tc_maxima<<<g1, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax);
   TN_CUDA(cudaGetLastError());
+}
+
+void launch_tc_slices(int ns, const TcSector* secs, int nsec, const int64_t* a_ts, int64_t a_tiles,
+                      const int64_t* b_ts, int64_t b_tiles, const double* A, const double* B,
+                      const unsigned long long* amax, const unsigned long long* bmax, uint8_t* images, int num_sms,
+                      cudaStream_t s) {
   int g2 = (int)std::min<int64_t>(a_tiles + b_tiles, (int64_t)num_sms * 8);
   if (ns == 7)
     tc_slices<7><<<g2, 256, 0, s>>>(secs, a_ts, b_ts, nsec, a_tiles, b_tiles, A, B, amax, bmax, images);
