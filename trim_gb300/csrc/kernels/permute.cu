@@ -305,6 +305,52 @@ __device__ __forceinline__ void store_tile(const TileInfo& w, const T* buf, T* _
     walk3(a, b, c, [&](int m, int64_t g) { d0[g] = apply_flip(buf[m], f); });
     return;
   }
+  if constexpr (sizeof(T) == 8) {
+    // 16-byte stores: x is the destination-contiguous dim (dx = 1); with a
+    // 16-byte aligned destination, an even base offset, an even row step and
+    // an even tile width every pair (x, x+1),
+    // x even, is one aligned 16-byte request, read from shared memory as two
+    // 8-byte values (the odd pitch of a transpose tile leaves pairs unaligned
+    // there)
+    if ((w.mode == 0 || w.mode == 1) && w.dx == 1 && ((w.bd | w.dy) & 1) == 0 && (w.tx & 1) == 0 &&
+        ((uintptr_t)dst & 15) == 0) {
+      const int pitch = w.mode == 0 ? w.tx : w.tx + 1;
+      const int hx = w.tx >> 1;  // pairs per tile row
+      const uint64_t fl = f.re;
+      auto put = [&](int yy, int xx) {
+        const T* sp = buf + yy * pitch + xx;
+        T* g = dst + w.bd + (int64_t)yy * w.dy + xx;
+        if (xx + 1 < w.nx) {
+          double2 v;
+          v.x = flip_sign(sp[0], fl);
+          v.y = flip_sign(sp[1], fl);
+          *(double2*)g = v;
+        } else {
+          *g = flip_sign(sp[0], fl);
+        }
+      };
+      if (hx >= kThreads) {  // long rows
+        for (int yy = 0; yy < w.ny; yy++)
+          for (int xx = 2 * threadIdx.x; xx < w.nx; xx += 2 * kThreads) put(yy, xx);
+        return;
+      }
+      const int q = kThreads / hx, r = kThreads - q * hx;
+      int yy = threadIdx.x / hx, xp = threadIdx.x - (threadIdx.x / hx) * hx;
+      if (r == 0) {  // constant step: q whole rows
+        if (2 * xp < w.nx)
+          for (; yy < w.ny; yy += q) put(yy, 2 * xp);
+        return;
+      }
+      for (int k = 0; k < kPerThread; k++) {
+        if (yy >= w.ny) break;
+        if (2 * xp < w.nx) put(yy, 2 * xp);
+        xp += r;
+        yy += q;
+        if (xp >= hx) { xp -= hx; yy++; }
+      }
+      return;
+    }
+  }
   if (w.mode == 0 && w.tx >= kThreads) {  // long rows, as loaded
     for (int yy = 0; yy < w.ny; yy++) {
       const T* sp = buf + yy * w.tx + threadIdx.x;
