@@ -10,19 +10,21 @@
 // On GB300 the FP64 pipe (~1.2 TFLOP/s for the whole chip) is the bound, not
 // memory, so no FMA lane may be spent on padding: an output tile has 512
 // entries laid out to the sector's width, tn = 32, 16, 8 or 4 columns by
-// 512/tn rows (GemmTile::tn, chosen by the planner).  Lane l of a warp owns
-// column l % tn and rows (l / tn) + i * (32 / tn), i < 4, of the warp's
-// 4 * 32/tn rows; A is broadcast across the lanes of a row, B rows are
-// coalesced.  Items split along K write partial tiles to a workspace; the
+// 512/tn rows (GemmTile::tn, chosen by the planner).  The tile's rows form
+// 16 groups of 32/tn consecutive rows, dealt to the 4 warps in turn (group
+// 4 i + w to warp w), so a tile cut short by the sector's last row leaves the
+// 4 warps -- one per SM sub-partition and FP64 pipe -- nearly equal work.
+// Lane l of a warp owns column l % tn and row l / tn of each of its groups;
+// A is broadcast across the lanes of a row, B rows are coalesced.  Items split along K write partial tiles to a workspace; the
 // last CTA of each split tile (or, without counters, a second kernel) sums
 // them in split order, so the result is deterministic.
 //
 // Consecutive launches on a stream (the chain of contractions of a network)
-// use programmatic dependent launch: a CTA first lets the next grid launch,
-// then waits (griddepcontrol.wait) for the previous grid to complete and its
-// writes to be visible before it touches global memory, so the next launch's
-// set-up overlaps this one's tail while every access stays ordered.
+// use programmatic dependent launch (pdl.cuh): a CTA lets the next grid
+// launch, reads its first work item and the operand view tables (plan data),
+// and waits for the previous grid before it reads an operand or writes.
 #include "../engine/engine.h"
+#include "pdl.cuh"
 
 namespace tn {
 namespace {
@@ -47,21 +49,21 @@ __device__ __forceinline__ void fp64_tile(const GemmTile& t, const double* __res
                                           const double* __restrict__ B, double* __restrict__ C,
                                           double* __restrict__ ws, const ViewHdr* __restrict__ views,
                                           const int64_t* __restrict__ pool) {
-  constexpr int LR = 32 / TN;               // lane rows of a warp
-  constexpr int WM = LR * kRowsPerLane;     // rows of a warp
+  constexpr int LR = 32 / TN;               // rows of a group (lane rows of a warp)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int cl = lane % TN, rl = lane / TN;
-  const int wm0 = t.m0 + warp * WM;
   const int n = t.n0 + cl;
   const bool nvalid = n < t.N;
-  const int rem = t.M - wm0;
-  // row slots i with a valid row somewhere in the warp (warp-uniform)
-  const int slots = rem <= 0 ? 0 : min(kRowsPerLane, (rem + LR - 1) / LR);
+  // local row of slot i: group 4 i + warp; slots whose group starts before M (warp-uniform)
+  const int groups = (t.M - t.m0 + LR - 1) / LR;
+  const int slots = max(0, min(kRowsPerLane, (groups - warp + 3) / 4));
   double acc[kRowsPerLane] = {0.0, 0.0, 0.0, 0.0};
+  if (slots == 0) pdl_wait();  // the partial-tile store below writes
   if (slots > 0) {
     int mrow[kRowsPerLane];
 #pragma unroll
-    for (int i = 0; i < kRowsPerLane; i++) mrow[i] = min(wm0 + rl + i * LR, t.M - 1);  // rows past M: dropped
+    for (int i = 0; i < kRowsPerLane; i++)
+      mrow[i] = min(t.m0 + (4 * i + warp) * LR + rl, t.M - 1);  // rows past M: dropped
     const ViewHdr* av = t.a_vw >= 0 ? views + t.a_vw : nullptr;
     const ViewHdr* bv = t.b_vw >= 0 ? views + t.b_vw : nullptr;
     // K is walked in segments: the column tuples of a viewed A (the row
@@ -74,6 +76,7 @@ __device__ __forceinline__ void fp64_tile(const GemmTile& t, const double* __res
     const int ncol = nvalid ? n : 0;
     const int cj = bv ? find_start(pool + bv->cs, bv->nc, ncol) : 0;
     int sidx = seg ? find_start(seg, nseg, t.k0) : 0;
+    pdl_wait();  // A and B may be written by the previous grid
     for (int k0 = t.k0; k0 < t.k1; sidx++) {
       const int k1 = seg ? (int)min((int64_t)t.k1, seg[sidx + 1]) : t.k1;
       const int64_t s0 = seg ? seg[sidx] : 0;
@@ -115,14 +118,14 @@ __device__ __forceinline__ void fp64_tile(const GemmTile& t, const double* __res
   if (t.nsplit == 1) {
     if (nvalid)
       for (int i = 0; i < slots; i++) {
-        const int m = wm0 + rl + i * LR;
+        const int m = t.m0 + (4 * i + warp) * LR + rl;
         if (m < t.M) C[t.c_off + (int64_t)m * t.N + n] = acc[i];
       }
   } else {
     // partial tile [512/tn rows][tn columns]
     double* p = ws + t.ws_off + (int64_t)t.split * kTileElems;
 #pragma unroll
-    for (int i = 0; i < kRowsPerLane; i++) p[(warp * WM + rl + i * LR) * TN + cl] = acc[i];
+    for (int i = 0; i < kRowsPerLane; i++) p[((4 * i + warp) * LR + rl) * TN + cl] = acc[i];
   }
 }
 
@@ -137,6 +140,7 @@ __device__ __forceinline__ void rowdot_tile(const GemmTile& t, const double* __r
                                             const double* __restrict__ B, double* __restrict__ C) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double* __restrict__ b = B + t.b_off;
+  pdl_wait();  // A and B may be written by the previous grid
   for (int r = warp; r < kRowDotRows; r += 4) {
     const int m = t.m0 + r;
     if (m >= t.M) break;  // warp-uniform
@@ -204,9 +208,9 @@ __global__ void __launch_bounds__(128) gemm_fp64_kernel(const GemmTile* __restri
                                                         double* __restrict__ ws, int* __restrict__ counters,
                                                         const ViewHdr* __restrict__ views,
                                                         const int64_t* __restrict__ pool) {
-  // no global access before the wait: the previous grid may still be running
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-  asm volatile("griddepcontrol.wait;" ::: "memory");
+  pdl_trigger();
+  // the work list and view tables are plan data, read before the wait (in
+  // the tile and row-dot paths) on the previous grid's operands
   for (int it = blockIdx.x; it < ntiles; it += gridDim.x) {
     const GemmTile t = tiles[it];
     switch (t.tn) {

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../engine/engine.h"
+#include "pdl.cuh"
 
 namespace tn {
 namespace {
@@ -419,8 +420,10 @@ __global__ void __launch_bounds__(kThreads, 2) permute_kernel(const PermSub* __r
   extern __shared__ double smem_d[];  // kStages * kSmem doubles
   T* smem = (T*)smem_d;
   __shared__ TileInfo ring[kRing];
+  pdl_trigger();
   const int64_t G = gridDim.x;
-  if (threadIdx.x < 32) decode_batch(ring, subs, tile_start, nsub, ntiles, 0);
+  if (threadIdx.x < 32) decode_batch(ring, subs, tile_start, nsub, ntiles, 0);  // plan data
+  pdl_wait();  // src may be written, and dst read, by the previous grid
   __syncthreads();
 #pragma unroll
   for (int s = 0; s < kStages - 1; s++) {
@@ -540,8 +543,7 @@ static void launch_permute_t(const PermSub* subs, const int64_t* tile_start, int
     TN_CUDA(cudaFuncSetAttribute(permute_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr = true;
   }
-  permute_kernel<T><<<grid, kThreads, smem, s>>>(subs, tile_start, nsub, ntiles, src, dst, conj);
-  TN_CUDA(cudaGetLastError());
+  launch_pdl(permute_kernel<T>, dim3(grid), dim3(kThreads), smem, s, subs, tile_start, nsub, ntiles, src, dst, conj);
 }
 
 void launch_permute_kernel(const PermSub* subs, const int64_t* tile_start, int nsub, int64_t ntiles, int esz,
