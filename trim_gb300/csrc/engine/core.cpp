@@ -204,7 +204,7 @@ DevBuf::DevBuf(size_t n, Ctx& c) : bytes(n), ctx(&c) {
 }
 
 DevBuf::~DevBuf() {
-  if (ptr) cudaFreeAsync(ptr, ctx->stream);
+  if (ptr && !parent) cudaFreeAsync(ptr, ctx->stream);
 }
 
 DevBufP Ctx::ensure_workspace(size_t bytes) {

@@ -97,6 +97,7 @@ struct DevBuf {
   void* ptr = nullptr;
   size_t bytes = 0;
   Ctx* ctx = nullptr;
+  std::shared_ptr<DevBuf> parent;  // set: ptr lies inside parent's allocation and is not freed here
   DevBuf() = default;
   DevBuf(size_t n, Ctx& c);
   ~DevBuf();
@@ -323,6 +324,15 @@ struct Ctx {
   void keep_alive(const std::shared_ptr<void>& p) {
     if (keep && p) keep->push_back(p);
   }
+  // Tensor elements allocated while a capture records work are carved from
+  // one arena (sized by counting the same launch run once before), so no
+  // graph memory node sits between two kernels and consecutive kernels keep
+  // their programmatic-launch edge.  Carved blocks are never reused within
+  // the graph; an allocation that does not fit is an ordinary one.
+  std::shared_ptr<DevBuf> elem_arena;
+  size_t elem_arena_off = 0;
+  bool elem_arena_count = false;  // count element allocations into elem_arena_need
+  size_t elem_arena_need = 0;
   bool autotune = false;            // FP64 GEMM policies timed per sector histogram
   std::unordered_map<uint64_t, Fp64Policy> tuned;
   // tensor-core modes: for a contraction the fused form fits, the faster of

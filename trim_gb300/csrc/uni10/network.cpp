@@ -543,7 +543,17 @@ void Network::drop_graph() {
 
 void Network::capture() {
   drop_graph();
-  UniTensor warm = launch();  // plans, workspace and tree in place
+  tn::Ctx& c = *tn::default_ctx();
+  c.elem_arena_count = true;  // the launch's tensor allocations, for the arena below
+  c.elem_arena_need = 0;
+  UniTensor warm;
+  try {
+    warm = launch();  // plans, workspace and tree in place
+  } catch (...) {
+    c.elem_arena_count = false;
+    throw;
+  }
+  c.elem_arena_count = false;
   // swap gates go on a tensor once, at the launch after it is put; a replay on
   // new elements would skip them
   for (const auto& sw : swaps_arr)
@@ -551,8 +561,15 @@ void Network::capture() {
   graph_out = warm;           // persistent output buffer, allocated outside the graph
   graph_sigs.clear();
   for (UniTensor* t : tensors) graph_sigs.push_back(t->sectorMap() ? t->sectorMap()->key : std::string());
-  tn::Ctx& c = *tn::default_ctx();
   c.device_error_word();
+  // intermediates in one arena owned by the graph (up to kArenaCap bytes;
+  // beyond it, graph memory nodes, which reuse freed blocks)
+  constexpr size_t kArenaCap = (size_t)1 << 30;
+  std::shared_ptr<tn::DevBuf> arena;
+  if (c.elem_arena_need > 0 && c.elem_arena_need <= kArenaCap) {
+    arena = std::make_shared<tn::DevBuf>(c.elem_arena_need, c);
+    graph_keep.push_back(arena);
+  }
   TN_CUDA(cudaStreamSynchronize(c.stream));
   // capture on a private stream (the context's may be the legacy default
   // stream, which cannot be captured); the graph is replayed on c.stream
@@ -568,6 +585,8 @@ void Network::capture() {
     TN_CUDA(began);
   }
   c.keep = &graph_keep;  // plans and workspace the recorded kernels read
+  c.elem_arena = arena;
+  c.elem_arena_off = 0;
   try {
     // bound host inputs into the put tensors.  Pinned host buffers are mapped
     // into the device's address space: then one kernel reads them all
@@ -618,6 +637,7 @@ void Network::capture() {
     }
   } catch (...) {
     c.keep = nullptr;
+    c.elem_arena = nullptr;
     graph_keep.clear();
     cudaStreamEndCapture(cap, &g);
     if (g) cudaGraphDestroy(g);
@@ -627,6 +647,7 @@ void Network::capture() {
     throw;
   }
   c.keep = nullptr;
+  c.elem_arena = nullptr;
   cudaError_t ended = cudaStreamEndCapture(cap, &g);
   c.stream = orig;
   cudaStreamDestroy(cap);

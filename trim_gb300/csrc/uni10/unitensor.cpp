@@ -45,8 +45,18 @@ static Qnum to_qnum(const tn::Q& q) { return Qnum((parityFType)q.prtf, q.u1, (pa
 
 static std::shared_ptr<DevBuf> alloc_elem(size_t n) {
   tn::Ctx& c = C();
-  auto b = std::make_shared<DevBuf>(n * sizeof(double), c);
-  return b;
+  const size_t bytes = n * sizeof(double), carved = (bytes + 255) / 256 * 256;
+  if (c.elem_arena_count) c.elem_arena_need += carved;
+  if (c.elem_arena && bytes > 0 && c.elem_arena_off + carved <= c.elem_arena->bytes) {
+    auto b = std::make_shared<DevBuf>();
+    b->ptr = (char*)c.elem_arena->ptr + c.elem_arena_off;
+    b->bytes = bytes;
+    b->ctx = &c;
+    b->parent = c.elem_arena;
+    c.elem_arena_off += carved;
+    return b;
+  }
+  return std::make_shared<DevBuf>(bytes, c);
 }
 
 static double* dptr(const std::shared_ptr<DevBuf>& b) { return b ? (double*)b->ptr : nullptr; }
