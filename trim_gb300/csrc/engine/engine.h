@@ -158,7 +158,7 @@ struct GemmTile {
 };
 
 // Planning choices of the FP64 grouped GEMM (the autotuner's search space):
-// tile width rule (0: the one of 4/8/16/32 that pads N least; 1: always 32)
+// tile width rule (0: the narrowest of 4/8/16/32 that covers N; 1: always 32)
 // and the K-split target (work items per SM).
 struct Fp64Policy {
   int tn_rule = 0;
