@@ -48,9 +48,10 @@ class Network {
   // contraction tree as brackets of tensor names, e.g. "((A B) C)"
   std::string tree();
   // Record launch() (in the current contraction mode) as a CUDA graph: one
-  // eager launch builds every plan and sizes the workspace, then the launch
-  // is captured with its intermediates as graph memory nodes and the result
-  // copied into a persistent output tensor.  replay() reruns the graph on the
+  // eager launch builds every plan, sizes the workspace and counts the
+  // intermediates' bytes, then the launch is captured with its intermediates
+  // carved from one device arena owned by the graph (graph memory nodes
+  // beyond 1 GiB) and the result copied into a persistent output tensor.  replay() reruns the graph on the
   // tensors currently put in the network, which must keep the signatures
   // they had at capture; output() is that persistent tensor.
   void capture();
