@@ -208,7 +208,9 @@ struct TcSector {
 struct SvdJob {
   int64_t a_off, v_off, u_off, s_off, vt_off;
   int32_t M, N, b, L;
-  int32_t id;  // index of the sector in the caller's list (sweep counts)
+  int32_t id;         // index of the sector in the caller's list (sweep counts)
+  int32_t vpart = 1;  // 0: the first FP32 pass on Y = R^T of the QR preconditioner: records without
+                      // a V part; out: the rotated columns in X's row order (order p at u_off)
 };
 constexpr int kSvdMaxSweeps = 40;    // FP64 stage
 constexpr int kSvdMaxSweeps32 = 20;  // FP32 stage
@@ -491,6 +493,14 @@ void launch_svd_jacobi(int stage, int pass, const SvdJob* jobs, int njobs, int P
 // the factor T of a Newton-Schulz step of order 2 or 3 for every (n, g_off,
 // g2_off, t_off) entry of tab (device)
 void launch_ns_factor(const int64_t* tab, int njobs, double* ws, int order, cudaStream_t s);
+// QR preconditioner of the first FP32 pass: per (m, n, tr, a_off, y_off,
+// p_off) of tab, Y = R^T of X's columns sorted by norm and their order p
+// (into ws); then the right-singular-vector estimate V and V^T from the pass
+// over Y, per (n, v_off) of tab (svd_jacobi.cu)
+size_t svd_qr_smem(int64_t m, int64_t n);
+size_t svd_v1_smem(int64_t n);
+void launch_svd_qr(const int64_t* tab, int njobs, const double* A, double* ws, size_t smem, cudaStream_t s);
+void launch_svd_v1(const int64_t* tab, int njobs, double* ws, size_t smem, cudaStream_t s);
 // dst = src^T (n x n) for every (n, src_off, dst_off) triple of tab (device)
 void launch_ns_transpose(const int64_t* tab, int njobs, double* ws, cudaStream_t s);
 void launch_truncate(const int64_t* s_off, const int64_t* s_cnt, int nsec, double* S, int64_t chi, int64_t* kept,
@@ -500,9 +510,11 @@ void launch_gather_truncated(const TruncSector* secs, int nsec, const double* U,
 void launch_transpose(const double* src, double* dst, int rows, int cols, cudaStream_t s);
 // all sectors of `list` in one batch; info (device, optional) receives the
 // sweeps each sector took (-1: no convergence within kSvdMaxSweeps; 0 for a
-// sector solved by the cuSOLVER fallback)
+// sector solved by the cuSOLVER fallback).  precond: sectors of 16..200
+// columns start from the QR preconditioner (FP32 Householder QR of the
+// norm-sorted columns, the first FP32 pass on R^T)
 void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const double* A, double* U, double* S,
-                     double* VT, int* info);
+                     double* VT, int* info, bool precond = true);
 // symmetric eigendecomposition of n x n sectors through the SVD of a scaled,
 // shifted positive definite copy (eigh_shift.cu): offsets of A; of the
 // shifted copy M and the scaled copy S (both in the M buffer); of E and V;

@@ -22,11 +22,11 @@ static int svd_threads(int64_t b) { return 32 * (int)std::max<int64_t>(8, b + (b
 // within shared memory and the warps of the kernel instance; larger sectors
 // take P = max_cluster with wider blocks while they fit.  P = 0: the sector
 // does not fit at all (cuSOLVER fallback).
-static SvdGeom geometry(int64_t M, int64_t N, int max_cluster, int es, int64_t bmax) {
+static SvdGeom geometry(int64_t M, int64_t N, int max_cluster, int es, int64_t bmax, int64_t rec = 0) {
   SvdGeom g;
   const int64_t mx = std::max(M, N), nx = std::min(M, N);
   if (nx <= 0 || mx > INT_MAX / 4) return g;
-  const SvdKernelCaps caps = svd_kernel_caps(es, mx + nx);
+  const SvdKernelCaps caps = svd_kernel_caps(es, rec > 0 ? rec : mx + nx);  // records [X | V], or rec entries
   if (!caps.K) return g;
   const int64_t L = 32 * (int64_t)caps.K;  // record length (padded)
   for (int P = 1; P <= max_cluster; P *= 2) {
@@ -81,14 +81,18 @@ struct SvdClass {
 // Newton-Schulz factor), X1 = A Q1, X2 = A Q1 Q2 (M x N each).
 struct SvdWs {
   int64_t v, q, r, g, g2, t, x1, x2;
+  int64_t y = -1, p = -1;  // QR preconditioner: Y = R^T (n x n) and the column order (n)
 };
 
 struct SvdPlan {
   std::vector<tn_svd_sector> list;
-  DevBufP jobs1, jobs1b, jobs2;  // FP32 passes 0 and 1, FP64 stage; grouped by class
-  DevBufP ns_tab;                // (n, g_off, g2_off, t_off) per Jacobi sector
-  DevBufP tr_tab;                // (n, src, dst) per sector for each of the 3 Newton-Schulz steps
-  std::vector<SvdClass> classes1, classes2;  // per stage, largest cluster first
+  DevBufP jobs1, jobs1p, jobs1b, jobs2;  // FP32 pass 0 on A / on R^T, pass 1, FP64 stage; grouped by class
+  DevBufP ns_tab;                        // (n, g_off, g2_off, t_off) per Jacobi sector
+  DevBufP tr_tab;                        // (n, src, dst) per sector for each of the 3 Newton-Schulz steps
+  DevBufP qr_tab, v1_tab;                // QR preconditioner: (m, n, tr, a_off, y_off, p_off), (n, v_off)
+  int nqr = 0;
+  size_t qr_smem = 0, v1_smem = 0;
+  std::vector<SvdClass> classes1, classes1p, classes1b, classes2;  // per pass, largest cluster first
   std::vector<tn_svd_sector> jac;  // the Jacobi sectors
   std::vector<SvdWs> ws;
   int64_t ws_elems = 0;
@@ -128,9 +132,9 @@ void ns_step(std::vector<tn_sector_gemm>& gram, std::vector<tn_sector_gemm>* sq,
   tr.push_back(to + n * n);
 }
 
-std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>& list) {
+std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>& list, bool precond) {
   const int maxp = svd_max_cluster();
-  const uint64_t key = hash_svd(list, maxp);
+  const uint64_t key = hash_svd(list, maxp) ^ (precond ? 0x9E3779B97F4A7C15ull : 0ull);
   auto it = ctx.svd_cache.find(key);
   if (it != ctx.svd_cache.end()) {
     auto p = std::static_pointer_cast<SvdPlan>(it->second);
@@ -146,8 +150,8 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     size_t smem = 0;
     int threads = 0;
   };
-  std::map<std::pair<int, int>, Acc> cls1, cls2;
-  std::vector<int64_t> tab, tr[3];
+  std::map<std::pair<int, int>, Acc> cls1, cls1p, cls2;
+  std::vector<int64_t> tab, tr[3], qtab, vtab;
   for (size_t i = 0; i < list.size(); i++) {
     const tn_svd_sector& s = list[i];
     if (s.M < 0 || s.N < 0) fail(TN_ERR_ARG, "svd: negative sector dimension");
@@ -162,7 +166,15 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
       plan->fallback.push_back((int)i);
       continue;
     }
-    const int64_t n = std::min(s.M, s.N), mn = s.M * s.N;
+    const int64_t n = std::min(s.M, s.N), mx = std::max(s.M, s.N), mn = s.M * s.N;
+    // the first FP32 pass on Y = R^T of the QR preconditioner (records of n
+    // entries, no V part) where its QR and the V completion fit one CTA's
+    // shared memory; below 16 columns Jacobi on A converges in a few sweeps
+    SvdGeom gp;
+    // (1 KB of the 227 KB left for the kernels' static shared memory)
+    if (precond && n >= 16 && n <= 200 && svd_qr_smem(mx, n) <= (size_t)kSvdMaxSmem - 1024 &&
+        svd_v1_smem(n) <= (size_t)kSvdMaxSmem - 1024)
+      gp = geometry(n, n, maxp, 4, 9, n);
     SvdWs w;
     w.v = plan->ws_elems;
     w.q = w.v + 2 * n * n;
@@ -173,6 +185,11 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     w.x1 = w.t + n * n;
     w.x2 = w.x1 + mn;
     plan->ws_elems = w.x2 + mn;
+    if (gp.P) {
+      w.y = plan->ws_elems;
+      w.p = w.y + n * n;
+      plan->ws_elems = w.p + n;
+    }
     plan->ws.push_back(w);
     plan->jac.push_back(s);
     // Q1 from the first FP32 pass's rotations, whose E reaches 1e-4: two
@@ -217,7 +234,25 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
     j2.b = g.b;
     j2.L = g.L;
     Acc& c1 = cls1[{g1.P, g1.K}];
-    c1.a.push_back(j1);
+    if (gp.P) {
+      SvdJob jp = j1;
+      jp.a_off = w.y;
+      jp.u_off = w.p;
+      jp.M = jp.N = (int)n;
+      jp.b = gp.b;
+      jp.L = gp.L;
+      jp.vpart = 0;
+      Acc& cp = cls1p[{gp.P, gp.K}];
+      cp.a.push_back(jp);
+      cp.smem = std::max(cp.smem, gp.smem);
+      cp.threads = std::max(cp.threads, gp.threads);
+      qtab.insert(qtab.end(), {mx, n, (int64_t)(s.M < s.N), s.a_off, w.y, w.p});
+      vtab.insert(vtab.end(), {n, w.v});
+      plan->qr_smem = std::max(plan->qr_smem, svd_qr_smem(mx, n));
+      plan->v1_smem = std::max(plan->v1_smem, svd_v1_smem(n));
+    } else {
+      c1.a.push_back(j1);
+    }
     c1.b.push_back(j1b);
     c1.smem = std::max(c1.smem, g1.smem);
     c1.threads = std::max(c1.threads, g1.threads);
@@ -231,6 +266,7 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
                    std::vector<SvdJob>& all) {
     for (auto c = by.rbegin(); c != by.rend(); ++c) {
       const std::vector<SvdJob>& jobs = second ? c->second.b : c->second.a;
+      if (jobs.empty()) continue;
       SvdClass k;
       k.P = c->first.first;
       k.K = c->first.second;
@@ -238,17 +274,23 @@ std::shared_ptr<SvdPlan> get_svd_plan(Ctx& ctx, const std::vector<tn_svd_sector>
       k.first = (int64_t)all.size();
       k.smem = c->second.smem;
       k.threads = c->second.threads;
-      if (!second) classes.push_back(k);
+      classes.push_back(k);
       all.insert(all.end(), jobs.begin(), jobs.end());
     }
   };
-  std::vector<SvdJob> all1, all1b, all2;
+  std::vector<SvdJob> all1, all1p, all1b, all2;
   group(cls1, false, plan->classes1, all1);
-  std::vector<SvdClass> unused;
-  group(cls1, true, unused, all1b);
+  group(cls1p, false, plan->classes1p, all1p);
+  group(cls1, true, plan->classes1b, all1b);
   group(cls2, false, plan->classes2, all2);
-  if (!all1.empty()) {
-    plan->jobs1 = upload(ctx, all1.data(), all1.size() * sizeof(SvdJob));
+  if (!all1b.empty()) {
+    if (!all1.empty()) plan->jobs1 = upload(ctx, all1.data(), all1.size() * sizeof(SvdJob));
+    if (!all1p.empty()) {
+      plan->jobs1p = upload(ctx, all1p.data(), all1p.size() * sizeof(SvdJob));
+      plan->qr_tab = upload(ctx, qtab.data(), qtab.size() * sizeof(int64_t));
+      plan->v1_tab = upload(ctx, vtab.data(), vtab.size() * sizeof(int64_t));
+      plan->nqr = (int)(vtab.size() / 2);
+    }
     plan->jobs1b = upload(ctx, all1b.data(), all1b.size() * sizeof(SvdJob));
     plan->jobs2 = upload(ctx, all2.data(), all2.size() * sizeof(SvdJob));
     plan->ns_tab = upload(ctx, tab.data(), tab.size() * sizeof(int64_t));
@@ -311,28 +353,42 @@ void release_solver(Ctx* c) {
 }
 
 void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const double* A, double* U, double* S,
-                     double* VT, int* info) {
+                     double* VT, int* info, bool precond) {
   if (list.empty()) return;
-  auto plan = get_svd_plan(ctx, list);
+  auto plan = get_svd_plan(ctx, list, precond);
   if (!plan->jac.empty()) {
     ProfScope ps(ctx, "svd");
     DevBuf wsb((size_t)plan->ws_elems * sizeof(double), ctx);
     double* ws = (double*)wsb.ptr;
-    // st 1: FP32 sweeps on A (pass 0) or on X1 = A Q1 (pass 1); st 2: FP64
-    // sweeps on [X2 | Q1 Q2]
+    // st 1: FP32 sweeps on A or on Y = R^T of its QR (pass 0), or on
+    // X1 = A Q1 (pass 1); st 2: FP64 sweeps on [X2 | Q1 Q2]
     auto stage = [&](int st, int pass) {
       ProfScope pst(ctx, st == 1 ? "svd_stage1_fp32" : "svd_stage2_fp64");
-      const std::vector<SvdClass>& cls = st == 1 ? plan->classes1 : plan->classes2;
-      const DevBufP& jl = st == 2 ? plan->jobs2 : (pass == 0 ? plan->jobs1 : plan->jobs1b);
-      const int nc = (int)cls.size();
-      ctx.fork(nc);
-      for (int c = 0; c < nc; c++) {
-        const SvdClass& k = cls[c];
-        const SvdJob* jobs = (const SvdJob*)jl->ptr + k.first;
-        launch_svd_jacobi(st, pass, jobs, k.njobs, k.P, k.threads, k.smem, st == 1 && pass == 0 ? A : ws, ws, ws, U,
-                          S, VT, info, ctx.side_stream(c), k.K);
-        ctx.launched();
+      struct Run {
+        const std::vector<SvdClass>* cls;
+        const DevBufP* jl;
+        const double* X;
+      };
+      std::vector<Run> runs;
+      if (st == 2) {
+        runs.push_back({&plan->classes2, &plan->jobs2, ws});
+      } else if (pass == 1) {
+        runs.push_back({&plan->classes1b, &plan->jobs1b, ws});
+      } else {
+        runs.push_back({&plan->classes1p, &plan->jobs1p, ws});
+        runs.push_back({&plan->classes1, &plan->jobs1, A});
       }
+      int nc = 0;
+      for (const Run& r : runs) nc += (int)r.cls->size();
+      ctx.fork(nc);
+      int c = 0;
+      for (const Run& r : runs)
+        for (const SvdClass& k : *r.cls) {
+          const SvdJob* jobs = (const SvdJob*)(*r.jl)->ptr + k.first;
+          launch_svd_jacobi(st, pass, jobs, k.njobs, k.P, k.threads, k.smem, r.X, ws, ws, U, S, VT, info,
+                            ctx.side_stream(c++), k.K);
+          ctx.launched();
+        }
       ctx.join(nc);
     };
     const int nj = (int)plan->jac.size();
@@ -353,7 +409,17 @@ void run_svd_sectors(Ctx& ctx, const std::vector<tn_svd_sector>& list, const dou
     // orthogonal, rotates by small angles and is accurate relative to each
     // column, so the FP64 stage starts near 1e-5 and needs two rotating
     // sweeps and a confirming one.
-    stage(1, 0);                                     // FP32 sweeps on A: V, V^T
+    if (plan->nqr) {  // Y = R^T and the column order of the preconditioned sectors
+      ProfScope pq(ctx, "svd_qr");
+      launch_svd_qr((const int64_t*)plan->qr_tab->ptr, plan->nqr, A, ws, plan->qr_smem, ctx.stream);
+      ctx.launched();
+    }
+    stage(1, 0);  // FP32 sweeps on A (V, V^T) or on Y (its rotated columns in X's order)
+    if (plan->nqr) {  // V, V^T of the preconditioned sectors: normalised, numerically zero columns completed
+      ProfScope pq(ctx, "svd_qr");
+      launch_svd_v1((const int64_t*)plan->v1_tab->ptr, plan->nqr, ws, plan->v1_smem, ctx.stream);
+      ctx.launched();
+    }
     ns(plan->gram1, nullptr, plan->prod1, 0);
     ns(plan->gram2, nullptr, plan->prod2, 1);        // Q1 in R
     if (!plan->x1_a.empty()) run_sector_gemms(ctx, TN_MODE_FP64, plan->x1_a, A, ws, ws);
@@ -413,7 +479,9 @@ void run_eigh_sectors(Ctx& ctx, const std::vector<tn_eigh_sector>& list, const d
     launch_eigh_prep(dj, nj, A, ws, scale, ctx.stream);
     ctx.launched();
   }
-  run_svd_sectors(ctx, svd, ws, ws, ws, ws, info ? sw : nullptr);
+  // the shifted matrices' Jacobi sweeps converge fast without the QR
+  // preconditioner, which would cost more than it saves here
+  run_svd_sectors(ctx, svd, ws, ws, ws, ws, info ? sw : nullptr, false);
   {
     ProfScope ps(ctx, "eigh_shift");
     launch_eigh_rows(dj, nj, ws, V, ctx.stream);

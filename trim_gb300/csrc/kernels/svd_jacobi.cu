@@ -193,6 +193,320 @@ int svd_max_cluster() {
   return best;
 }
 
+// ---- preconditioner of the first FP32 pass (Drmac and Veselic: one-sided
+// Jacobi on R^T, A P = Q R with the columns of A in decreasing norm, needs
+// about half the sweeps of Jacobi on A: 8 instead of 15 on the iTEBD theta
+// blocks)
+namespace {
+
+constexpr int kQrThreads = 512, kQrWarps = kQrThreads / 32;
+
+// padded column length of the QR's shared-memory copy: a multiple of 4
+// floats plus 4 (mod 8), so that the 16-byte loads of 8 threads on 8
+// consecutive columns fall in distinct banks
+__host__ __device__ inline int qr_pitch(int m) { return (m + 3) / 8 * 8 + 4; }
+
+// Per sector (tab: m, n, tr, a_off, y_off, p_off; X = A (m x n) or A^T when
+// tr): unpivoted Householder QR, in FP32 and shared memory, of X's columns
+// taken in decreasing norm (ties by index), scaled by a power of two to a
+// maximum in [1, 2).  A pair of threads owns the column of X in position t
+// of that order (p[t]; columns stay where they were loaded, column c at
+// xs + c pm) and keeps the squared norm of its rows k.. for the next
+// reflection: in step k pair k forms the reflection of its column
+// (double-buffered scalars, one barrier per step) and every pair t > k
+// applies it to its own column with 16-byte shared-memory accesses.
+// Out: Y = R^T (n x n row-major, lower triangular; FP64 of the FP32 values)
+// at y_off and the order p at p_off, as doubles.  One CTA per sector, n <=
+// kQrThreads / 2.
+__global__ void __launch_bounds__(kQrThreads) svd_qr_kernel(const int64_t* __restrict__ tab,
+                                                           const double* __restrict__ A, double* __restrict__ ws) {
+  extern __shared__ __align__(16) unsigned char qsm[];
+  const int64_t* t6 = tab + 6 * blockIdx.x;
+  const int m = (int)t6[0], n = (int)t6[1], pm = qr_pitch(m);
+  const bool tr = t6[2] != 0;
+  const double* a = A + t6[3];
+  double* y = ws + t6[4];
+  double* pout = ws + t6[5];
+  float* xs = reinterpret_cast<float*>(qsm);  // [n][pm]
+  float* nsq = xs + (size_t)n * pm;           // [n]
+  int* perm = reinterpret_cast<int*>(nsq + n);  // [n]
+  __shared__ double red[kQrWarps];
+  __shared__ float hh[2][3];  // alpha, v0 and v^T v of the reflection of step k, buffer k & 1
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+
+  // scale: the largest |X| to [1, 2) by a power of two (exact).  GB300 runs
+  // FP64 arithmetic at ~2 operations per clock per SM: per element the work
+  // here is integer or FP32, and no loop divides per element
+  long long bmax = 0;
+  const int mn = m * n;
+  for (int e = tid; e < mn; e += kQrThreads) bmax = max(bmax, __double_as_longlong(a[e]) & 0x7fffffffffffffffll);
+  for (int o = 16; o; o >>= 1) bmax = max(bmax, __shfl_xor_sync(0xffffffffu, bmax, o));
+  if (lane == 0) red[warp] = __longlong_as_double(bmax);
+  __syncthreads();
+  double amax = 0.0;
+  for (int w = 0; w < kQrWarps; w++) amax = max(amax, red[w]);  // non-negative finite values
+  int E = amax > 0.0 ? ((__double2hiint(amax) >> 20) & 0x7ff) : 0;
+  if (E == 0) E = 1023;  // zero or subnormal maximum: no scaling
+  const double sc = __hiloint2double((2046 - E) << 20, 0);
+
+  // X into shared memory (coalesced global reads: lanes along the contiguous
+  // index), rows m .. pm-1 zero
+  if (tr) {
+    for (int c = warp; c < n; c += kQrWarps)
+      for (int r = lane; r < pm; r += 32) xs[c * pm + r] = r < m ? (float)(a[c * m + r] * sc) : 0.0f;
+  } else {
+    for (int r = warp; r < pm; r += kQrWarps)
+      for (int c = lane; c < n; c += 32) xs[c * pm + r] = r < m ? (float)(a[r * n + c] * sc) : 0.0f;
+  }
+  __syncthreads();
+  if (tid < n) {
+    const float4* col = reinterpret_cast<const float4*>(xs + tid * pm);
+    float s0 = 0.0f, s1 = 0.0f;
+    for (int q = 0; q < pm / 4; q++) {
+      const float4 x = col[q];
+      s0 = fmaf(x.x, x.x, fmaf(x.y, x.y, s0));
+      s1 = fmaf(x.z, x.z, fmaf(x.w, x.w, s1));
+    }
+    nsq[tid] = s0 + s1;
+  }
+  __syncthreads();
+  // two threads per column: position t = tid / 2, half h = tid & 1 takes
+  // the 16-byte row chunks q = h mod 2 (and h = 0 the rows before the first
+  // chunk); the partners combine dot products and norms by one shuffle
+  const int t = tid >> 1, h = tid & 1;
+  float own2 = 0.0f;  // squared norm of rows k.. of the own column (both partners)
+  int oc = 0;
+  if (tid < n) {
+    int rk = 0;
+    const float x = nsq[tid];
+    for (int d = 0; d < n; d++) rk += (nsq[d] > x || (nsq[d] == x && d < tid)) ? 1 : 0;
+    perm[rk] = tid;
+  }
+  __syncthreads();
+  if (t < n) {
+    oc = perm[t];
+    own2 = nsq[oc];
+  }
+  float* own = xs + oc * pm;
+
+  for (int k = 0; k < n; k++) {
+    if (t == k && h == 0) {  // the reflection of the own column, rows k ..
+      const float x0 = own[k], nx = sqrtf(own2);
+      const float alpha = x0 >= 0.0f ? -nx : nx;  // no cancellation in v0 = x0 - alpha
+      const float v0 = x0 - alpha;
+      const float vv = fmaf(v0, v0, own2 - x0 * x0);
+      hh[k & 1][0] = alpha;
+      hh[k & 1][1] = v0;
+      hh[k & 1][2] = vv;
+      if (vv > 0.0f) own[k] = alpha;  // R(k, k); no other thread reads this entry
+    }
+    __syncthreads();
+    const bool act = t > k && t < n;
+    const float v0 = hh[k & 1][1], vv = hh[k & 1][2];
+    const float* vk = xs + perm[k] * pm;
+    const int r4 = (k + 4) & ~3;  // rows k+1 .. r4-1 one by one (h = 0), then 4 at a time
+    float d0 = 0.0f, d1 = 0.0f;
+    if (act && vv > 0.0f) {
+      if (h == 0) {
+        d0 = v0 * own[k];
+        for (int r = k + 1; r < r4 && r < pm; r++) d0 = fmaf(vk[r], own[r], d0);
+      }
+      for (int q = r4 / 4 + h; q < pm / 4; q += 2) {
+        const float4 v = reinterpret_cast<const float4*>(vk)[q], x = reinterpret_cast<const float4*>(own)[q];
+        d0 = fmaf(v.x, x.x, fmaf(v.y, x.y, d0));
+        d1 = fmaf(v.z, x.z, fmaf(v.w, x.w, d1));
+      }
+    }
+    float dot = d0 + d1;
+    dot += __shfl_xor_sync(0xffffffffu, dot, 1);  // every lane: the partners sum
+    float n0 = 0.0f, n1 = 0.0f;
+    if (act && vv > 0.0f) {
+      const float f = 2.0f * dot / vv;
+      if (h == 0) {
+        own[k] = fmaf(-f, v0, own[k]);
+        for (int r = k + 1; r < r4 && r < pm; r++) {
+          const float x = fmaf(-f, vk[r], own[r]);
+          own[r] = x;
+          n0 = fmaf(x, x, n0);
+        }
+      }
+      for (int q = r4 / 4 + h; q < pm / 4; q += 2) {
+        const float4 v = reinterpret_cast<const float4*>(vk)[q];
+        float4 x = reinterpret_cast<float4*>(own)[q];
+        x.x = fmaf(-f, v.x, x.x);
+        x.y = fmaf(-f, v.y, x.y);
+        x.z = fmaf(-f, v.z, x.z);
+        x.w = fmaf(-f, v.w, x.w);
+        reinterpret_cast<float4*>(own)[q] = x;
+        n0 = fmaf(x.x, x.x, fmaf(x.y, x.y, n0));
+        n1 = fmaf(x.z, x.z, fmaf(x.w, x.w, n1));
+      }
+    }
+    float nn = n0 + n1;
+    nn += __shfl_xor_sync(0xffffffffu, nn, 1);
+    if (act) own2 = vv > 0.0f ? nn : fmaxf(0.0f, own2 - own[k] * own[k]);  // no reflection: rows k+1 .. unchanged
+  }
+  __syncthreads();
+
+  // Y = R^T: Y(t, k) = R(k, t) = row k of the column in position t, k <= t
+  for (int r = warp; r < n; r += kQrWarps) {
+    const float* col = xs + perm[r] * pm;
+    for (int c = lane; c < n; c += 32) y[r * n + c] = c <= r ? (double)col[c] : 0.0;
+  }
+  for (int k = tid; k < n; k += kQrThreads) pout[k] = (double)perm[k];
+}
+
+constexpr int kV1Threads = 512, kV1Warps = kV1Threads / 32;
+
+// Per sector (tab: n, v_off): V (n x n row-major at v_off) holds the first
+// FP32 pass's rotated columns of R^T moved to the rows of X's order
+// (W = P R^T V_y): the right singular vectors of X times the singular values.
+// Columns above 1e-6 of the largest norm are normalised; each other one (a
+// numerically zero singular value, whose direction is noise) is replaced by
+// the unit vector e_k with the largest part outside the span of the columns
+// so far (the least row norm of the FP32 copy), orthogonalised twice against
+// that span (FP32; the Newton-Schulz steps that follow make V orthogonal in
+// FP64).  V^T goes to v_off + n n.  One CTA per sector.
+__global__ void __launch_bounds__(kV1Threads) svd_v1_kernel(const int64_t* __restrict__ tab, double* __restrict__ ws) {
+  extern __shared__ __align__(16) unsigned char vsm[];
+  const int n = (int)tab[2 * blockIdx.x];
+  double* v = ws + tab[2 * blockIdx.x + 1];
+  double* vt = v + (int64_t)n * n;
+  double* cn = reinterpret_cast<double*>(vsm);       // [n] column norms^2, then the column scales
+  float* vs = reinterpret_cast<float*>(cn + n);      // [n][n] column-major FP32 copy (column g at vs + g n)
+  float* rn = vs + (size_t)n * n;                    // [n] row norms^2 of vs
+  float* u = rn + n;                                 // [n] candidate
+  float* cf = u + n;                                 // [n] coefficients V^T u
+  __shared__ double redd[kV1Warps];
+  __shared__ float redf[kV1Warps];
+  __shared__ int redi[kV1Warps];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // column norms: a thread per column (consecutive threads, consecutive
+  // addresses); the scale of every column computed once (FP64 division and
+  // square root are long FP64-pipe sequences on GB300), then 2-D loops
+  double cmax = 0.0;
+  for (int g = threadIdx.x; g < n; g += kV1Threads) {
+    double s2 = 0.0;
+    for (int i = 0; i < n; i++) s2 = fma(v[i * n + g], v[i * n + g], s2);
+    cn[g] = s2;
+    cmax = fmax(cmax, s2);
+  }
+  for (int o = 16; o; o >>= 1) cmax = fmax(cmax, __shfl_xor_sync(0xffffffffu, cmax, o));
+  if (lane == 0) redd[warp] = cmax;
+  __syncthreads();
+  cmax = 0.0;
+  for (int w = 0; w < kV1Warps; w++) cmax = fmax(cmax, redd[w]);
+  const double keep = cmax * 1e-12;  // (1e-6 of the largest norm)^2
+  __syncthreads();                   // redd is reused below
+  for (int g = threadIdx.x; g < n; g += kV1Threads) cn[g] = cn[g] > keep && cn[g] > 0.0 ? 1.0 / sqrt(cn[g]) : 0.0;
+  __syncthreads();  // cn: the column scales (0: a column to complete)
+  for (int i = warp; i < n; i += kV1Warps)
+    for (int g = lane; g < n; g += 32) {
+      const double x = v[i * n + g] * cn[g];
+      v[i * n + g] = x;
+      vs[g * n + i] = (float)x;
+    }
+  __syncthreads();
+  for (int i = threadIdx.x; i < n; i += kV1Threads) {
+    float s2 = 0.0f;
+    for (int g = 0; g < n; g++) s2 = fmaf(vs[(size_t)g * n + i], vs[(size_t)g * n + i], s2);
+    rn[i] = s2;
+  }
+  __syncthreads();
+  for (int g = 0; g < n; g++) {
+    if (cn[g] > 0.0) continue;  // the same for every thread
+    float best = 3.0e38f;
+    int bk = n;
+    for (int i = threadIdx.x; i < n; i += kV1Threads)
+      if (rn[i] < best) {
+        best = rn[i];
+        bk = i;
+      }
+    for (int o = 16; o; o >>= 1) {
+      const float ob = __shfl_xor_sync(0xffffffffu, best, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bk, o);
+      if (ob < best || (ob == best && oi < bk)) {
+        best = ob;
+        bk = oi;
+      }
+    }
+    if (lane == 0) {
+      redf[warp] = best;
+      redi[warp] = bk;
+    }
+    __syncthreads();
+    best = redf[0];
+    bk = redi[0];
+    for (int w = 1; w < kV1Warps; w++)
+      if (redf[w] < best || (redf[w] == best && redi[w] < bk)) {
+        best = redf[w];
+        bk = redi[w];
+      }
+    for (int i = threadIdx.x; i < n; i += kV1Threads) u[i] = i == bk ? 1.0f : 0.0f;
+    __syncthreads();
+    for (int pass = 0; pass < 2; pass++) {  // u -= V (V^T u), twice
+      for (int c = threadIdx.x; c < n; c += kV1Threads) {
+        float s2 = 0.0f;
+        for (int i = 0; i < n; i++) s2 = fmaf(vs[(size_t)c * n + i], u[i], s2);
+        cf[c] = s2;
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < n; i += kV1Threads) {
+        float s2 = u[i];
+        for (int c = 0; c < n; c++) s2 = fmaf(-cf[c], vs[(size_t)c * n + i], s2);
+        u[i] = s2;
+      }
+      __syncthreads();
+    }
+    float s2 = 0.0f;
+    for (int i = threadIdx.x; i < n; i += kV1Threads) s2 = fmaf(u[i], u[i], s2);
+    for (int o = 16; o; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    __syncthreads();  // redf is read above by every thread
+    if (lane == 0) redf[warp] = s2;
+    __syncthreads();
+    s2 = 0.0f;
+    for (int w = 0; w < kV1Warps; w++) s2 += redf[w];
+    const float inv = s2 > 0.0f ? rsqrtf(s2) : 0.0f;
+    for (int i = threadIdx.x; i < n; i += kV1Threads) {
+      const float x = u[i] * inv;
+      vs[(size_t)g * n + i] = x;
+      v[(int64_t)i * n + g] = (double)x;
+      rn[i] = fmaf(x, x, rn[i]);
+    }
+    __syncthreads();
+  }
+  for (int g = warp; g < n; g += kV1Warps)
+    for (int i = lane; i < n; i += 32) vt[g * n + i] = v[i * n + g];
+}
+
+}  // namespace
+
+size_t svd_qr_smem(int64_t m, int64_t n) { return (size_t)n * qr_pitch((int)m) * 4 + (size_t)n * 8; }
+size_t svd_v1_smem(int64_t n) { return (size_t)n * 8 + (size_t)n * n * 4 + (size_t)n * 12; }
+
+void launch_svd_qr(const int64_t* tab, int njobs, const double* A, double* ws, size_t smem, cudaStream_t s) {
+  if (njobs == 0) return;
+  static size_t set = 0;  // the dynamic shared memory allowed so far (the attribute is per function)
+  if (smem > set) {
+    TN_CUDA(cudaFuncSetAttribute(svd_qr_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set = smem;
+  }
+  svd_qr_kernel<<<njobs, kQrThreads, smem, s>>>(tab, A, ws);
+  TN_CUDA(cudaGetLastError());
+}
+
+void launch_svd_v1(const int64_t* tab, int njobs, double* ws, size_t smem, cudaStream_t s) {
+  if (njobs == 0) return;
+  static size_t set = 0;
+  if (smem > set) {
+    TN_CUDA(cudaFuncSetAttribute(svd_v1_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set = smem;
+  }
+  svd_v1_kernel<<<njobs, kV1Threads, smem, s>>>(tab, ws);
+  TN_CUDA(cudaGetLastError());
+}
+
 void launch_ns_factor(const int64_t* tab, int njobs, double* ws, int order, cudaStream_t s) {
   if (njobs == 0) return;
   ns_factor_kernel<<<dim3(16, (unsigned)njobs), 256, 0, s>>>(tab, njobs, order, ws);

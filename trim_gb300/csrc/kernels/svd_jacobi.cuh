@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
     if (g < nx) {
       if (r < mx)
         v = (tr ? a[(size_t)g * jb.N + r] : a[(size_t)r * jb.N + g]) * sc;
-      else if (r - mx < nx)
+      else if (jb.vpart && r - mx < nx)
         v = kFinal ? Vin[jb.v_off + (size_t)g * nx + (r - mx)] : (r - mx == g ? 1.0 : 0.0);
     }
     rec[(size_t)col * L + r] = (T)v;
@@ -568,6 +568,14 @@ __global__ void __launch_bounds__(kThreads) svd_jacobi_kernel(const SvdJob* __re
     for (int col = warp; col < nb2; col += nwarps) {
       const int g = (col % b) * nblk + ((col / b) == 0 ? rank : nblk - 1 - rank);
       if (g >= nx) continue;
+      if (!jb.vpart) {
+        // Y V_y = P^T W: row i of the rotated column is row p[i] of X's order
+        // (normalised and completed by svd_v1_kernel, which writes V^T)
+        const T* x = R + (size_t)col * L;
+        const double* p = X + jb.u_off;
+        for (int i = lane; i < nx; i += 32) v[(size_t)(int)p[i] * nx + g] = (double)x[i];
+        continue;
+      }
       const T* x = R + (size_t)col * L + mx;
       for (int i = lane; i < nx; i += 32) {
         const double e = (double)x[i];
