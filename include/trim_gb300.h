@@ -217,9 +217,11 @@ typedef struct {
 } tn_svd_sector;
 
 /* All n sector SVDs in FP64 on the GPU, in one batch (one-sided Jacobi, each
- * sector on a thread-block cluster: FP32 sweeps, an FP64 orthogonalisation
- * of their rotations, a second FP32 pass on the product, FP64 sweeps; sectors
- * too large for shared memory use cuSOLVER's gesvdj).  list is a host array;
+ * sector on a thread-block cluster: FP32 sweeps -- for sectors of 16 to 200
+ * columns on R^T of an FP32 QR of the norm-sorted columns --, an FP64
+ * orthogonalisation of the resulting right vectors, a second FP32 pass on
+ * the product, FP64 sweeps; sectors too large for shared memory use
+ * cuSOLVER's gesvdj).  list is a host array;
  * A, U, S, VT are device buffers.  sweeps (host, n entries, may be NULL)
  * receives per sector the FP64 sweeps plus 100 times the FP32 sweeps of both
  * passes (0 for the cuSOLVER fallback; FP64 part -1
