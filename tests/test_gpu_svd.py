@@ -99,8 +99,17 @@ def test_svd_graded_and_rank_deficient(env):
     rank3 = rng.standard_normal((40, 3)) @ rng.standard_normal((3, 30))
     zero_col = rng.standard_normal((20, 10))
     zero_col[:, 4] = 0.0
-    mats = [graded, rank3, zero_col]
+    # sectors of >= 16 columns start from the QR preconditioner, whose V
+    # completion replaces the columns of numerically zero singular values
+    rank1 = np.outer(rng.standard_normal(60), rng.standard_normal(48))
+    zero = np.zeros((40, 40))
+    mats = [graded, rank3, zero_col, rank1, zero]
     res, _ = run_svd(env, mats)
+    for a, (u, s, vt) in zip(mats[3:], res[3:]):
+        ref = np.linalg.svd(a, compute_uv=False)
+        assert np.max(np.abs(s - ref)) <= TOL * max(ref.max(), 1e-300)
+        assert np.linalg.norm(u @ np.diag(s) @ vt - a) <= TOL * max(np.linalg.norm(a), 1e-300)
+    assert not np.any(res[4][1])  # the zero sector: zero singular values
     check_svd(graded, *res[0])
     u, s, vt = res[1]
     ref = np.linalg.svd(rank3, compute_uv=False)
