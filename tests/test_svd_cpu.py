@@ -7,6 +7,9 @@
   pair exactly once per sweep, never gives one column to two warps in the
   same sub-round, and its block exchange is a permutation of the slots.
 * The oracle's global truncation follows its stated order and normalises.
+* The QR preconditioner of the first FP32 pass, restated in numpy FP32,
+  gives a nonsingular start that two Newton-Schulz steps make orthogonal in
+  FP64, on random, graded, rank-deficient and zero blocks.
 """
 import itertools
 
@@ -153,3 +156,114 @@ def test_itebd_svd_truncate_oracle():
     # theta minus its rank-512 part: the discarded singular values
     err = np.linalg.norm(rec.elem * norm - th.elem)
     assert err == pytest.approx(np.linalg.norm(gold[512:]), rel=1e-9)
+
+
+# ---- the QR preconditioner of the first FP32 pass (svd_qr_kernel,
+# svd_v1_kernel in trim_gb300/csrc/kernels/svd_jacobi.cu), restated in numpy
+# FP32: columns sorted by decreasing norm, unpivoted Householder QR, one-sided
+# Jacobi on R^T, V = P W with the columns normalised and the numerically zero
+# ones completed by the unit vector of least row norm, orthogonalised twice.
+# The Newton-Schulz steps that follow need V nonsingular and near orthogonal.
+
+def _house_r32(x):
+    x = x.astype(np.float32).copy()
+    m, n = x.shape
+    for k in range(n):
+        s2 = np.float32(np.dot(x[k:, k], x[k:, k]))
+        x0 = x[k, k]
+        nx = np.float32(np.sqrt(s2))
+        alpha = -nx if x0 >= 0 else nx
+        v0 = np.float32(x0 - alpha)
+        vv = np.float32(v0 * v0 + (s2 - x0 * x0))
+        if vv <= 0:
+            continue
+        v = x[k:, k].copy()
+        v[0] = v0
+        for c in range(k + 1, n):
+            f = np.float32(2 * np.dot(v, x[k:, c]) / vv)
+            x[k:, c] -= f * v
+        x[k, k] = alpha
+    return np.triu(x[:n, :n])
+
+
+def _jacobi32(y, tol=1e-5, sweeps=30):
+    """One-sided Jacobi on the columns of y (FP32), cyclic order."""
+    y = y.astype(np.float32).copy()
+    n = y.shape[1]
+    for _ in range(sweeps):
+        rot = 0
+        for i in range(n - 1):
+            for j in range(i + 1, n):
+                a, b = np.dot(y[:, i], y[:, i]), np.dot(y[:, j], y[:, j])
+                g = np.dot(y[:, i], y[:, j])
+                if a <= 0 or b <= 0 or g * g <= tol * tol * a * b:
+                    continue
+                rot += 1
+                z = (b - a) / (2 * g)
+                t = np.sign(z) / (abs(z) + np.sqrt(1 + z * z)) if z != 0 else 1.0
+                c = 1 / np.sqrt(1 + t * t)
+                s = c * t
+                yi, yj = y[:, i].copy(), y[:, j].copy()
+                y[:, i], y[:, j] = c * yi - s * yj, s * yi + c * yj
+        if rot == 0:
+            break
+    return y
+
+
+def _precond_v(x):
+    n = x.shape[1]
+    p = np.argsort(-np.linalg.norm(x, axis=0), kind="stable")
+    w = _jacobi32(_house_r32(x[:, p]).T)      # Y V_y, Y = R^T
+    v = np.zeros((n, n))
+    v[p, :] = w
+    cn = np.sum(v * v, axis=0)
+    good = cn > 1e-12 * cn.max() if cn.max() > 0 else np.zeros(n, bool)
+    v[:, good] /= np.sqrt(cn[good])
+    v[:, ~good] = 0
+    vs = v.astype(np.float32)
+    for g in np.nonzero(~good)[0]:
+        k = int(np.argmin(np.sum(vs * vs, axis=1)))  # least row norm: e_k most outside the span
+        u = np.zeros(n, np.float32)
+        u[k] = 1
+        for _ in range(2):
+            u -= vs @ (vs.T @ u)
+        vs[:, g] = u / np.linalg.norm(u)
+        v[:, g] = vs[:, g]
+    return v
+
+
+def _ns2(q):
+    for _ in range(2):
+        g = q.T @ q
+        q = q @ (1.5 * np.eye(len(g)) - 0.25 * (g + g.T))
+    return q
+
+
+@pytest.mark.parametrize("kind", ["random", "graded", "rank2", "zero_col", "zero"])
+def test_qr_preconditioner_start_is_orthogonal(kind):
+    rng = np.random.default_rng(21)
+    m, n = 24, 18
+    if kind == "random":
+        x = rng.standard_normal((m, n))
+    elif kind == "graded":
+        x = rng.standard_normal((m, n)) * np.logspace(0, -9, n)
+    elif kind == "rank2":
+        x = rng.standard_normal((m, 2)) @ rng.standard_normal((2, n))
+    elif kind == "zero_col":
+        x = rng.standard_normal((m, n))
+        x[:, 5] = 0
+    else:
+        x = np.zeros((m, n))
+    q1 = _ns2(_precond_v(x))
+    assert np.max(np.abs(q1.T @ q1 - np.eye(n))) < 1e-13  # a valid start for the FP64 stages
+    # X Q1: the columns of the leading singular values (above 1e-2 of the
+    # largest) are orthogonal to FP32 accuracy; the small ones are left to the
+    # second FP32 pass and the FP64 sweeps, as without the preconditioner
+    x1 = x @ q1
+    gm = x1.T @ x1
+    d = np.sqrt(np.diag(gm))
+    big = d > 1e-2 * max(d.max(), 1e-300)
+    if big.sum() > 1:
+        off = np.abs(gm[np.ix_(big, big)]) / np.outer(d[big], d[big])
+        np.fill_diagonal(off, 0)
+        assert off.max() < 1e-3
