@@ -199,7 +199,7 @@ int svd_max_cluster() {
 // blocks)
 namespace {
 
-constexpr int kQrThreads = 512, kQrWarps = kQrThreads / 32;
+constexpr int kQrThreads = 256, kQrWarps = kQrThreads / 32;
 
 // padded column length of the QR's shared-memory copy: a multiple of 4
 // floats plus 4 (mod 8), so that the 16-byte loads of 8 threads on 8
@@ -209,15 +209,15 @@ __host__ __device__ inline int qr_pitch(int m) { return (m + 3) / 8 * 8 + 4; }
 // Per sector (tab: m, n, tr, a_off, y_off, p_off; X = A (m x n) or A^T when
 // tr): unpivoted Householder QR, in FP32 and shared memory, of X's columns
 // taken in decreasing norm (ties by index), scaled by a power of two to a
-// maximum in [1, 2).  A pair of threads owns the column of X in position t
-// of that order (p[t]; columns stay where they were loaded, column c at
-// xs + c pm) and keeps the squared norm of its rows k.. for the next
-// reflection: in step k pair k forms the reflection of its column
-// (double-buffered scalars, one barrier per step) and every pair t > k
-// applies it to its own column with 16-byte shared-memory accesses.
+// maximum in [1, 2), stored in that order (the column in position t at
+// xs + t pm).  Thread t owns that column and keeps the squared norm of its
+// rows k.. for the next reflection: in step k thread k forms the reflection
+// of its column (double-buffered scalars, one barrier per step) and every
+// thread t > k applies it to its own column with 16-byte shared-memory
+// accesses, no reductions.
 // Out: Y = R^T (n x n row-major, lower triangular; FP64 of the FP32 values)
 // at y_off and the order p at p_off, as doubles.  One CTA per sector, n <=
-// kQrThreads / 2.
+// kQrThreads.
 __global__ void __launch_bounds__(kQrThreads) svd_qr_kernel(const int64_t* __restrict__ tab,
                                                            const double* __restrict__ A, double* __restrict__ ws) {
   extern __shared__ __align__(16) unsigned char qsm[];
@@ -229,7 +229,8 @@ __global__ void __launch_bounds__(kQrThreads) svd_qr_kernel(const int64_t* __res
   double* pout = ws + t6[5];
   float* xs = reinterpret_cast<float*>(qsm);  // [n][pm]
   float* nsq = xs + (size_t)n * pm;           // [n]
-  int* perm = reinterpret_cast<int*>(nsq + n);  // [n]
+  int* perm = reinterpret_cast<int*>(nsq + n);  // [n] X's column in each position
+  int* rank = perm + n;                         // [n] the position of each column of X
   __shared__ double red[kQrWarps];
   __shared__ float hh[2][3];  // alpha, v0 and v^T v of the reflection of step k, buffer k & 1
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -249,48 +250,58 @@ __global__ void __launch_bounds__(kQrThreads) svd_qr_kernel(const int64_t* __res
   if (E == 0) E = 1023;  // zero or subnormal maximum: no scaling
   const double sc = __hiloint2double((2046 - E) << 20, 0);
 
-  // X into shared memory (coalesced global reads: lanes along the contiguous
-  // index), rows m .. pm-1 zero
+  // column norms (FP32 of the scaled values: only their order is used), by
+  // coalesced global reads (lanes along the contiguous index), summed in a
+  // fixed order
   if (tr) {
-    for (int c = warp; c < n; c += kQrWarps)
-      for (int r = lane; r < pm; r += 32) xs[c * pm + r] = r < m ? (float)(a[c * m + r] * sc) : 0.0f;
-  } else {
-    for (int r = warp; r < pm; r += kQrWarps)
-      for (int c = lane; c < n; c += 32) xs[c * pm + r] = r < m ? (float)(a[r * n + c] * sc) : 0.0f;
-  }
-  __syncthreads();
-  if (tid < n) {
-    const float4* col = reinterpret_cast<const float4*>(xs + tid * pm);
-    float s0 = 0.0f, s1 = 0.0f;
-    for (int q = 0; q < pm / 4; q++) {
-      const float4 x = col[q];
-      s0 = fmaf(x.x, x.x, fmaf(x.y, x.y, s0));
-      s1 = fmaf(x.z, x.z, fmaf(x.w, x.w, s1));
+    for (int c = warp; c < n; c += kQrWarps) {
+      float s2 = 0.0f;
+      for (int r = lane; r < m; r += 32) {
+        const float x = (float)(a[c * m + r] * sc);
+        s2 = fmaf(x, x, s2);
+      }
+      for (int o = 16; o; o >>= 1) s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      if (lane == 0) nsq[c] = s2;
     }
-    nsq[tid] = s0 + s1;
+  } else {
+    for (int c = tid; c < n; c += kQrThreads) {  // a thread per column, the warp's loads one row
+      float s2 = 0.0f;
+      for (int r = 0; r < m; r++) {
+        const float x = (float)(a[r * n + c] * sc);
+        s2 = fmaf(x, x, s2);
+      }
+      nsq[c] = s2;
+    }
   }
   __syncthreads();
-  // two threads per column: position t = tid / 2, half h = tid & 1 takes
-  // the 16-byte row chunks q = h mod 2 (and h = 0 the rows before the first
-  // chunk); the partners combine dot products and norms by one shuffle
-  const int t = tid >> 1, h = tid & 1;
-  float own2 = 0.0f;  // squared norm of rows k.. of the own column (both partners)
-  int oc = 0;
+  // the column of X in position t of the decreasing-norm order (ties by
+  // index) goes to xs + t pm: consecutive threads own consecutive columns,
+  // so their 16-byte accesses to shared memory stay free of bank conflicts
   if (tid < n) {
     int rk = 0;
     const float x = nsq[tid];
     for (int d = 0; d < n; d++) rk += (nsq[d] > x || (nsq[d] == x && d < tid)) ? 1 : 0;
     perm[rk] = tid;
+    rank[tid] = rk;
   }
   __syncthreads();
-  if (t < n) {
-    oc = perm[t];
-    own2 = nsq[oc];
+  if (tr) {
+    for (int c = warp; c < n; c += kQrWarps) {
+      float* col = xs + rank[c] * pm;
+      for (int r = lane; r < pm; r += 32) col[r] = r < m ? (float)(a[c * m + r] * sc) : 0.0f;
+    }
+  } else {
+    for (int r = warp; r < pm; r += kQrWarps)
+      for (int c = lane; c < n; c += 32) xs[rank[c] * pm + r] = r < m ? (float)(a[r * n + c] * sc) : 0.0f;
   }
-  float* own = xs + oc * pm;
+  __syncthreads();
+  // thread t owns the column in position t and keeps the squared norm of its
+  // rows k.. for the reflection it forms in step k
+  float* own = xs + (tid < n ? tid : 0) * pm;
+  float own2 = tid < n ? nsq[perm[tid]] : 0.0f;
 
   for (int k = 0; k < n; k++) {
-    if (t == k && h == 0) {  // the reflection of the own column, rows k ..
+    if (tid == k) {  // the reflection of the own column, rows k ..
       const float x0 = own[k], nx = sqrtf(own2);
       const float alpha = x0 >= 0.0f ? -nx : nx;  // no cancellation in v0 = x0 - alpha
       const float v0 = x0 - alpha;
@@ -301,58 +312,48 @@ __global__ void __launch_bounds__(kQrThreads) svd_qr_kernel(const int64_t* __res
       if (vv > 0.0f) own[k] = alpha;  // R(k, k); no other thread reads this entry
     }
     __syncthreads();
-    const bool act = t > k && t < n;
-    const float v0 = hh[k & 1][1], vv = hh[k & 1][2];
-    const float* vk = xs + perm[k] * pm;
-    const int r4 = (k + 4) & ~3;  // rows k+1 .. r4-1 one by one (h = 0), then 4 at a time
-    float d0 = 0.0f, d1 = 0.0f;
-    if (act && vv > 0.0f) {
-      if (h == 0) {
-        d0 = v0 * own[k];
+    if (tid > k && tid < n) {
+      const float v0 = hh[k & 1][1], vv = hh[k & 1][2];
+      const float* vk = xs + k * pm;
+      const int r4 = (k + 4) & ~3;  // rows k+1 .. r4-1 one by one, then 4 at a time
+      if (vv > 0.0f) {
+        float d0 = v0 * own[k], d1 = 0.0f;
         for (int r = k + 1; r < r4 && r < pm; r++) d0 = fmaf(vk[r], own[r], d0);
-      }
-      for (int q = r4 / 4 + h; q < pm / 4; q += 2) {
-        const float4 v = reinterpret_cast<const float4*>(vk)[q], x = reinterpret_cast<const float4*>(own)[q];
-        d0 = fmaf(v.x, x.x, fmaf(v.y, x.y, d0));
-        d1 = fmaf(v.z, x.z, fmaf(v.w, x.w, d1));
-      }
-    }
-    float dot = d0 + d1;
-    dot += __shfl_xor_sync(0xffffffffu, dot, 1);  // every lane: the partners sum
-    float n0 = 0.0f, n1 = 0.0f;
-    if (act && vv > 0.0f) {
-      const float f = 2.0f * dot / vv;
-      if (h == 0) {
+        for (int q = r4 / 4; q < pm / 4; q++) {
+          const float4 v = reinterpret_cast<const float4*>(vk)[q], x = reinterpret_cast<const float4*>(own)[q];
+          d0 = fmaf(v.x, x.x, fmaf(v.y, x.y, d0));
+          d1 = fmaf(v.z, x.z, fmaf(v.w, x.w, d1));
+        }
+        const float f = 2.0f * (d0 + d1) / vv;
         own[k] = fmaf(-f, v0, own[k]);
+        float n0 = 0.0f, n1 = 0.0f;
         for (int r = k + 1; r < r4 && r < pm; r++) {
           const float x = fmaf(-f, vk[r], own[r]);
           own[r] = x;
           n0 = fmaf(x, x, n0);
         }
-      }
-      for (int q = r4 / 4 + h; q < pm / 4; q += 2) {
-        const float4 v = reinterpret_cast<const float4*>(vk)[q];
-        float4 x = reinterpret_cast<float4*>(own)[q];
-        x.x = fmaf(-f, v.x, x.x);
-        x.y = fmaf(-f, v.y, x.y);
-        x.z = fmaf(-f, v.z, x.z);
-        x.w = fmaf(-f, v.w, x.w);
-        reinterpret_cast<float4*>(own)[q] = x;
-        n0 = fmaf(x.x, x.x, fmaf(x.y, x.y, n0));
-        n1 = fmaf(x.z, x.z, fmaf(x.w, x.w, n1));
+        for (int q = r4 / 4; q < pm / 4; q++) {
+          const float4 v = reinterpret_cast<const float4*>(vk)[q];
+          float4 x = reinterpret_cast<float4*>(own)[q];
+          x.x = fmaf(-f, v.x, x.x);
+          x.y = fmaf(-f, v.y, x.y);
+          x.z = fmaf(-f, v.z, x.z);
+          x.w = fmaf(-f, v.w, x.w);
+          reinterpret_cast<float4*>(own)[q] = x;
+          n0 = fmaf(x.x, x.x, fmaf(x.y, x.y, n0));
+          n1 = fmaf(x.z, x.z, fmaf(x.w, x.w, n1));
+        }
+        own2 = n0 + n1;
+      } else {
+        own2 = fmaxf(0.0f, own2 - own[k] * own[k]);  // no reflection: rows k+1 .. unchanged
       }
     }
-    float nn = n0 + n1;
-    nn += __shfl_xor_sync(0xffffffffu, nn, 1);
-    if (act) own2 = vv > 0.0f ? nn : fmaxf(0.0f, own2 - own[k] * own[k]);  // no reflection: rows k+1 .. unchanged
   }
   __syncthreads();
 
   // Y = R^T: Y(t, k) = R(k, t) = row k of the column in position t, k <= t
-  for (int r = warp; r < n; r += kQrWarps) {
-    const float* col = xs + perm[r] * pm;
-    for (int c = lane; c < n; c += 32) y[r * n + c] = c <= r ? (double)col[c] : 0.0;
-  }
+  for (int r = warp; r < n; r += kQrWarps)
+    for (int c = lane; c < n; c += 32) y[r * n + c] = c <= r ? (double)xs[r * pm + c] : 0.0;
   for (int k = tid; k < n; k += kQrThreads) pout[k] = (double)perm[k];
 }
 
@@ -482,7 +483,7 @@ __global__ void __launch_bounds__(kV1Threads) svd_v1_kernel(const int64_t* __res
 
 }  // namespace
 
-size_t svd_qr_smem(int64_t m, int64_t n) { return (size_t)n * qr_pitch((int)m) * 4 + (size_t)n * 8; }
+size_t svd_qr_smem(int64_t m, int64_t n) { return (size_t)n * qr_pitch((int)m) * 4 + (size_t)n * 12; }
 size_t svd_v1_smem(int64_t n) { return (size_t)n * 8 + (size_t)n * n * 4 + (size_t)n * 12; }
 
 void launch_svd_qr(const int64_t* tab, int njobs, const double* A, double* ws, size_t smem, cudaStream_t s) {
