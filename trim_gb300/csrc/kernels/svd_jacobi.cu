@@ -317,33 +317,67 @@ __global__ void __launch_bounds__(kQrThreads) svd_qr_kernel(const int64_t* __res
       const float* vk = xs + k * pm;
       const int r4 = (k + 4) & ~3;  // rows k+1 .. r4-1 one by one, then 4 at a time
       if (vv > 0.0f) {
-        float d0 = v0 * own[k], d1 = 0.0f;
-        for (int r = k + 1; r < r4 && r < pm; r++) d0 = fmaf(vk[r], own[r], d0);
-        for (int q = r4 / 4; q < pm / 4; q++) {
-          const float4 v = reinterpret_cast<const float4*>(vk)[q], x = reinterpret_cast<const float4*>(own)[q];
-          d0 = fmaf(v.x, x.x, fmaf(v.y, x.y, d0));
-          d1 = fmaf(v.z, x.z, fmaf(v.w, x.w, d1));
+        // four 16-byte chunks per iteration, their loads issued together and
+        // summed into four accumulators: with one or two warps per
+        // sub-partition nothing else hides the shared-memory latency
+        const float4* v4 = reinterpret_cast<const float4*>(vk);
+        float4* o4 = reinterpret_cast<float4*>(own);
+        const int q0 = r4 / 4, qe = pm / 4;
+        float d[4] = {v0 * own[k], 0.0f, 0.0f, 0.0f};
+        for (int r = k + 1; r < r4 && r < pm; r++) d[0] = fmaf(vk[r], own[r], d[0]);
+        int q = q0;
+        for (; q + 4 <= qe; q += 4) {
+          float4 v[4], x[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            v[u] = v4[q + u];
+            x[u] = o4[q + u];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            d[u] = fmaf(v[u].x, x[u].x, fmaf(v[u].y, x[u].y, fmaf(v[u].z, x[u].z, fmaf(v[u].w, x[u].w, d[u]))));
         }
-        const float f = 2.0f * (d0 + d1) / vv;
+        for (; q < qe; q++) {
+          const float4 v = v4[q], x = o4[q];
+          d[0] = fmaf(v.x, x.x, fmaf(v.y, x.y, fmaf(v.z, x.z, fmaf(v.w, x.w, d[0]))));
+        }
+        const float f = 2.0f * ((d[0] + d[1]) + (d[2] + d[3])) / vv;
         own[k] = fmaf(-f, v0, own[k]);
-        float n0 = 0.0f, n1 = 0.0f;
+        float nn[4] = {0.0f, 0.0f, 0.0f, 0.0f};
         for (int r = k + 1; r < r4 && r < pm; r++) {
           const float x = fmaf(-f, vk[r], own[r]);
           own[r] = x;
-          n0 = fmaf(x, x, n0);
+          nn[0] = fmaf(x, x, nn[0]);
         }
-        for (int q = r4 / 4; q < pm / 4; q++) {
-          const float4 v = reinterpret_cast<const float4*>(vk)[q];
-          float4 x = reinterpret_cast<float4*>(own)[q];
+        q = q0;
+        for (; q + 4 <= qe; q += 4) {
+          float4 v[4], x[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            v[u] = v4[q + u];
+            x[u] = o4[q + u];
+          }
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            x[u].x = fmaf(-f, v[u].x, x[u].x);
+            x[u].y = fmaf(-f, v[u].y, x[u].y);
+            x[u].z = fmaf(-f, v[u].z, x[u].z);
+            x[u].w = fmaf(-f, v[u].w, x[u].w);
+            o4[q + u] = x[u];
+            nn[u] = fmaf(x[u].x, x[u].x, fmaf(x[u].y, x[u].y, fmaf(x[u].z, x[u].z, fmaf(x[u].w, x[u].w, nn[u]))));
+          }
+        }
+        for (; q < qe; q++) {
+          const float4 v = v4[q];
+          float4 x = o4[q];
           x.x = fmaf(-f, v.x, x.x);
           x.y = fmaf(-f, v.y, x.y);
           x.z = fmaf(-f, v.z, x.z);
           x.w = fmaf(-f, v.w, x.w);
-          reinterpret_cast<float4*>(own)[q] = x;
-          n0 = fmaf(x.x, x.x, fmaf(x.y, x.y, n0));
-          n1 = fmaf(x.z, x.z, fmaf(x.w, x.w, n1));
+          o4[q] = x;
+          nn[0] = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, nn[0]))));
         }
-        own2 = n0 + n1;
+        own2 = (nn[0] + nn[1]) + (nn[2] + nn[3]);
       } else {
         own2 = fmaxf(0.0f, own2 - own[k] * own[k]);  // no reflection: rows k+1 .. unchanged
       }
